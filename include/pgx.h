@@ -1,0 +1,310 @@
+/*
+ * pgx.h — C ABI of the GB300-native wavefront path tracer.
+ *
+ * The reference (IsaGeriler/PathGuidingDissertation) is a header-only C++
+ * class API with no FFI: `Scene` (Scene.h:76-176), `RayTracer`
+ * (Renderer.h:236-752), the `BSDF` (Materials.h:121-134) and `Light`
+ * (Lights.h:16-26) virtual interfaces, the triangle BVH (Geometry.h:268-567)
+ * and the path-vertex cache `PointBVHNode` (Renderer.h:71-234).  Each entry
+ * point below names the reference member it stands in for.  The C++ façade
+ * in pgx.hpp rebuilds the reference's class names on top of these calls.
+ *
+ * Conventions
+ *  - Every function returns an int status (PGX_OK == 0).  On failure
+ *    pgx_last_error(ctx) gives a message.  Nothing exits or asserts.
+ *  - Inputs are copied at the call; the caller keeps ownership of its
+ *    buffers.  Outputs go to caller-allocated host buffers unless the name
+ *    ends in `_device`, where device pointers are borrowed for the call.
+ *  - One context owns one CUDA stream and all device memory it allocates.
+ *    Calls on one context must not overlap; separate contexts may be used
+ *    from separate threads.
+ *  - Floating point is IEEE binary32 throughout; triangle/box intersection
+ *    reproduces the reference's arithmetic exactly (no FMA contraction).
+ */
+#ifndef PGX_H_
+#define PGX_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define PGX_OK 0
+#define PGX_ERR_INVALID_ARG 1 /* null pointer, negative size, bad enum      */
+#define PGX_ERR_OOM 2         /* device or host allocation failed           */
+#define PGX_ERR_CUDA 3        /* a CUDA runtime call failed                 */
+#define PGX_ERR_OVERFLOW 4    /* traversal stack / queue capacity exceeded  */
+#define PGX_ERR_TIMEOUT 5     /* a bounded device wait gave up              */
+#define PGX_ERR_STATE 6       /* call out of order (e.g. render w/o scene)  */
+
+/* ---- scene description --------------------------------------------------- */
+
+/* Reference `Vertex` (MyMath.h:146-149) without the Vec4 w lanes. */
+typedef struct pgx_vertex {
+    float p[3];
+    float n[3];
+    float u, v;
+} pgx_vertex;
+
+/* Reference `Triangle` inputs (Geometry.h:76-94): three vertices and the
+ * index of its material.  Edges, normal and area are derived on upload
+ * exactly as `Triangle::init` derives them. */
+typedef struct pgx_triangle {
+    pgx_vertex v[3];
+    uint32_t material;
+} pgx_triangle;
+
+/* BSDF kinds, one per reference class in Materials.h. */
+enum pgx_bsdf_kind {
+    PGX_BSDF_DIFFUSE = 0,    /* DiffuseBSDF     Materials.h:136-189 */
+    PGX_BSDF_MIRROR = 1,     /* MirrorBSDF      Materials.h:191-234 */
+    PGX_BSDF_CONDUCTOR = 2,  /* ConductorBSDF   Materials.h:236-358 */
+    PGX_BSDF_GLASS = 3,      /* GlassBSDF       Materials.h:360-440 */
+    PGX_BSDF_DIELECTRIC = 4, /* DielectricBSDF  Materials.h:442-639 */
+    PGX_BSDF_ORENNAYAR = 5,  /* OrenNayarBSDF   Materials.h:641-721 */
+    PGX_BSDF_PLASTIC = 6     /* PlasticBSDF     Materials.h:724-853 */
+};
+
+/* One material: the constructor arguments of the reference BSDF classes.
+ * `roughness` is converted to alpha = 1.62142*sqrt(roughness) as the
+ * reference constructors do (Materials.h:249,455,737).  `albedo_texture`
+ * indexes the texture table given to pgx_scene_upload (the reference's
+ * `Texture*` albedo); -1 means a 1x1 texture holding `albedo`.
+ * `emission` with positive luminance turns the material into an area light
+ * (`BSDF::addLight`, `Scene::build` Scene.h:92-100).  `layered` != 0 wraps
+ * it in the pass-through LayeredBSDF (Materials.h:855-897). */
+typedef struct pgx_material {
+    int32_t kind;
+    int32_t albedo_texture;
+    float albedo[3];
+    float eta[3];
+    float k[3];
+    float int_ior;
+    float ext_ior;
+    float roughness;
+    float sigma;
+    float emission[3];
+    int32_t layered;
+} pgx_material;
+
+/* RGB float texture (reference `Texture`, Imaging.h:23-138). */
+typedef struct pgx_texture {
+    int32_t width;
+    int32_t height;
+    const float* rgb; /* width*height*3, row-major, row 0 first */
+} pgx_texture;
+
+/* Pinhole camera as `loadScene` sets it up (SceneLoader.h:226-243):
+ * Matrix::perspective(0.001, 10000, width/height, fov) and the inverse of
+ * Matrix::lookAt(from, to, up). */
+typedef struct pgx_camera {
+    float from[3];
+    float to[3];
+    float up[3];
+    float fov_degrees;
+    int32_t width;
+    int32_t height;
+    int32_t flip_x;
+} pgx_camera;
+
+/* ---- rays and hits -------------------------------------------------------- */
+
+/* A ray.  Closest hit starts its search at t = tmax (FLT_MAX gives the
+ * reference's `IntersectionData` default, Geometry.h:247-253); any hit
+ * reports an occluder only for t in (1e-4, tmax) (Geometry.h:514-567). */
+typedef struct pgx_ray {
+    float o[3];
+    float tmax;
+    float d[3];
+    float pad;
+} pgx_ray;
+
+/* Closest hit: triangle index (-1 on a miss), distance, and the barycentric
+ * beta (u) and gamma (v); alpha = 1 - (u + v) as in Geometry.h:478-480. */
+typedef struct pgx_hit {
+    int32_t id;
+    float t;
+    float u;
+    float v;
+} pgx_hit;
+
+/* One node of a binary BVH in the reference's layout (BVHBuildNode,
+ * Geometry.h:255-261): children of an interior node are left_first and
+ * left_first + 1; a leaf (used > 0) owns tri_index[left_first ..
+ * left_first + used). */
+typedef struct pgx_bvh_node {
+    float bmin[3];
+    float bmax[3];
+    int32_t left_first;
+    int32_t used;
+} pgx_bvh_node;
+
+typedef struct pgx_bvh_stats {
+    int64_t nodes;
+    int64_t leaves;
+    int32_t max_depth;
+    int32_t max_leaf_size;
+    double sah_cost; /* sum_int A/A_root*1 + sum_leaf A/A_root*N*1.5 */
+    double build_ms;
+} pgx_bvh_stats;
+
+/* ---- rendering ---------------------------------------------------------- */
+
+enum pgx_render_mode {
+    /* `RayTracer::pathTrace` (Renderer.h:531-618): NEE + MIS, RR from
+     * depth > 3 on throughput, stop at depth 8. */
+    PGX_MODE_PLAIN = 0,
+    /* `RayTracer::guidedPath` with GUIDED_PATH (Renderer.h:368-528): image =
+     * BSDF-sampled incoming radiance, fixed RR 0.7, path vertices recorded
+     * and back-propagated; the cache is rebuilt after frames while the
+     * frame count is below 16 (Renderer.h:720-746). */
+    PGX_MODE_GUIDED_LI = 1,
+    /* Extension: plain estimator whose continuation directions are drawn
+     * by one-sample MIS between the BSDF and the radiance-cache QuadTree
+     * guide (the design sketched in Renderer.h:398-414). */
+    PGX_MODE_GUIDED_QUADTREE = 2
+};
+
+typedef struct pgx_render_config {
+    int32_t mode;          /* pgx_render_mode                              */
+    int32_t max_depth;     /* reference: 8                                 */
+    uint64_t seed;         /* PCG32 streams are hash(seed, pixel, sample)  */
+    float guide_fraction;  /* probability of sampling the guide (0.5)      */
+    int32_t record_paths;  /* keep path vertices for the cache (guided Li) */
+    int32_t reserved;
+} pgx_render_config;
+
+typedef struct pgx_render_stats {
+    int64_t paths;
+    int64_t extension_rays;
+    int64_t shadow_rays;
+    int64_t path_vertices;
+    double ms_total;
+    double ms_extend;
+    double ms_shadow;
+    double ms_shade;
+} pgx_render_stats;
+
+/* Reference `PathVertex` (Renderer.h:42-47) without the Vec4 w lanes. */
+typedef struct pgx_path_vertex {
+    float position[3];
+    float normal[3];
+    float wi[3];
+    float Li[3];
+} pgx_path_vertex;
+
+/* Point-BVH node (PointBVHNode, Renderer.h:71-81) flattened: interior
+ * nodes have left/right child indices; leaves (left == -1) own
+ * records [offset, offset + used). */
+typedef struct pgx_cache_node {
+    float bmin[3];
+    float bmax[3];
+    int32_t left;
+    int32_t right;
+    int32_t offset;
+    int32_t used;
+} pgx_cache_node;
+
+typedef struct pgx_cache_stats {
+    int64_t records;
+    int64_t nodes;
+    int64_t leaves;
+    int32_t min_leaf_depth;
+    int32_t max_leaf_depth;
+    double mean_leaf_depth;
+    double build_ms;
+} pgx_cache_stats;
+
+/* ---- context -------------------------------------------------------------- */
+
+typedef struct pgx_ctx pgx_ctx;
+
+/* Creates a context on CUDA device `device`. */
+int pgx_create(int32_t device, pgx_ctx** out);
+int pgx_destroy(pgx_ctx* ctx);
+/* Message of the last failed call on ctx ("" if none).  ctx may be NULL for
+ * failures of pgx_create. */
+const char* pgx_last_error(const pgx_ctx* ctx);
+/* Library version string. */
+const char* pgx_version(void);
+
+/* `Scene::init` (Scene.h:121-137): copies triangles, materials, textures,
+ * the optional environment map (`EnvironmentMap`, Lights.h:128-228; NULL
+ * gives the reference's black `BackgroundColour`) and the camera to the
+ * device, builds the emitter list (Scene.h:92-100), the scene bounds
+ * (SceneLoader.h:267-268) and the environment sampling tables
+ * (`Distribution2D`, Sampling.h:171-189).  Does not build the BVH. */
+int pgx_scene_upload(pgx_ctx* ctx, const pgx_triangle* tris, int64_t ntris,
+                     const pgx_material* mats, int32_t nmats,
+                     const pgx_texture* textures, int32_t ntextures,
+                     const pgx_texture* envmap, const pgx_camera* camera);
+
+/* `BVHNode::build` (Geometry.h:419-446) on the GPU: binned SAH, 16 bins per
+ * axis, leaves of at most 4 triangles unless splitting costs more. */
+int pgx_bvh_build(pgx_ctx* ctx);
+/* Installs a BVH built elsewhere (e.g. exported from the reference) in the
+ * reference layout; the traversal then visits nodes in the reference's
+ * order. */
+int pgx_bvh_import(pgx_ctx* ctx, const pgx_bvh_node* nodes, int64_t nnodes,
+                   const int32_t* tri_index);
+/* Copies the current BVH out in the reference layout.  Pass NULL buffers to
+ * query the sizes. */
+int pgx_bvh_export(pgx_ctx* ctx, pgx_bvh_node* nodes, int64_t* nnodes,
+                   int32_t* tri_index, int64_t* ntri_index);
+int pgx_bvh_get_stats(pgx_ctx* ctx, pgx_bvh_stats* out);
+
+/* `BVHNode::traverse` (Geometry.h:448-512) for a batch of host rays. */
+int pgx_trace_closest(pgx_ctx* ctx, const pgx_ray* rays, int64_t n, pgx_hit* hits);
+/* `BVHNode::traverseVisible` (Geometry.h:514-567): visible[i] = 1 when no
+ * triangle is hit in (1e-4, tmax). */
+int pgx_trace_any(pgx_ctx* ctx, const pgx_ray* rays, int64_t n, uint8_t* visible);
+/* Device-pointer variants on a caller stream (cudaStream_t or NULL). */
+int pgx_trace_closest_device(pgx_ctx* ctx, const pgx_ray* d_rays, int64_t n,
+                             pgx_hit* d_hits, void* stream);
+int pgx_trace_any_device(pgx_ctx* ctx, const pgx_ray* d_rays, int64_t n,
+                         uint8_t* d_visible, void* stream);
+/* Node/triangle fetch counters of the last trace call (algorithmic bytes). */
+int pgx_trace_counters(pgx_ctx* ctx, int64_t* nodes_visited, int64_t* tris_tested);
+
+/* Camera rays (`Camera::generateRay`, Scene.h:253-265) for pixel sample
+ * positions px, py (n of each). */
+int pgx_camera_rays(pgx_ctx* ctx, const float* px, const float* py, int64_t n, pgx_ray* rays);
+
+/* `RayTracer::render` (Renderer.h:648-747) called `frames` times: each frame
+ * is one sample per pixel accumulated into the film. */
+int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t frames);
+/* `RayTracer::clear` (Renderer.h:265-267). */
+int pgx_clear(pgx_ctx* ctx);
+/* `RayTracer::getSPP` (Renderer.h:749). */
+int pgx_get_spp(pgx_ctx* ctx, int32_t* spp);
+/* Film sums (`Film::film`, Imaging.h:186-217) to host: rgb = sum of samples
+ * per pixel (divide by spp for `Film::save`), rgb2 = sum of squares (may be
+ * NULL).  Both width*height*3 floats. */
+int pgx_film_read(pgx_ctx* ctx, float* rgb, float* rgb2, int32_t* spp);
+int pgx_render_get_stats(pgx_ctx* ctx, pgx_render_stats* out);
+
+/* ---- radiance cache ------------------------------------------------------ */
+
+/* `PointBVHNode::buildPointBVHNode` (Renderer.h:189-211) over host records. */
+int pgx_cache_build(pgx_ctx* ctx, const pgx_path_vertex* records, int64_t n);
+/* Builds the cache from the path vertices the last guided render kept. */
+int pgx_cache_build_from_render(pgx_ctx* ctx);
+int pgx_cache_get_stats(pgx_ctx* ctx, pgx_cache_stats* out);
+/* Copies the cache out: nodes (root first) and the records in leaf order. */
+int pgx_cache_export(pgx_ctx* ctx, pgx_cache_node* nodes, int64_t* nnodes,
+                     pgx_path_vertex* records, int64_t* nrecords);
+/* k nearest cached records to each query point (extension; the reference
+ * has no cache query).  idx is nq*k record indices into the exported record
+ * order (-1 when fewer than k exist), d2 the squared distances, ascending,
+ * ties broken by the lower index. */
+int pgx_cache_knn(pgx_ctx* ctx, const float* queries, int64_t nq, int32_t k,
+                  int32_t* idx, float* d2);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PGX_H_ */

@@ -1,0 +1,171 @@
+"""ctypes access to the oracle libraries — TEST INFRASTRUCTURE ONLY.
+
+Used by tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline
+leg as the checker / CPU baseline; the product (libpgx) never loads it.
+
+* ``Oracle`` — oracle/_build/liboracle.so, the C restatement.
+* ``Reference`` — oracle/_ref/liborcref*.so, the reference itself compiled
+  headless (available where the reference sources were staged).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+_P = C.c_void_p
+_I64 = C.c_int64
+_I32 = C.c_int32
+_U64 = C.c_uint64
+
+# numpy layouts of include/pgx.h structs (duplicated to keep the oracle
+# independent of the product package).
+VERTEX = np.dtype([("p", "<f4", 3), ("n", "<f4", 3), ("u", "<f4"), ("v", "<f4")])
+TRIANGLE = np.dtype([("v", VERTEX, 3), ("material", "<u4")])
+RAY = np.dtype([("o", "<f4", 3), ("tmax", "<f4"), ("d", "<f4", 3), ("pad", "<f4")])
+HIT = np.dtype([("id", "<i4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4")])
+BVH_NODE = np.dtype([("bmin", "<f4", 3), ("bmax", "<f4", 3), ("left_first", "<i4"), ("used", "<i4")])
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+class Oracle:
+    def __init__(self, path: str | Path | None = None):
+        if path is None:
+            from . import build as _b  # noqa: PLC0415
+            path = _b.build_oracle()
+        self.lib = C.CDLL(str(path))
+        L = self.lib
+        L.orc_bvh_build.restype = _I64
+        L.orc_bvh_build.argtypes = [_P, _I64, _P, _P]
+        L.orc_sah_cost.restype = C.c_double
+        L.orc_sah_cost.argtypes = [_P, _I64]
+        for name in ("orc_trace_closest", "orc_trace_any"):
+            fn = getattr(L, name)
+            fn.restype = None
+            fn.argtypes = [_P, _P, _P, _P, _I64, _P, C.POINTER(_I64), C.POINTER(_I64)]
+        L.orc_trace_closest_mt.restype = None
+        L.orc_trace_closest_mt.argtypes = [_P, _P, _P, _P, _I64, _P, _I32]
+        L.orc_rng_floats.restype = None
+        L.orc_rng_floats.argtypes = [_U64, _U64, _U64, _I32, _P]
+
+    def bvh_build(self, tris: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+        tris = np.ascontiguousarray(tris, TRIANGLE)
+        n = len(tris)
+        nodes = np.zeros(max(1, 2 * n - 1), BVH_NODE)
+        idx = np.zeros(max(1, n), np.int32)
+        cnt = self.lib.orc_bvh_build(_p(tris), n, _p(nodes), _p(idx))
+        return nodes[:cnt].copy(), idx[:n].copy()
+
+    def sah_cost(self, nodes: np.ndarray) -> float:
+        nodes = np.ascontiguousarray(nodes, BVH_NODE)
+        return float(self.lib.orc_sah_cost(_p(nodes), len(nodes)))
+
+    def trace_closest(self, tris, nodes, idx, rays) -> tuple[np.ndarray, int, int]:
+        tris = np.ascontiguousarray(tris, TRIANGLE)
+        nodes = np.ascontiguousarray(nodes, BVH_NODE)
+        idx = np.ascontiguousarray(idx, np.int32)
+        rays = np.ascontiguousarray(rays, RAY)
+        hits = np.zeros(len(rays), HIT)
+        a, b = _I64(0), _I64(0)
+        self.lib.orc_trace_closest(_p(tris), _p(nodes), _p(idx), _p(rays), len(rays), _p(hits), C.byref(a),
+                                   C.byref(b))
+        return hits, a.value, b.value
+
+    def trace_any(self, tris, nodes, idx, rays) -> tuple[np.ndarray, int, int]:
+        tris = np.ascontiguousarray(tris, TRIANGLE)
+        nodes = np.ascontiguousarray(nodes, BVH_NODE)
+        idx = np.ascontiguousarray(idx, np.int32)
+        rays = np.ascontiguousarray(rays, RAY)
+        vis = np.zeros(len(rays), np.uint8)
+        a, b = _I64(0), _I64(0)
+        self.lib.orc_trace_any(_p(tris), _p(nodes), _p(idx), _p(rays), len(rays), _p(vis), C.byref(a), C.byref(b))
+        return vis, a.value, b.value
+
+    def trace_closest_mt(self, tris, nodes, idx, rays, threads: int) -> np.ndarray:
+        tris = np.ascontiguousarray(tris, TRIANGLE)
+        nodes = np.ascontiguousarray(nodes, BVH_NODE)
+        idx = np.ascontiguousarray(idx, np.int32)
+        rays = np.ascontiguousarray(rays, RAY)
+        hits = np.zeros(len(rays), HIT)
+        self.lib.orc_trace_closest_mt(_p(tris), _p(nodes), _p(idx), _p(rays), len(rays), _p(hits), threads)
+        return hits
+
+    def rng_floats(self, seed: int, pixel: int, sample: int, count: int) -> np.ndarray:
+        out = np.zeros(count, np.float32)
+        self.lib.orc_rng_floats(seed, pixel, sample, count, _p(out))
+        return out
+
+
+def reference_available() -> bool:
+    return (HERE / "_ref" / "liborcref.so").exists() or (HERE / "_ref" / "src" / "Renderer.h").exists() or \
+        Path(os.environ.get("PGX_REFERENCE_DIR", "/root/reference/PathGuidingDissertation")).is_dir()
+
+
+class Reference:
+    """The reference renderer compiled headless (oracle/ref_harness.cpp)."""
+
+    def __init__(self, fast: bool = False):
+        from . import build as _b  # noqa: PLC0415
+        p = _b.build_reference()
+        if p is None:
+            raise RuntimeError("reference sources unavailable")
+        if fast:
+            p = p.parent / "liborcref_fast.so"
+        self.lib = C.CDLL(str(p))
+        L = self.lib
+        L.orcref_bvh_build.restype = _I64
+        L.orcref_bvh_build.argtypes = [_P, _I64, _P, _P]
+        L.orcref_world_create.restype = _P
+        L.orcref_world_create.argtypes = [_P, _I64]
+        L.orcref_world_destroy.restype = None
+        L.orcref_world_destroy.argtypes = [_P]
+        L.orcref_trace_closest.restype = C.c_double
+        L.orcref_trace_closest.argtypes = [_P, _P, _I64, _P, _I32]
+        L.orcref_trace_any.restype = C.c_double
+        L.orcref_trace_any.argtypes = [_P, _P, _I64, _P, _I32]
+        L.orcref_rng_floats.restype = None
+        L.orcref_rng_floats.argtypes = [_U64, _U64, _U64, _I32, _P]
+
+    def bvh_build(self, tris: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+        tris = np.ascontiguousarray(tris, TRIANGLE)
+        n = len(tris)
+        nodes = np.zeros(max(1, 2 * n - 1), BVH_NODE)
+        idx = np.zeros(max(1, n), np.int32)
+        cnt = self.lib.orcref_bvh_build(_p(tris), n, _p(nodes), _p(idx))
+        return nodes[:cnt].copy(), idx[:n].copy()
+
+    def world(self, tris: np.ndarray) -> "RefWorld":
+        return RefWorld(self, tris)
+
+
+class RefWorld:
+    def __init__(self, ref: Reference, tris: np.ndarray):
+        self.ref = ref
+        self.tris = np.ascontiguousarray(tris, TRIANGLE)
+        self.h = ref.lib.orcref_world_create(_p(self.tris), len(self.tris))
+
+    def close(self):
+        if self.h:
+            self.ref.lib.orcref_world_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def trace_closest(self, rays: np.ndarray, threads: int = 1) -> tuple[np.ndarray, float]:
+        rays = np.ascontiguousarray(rays, RAY)
+        hits = np.zeros(len(rays), HIT)
+        secs = self.ref.lib.orcref_trace_closest(self.h, _p(rays), len(rays), _p(hits), threads)
+        return hits, secs
+
+    def trace_any(self, rays: np.ndarray, threads: int = 1) -> tuple[np.ndarray, float]:
+        rays = np.ascontiguousarray(rays, RAY)
+        vis = np.zeros(len(rays), np.uint8)
+        secs = self.ref.lib.orcref_trace_any(self.h, _p(rays), len(rays), _p(vis), threads)
+        return vis, secs

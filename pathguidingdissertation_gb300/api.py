@@ -1,0 +1,255 @@
+"""Python mirror of the reference's renderer interface over the C ABI.
+
+``Context`` wraps one ``pgx_ctx``.  ``Scene`` and ``RayTracer`` keep the
+reference's names and semantics (Scene.h:76-176, Renderer.h:236-752):
+``Scene.init``/``build``/``traverse``/``visible``, ``RayTracer.init``/
+``render`` (one sample per pixel per call, accumulated)/``clear``/``getSPP``/
+``saveHDR``.  All work happens in libpgx; nothing here computes on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from .abi import PgxError, ptr
+from .scenes import SceneDesc
+
+
+class Context:
+    def __init__(self, device: int = 0, lib_path=None):
+        self.lib = abi.load(lib_path)
+        h = C.c_void_p()
+        rc = self.lib.pgx_create(device, C.byref(h))
+        if rc != abi.PGX_OK:
+            raise PgxError(rc, self.lib.pgx_last_error(None).decode())
+        self.h = h
+        self.scene: SceneDesc | None = None
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.pgx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def check(self, rc: int) -> None:
+        if rc != abi.PGX_OK:
+            raise PgxError(rc, self.lib.pgx_last_error(self.h).decode())
+
+    # ---- scene ---------------------------------------------------------------
+    def upload(self, scene: SceneDesc) -> None:
+        tris = np.ascontiguousarray(scene.triangles)
+        mats = np.ascontiguousarray(scene.materials)
+        texs = [np.ascontiguousarray(t, dtype=np.float32) for t in scene.textures]
+        tex_arr = (abi.Texture * max(1, len(texs)))()
+        for i, t in enumerate(texs):
+            tex_arr[i] = abi.Texture(t.shape[1], t.shape[0], t.ctypes.data)
+        env = None
+        env_keep = None
+        if scene.env is not None:
+            env_keep = np.ascontiguousarray(scene.env, dtype=np.float32)
+            env = abi.Texture(env_keep.shape[1], env_keep.shape[0], env_keep.ctypes.data)
+        c = scene.camera
+        cam = abi.Camera((C.c_float * 3)(*c["from_"]), (C.c_float * 3)(*c["to"]), (C.c_float * 3)(*c["up"]),
+                         float(c["fov"]), int(c["width"]), int(c["height"]), int(c.get("flip_x", 0)))
+        self.check(self.lib.pgx_scene_upload(self.h, ptr(tris), len(tris), ptr(mats), len(mats),
+                                             C.cast(tex_arr, C.c_void_p) if texs else None, len(texs),
+                                             C.byref(env) if env is not None else None, C.byref(cam)))
+        self.scene = scene
+        del env_keep, texs
+
+    def bvh_build(self) -> None:
+        self.check(self.lib.pgx_bvh_build(self.h))
+
+    def bvh_import(self, nodes: np.ndarray, idx: np.ndarray) -> None:
+        nodes = np.ascontiguousarray(nodes, abi.BVH_NODE)
+        idx = np.ascontiguousarray(idx, np.int32)
+        self.check(self.lib.pgx_bvh_import(self.h, ptr(nodes), len(nodes), ptr(idx)))
+
+    def bvh_export(self) -> tuple[np.ndarray, np.ndarray]:
+        nn, ni = C.c_int64(), C.c_int64()
+        self.check(self.lib.pgx_bvh_export(self.h, None, C.byref(nn), None, C.byref(ni)))
+        nodes = np.zeros(nn.value, abi.BVH_NODE)
+        idx = np.zeros(ni.value, np.int32)
+        self.check(self.lib.pgx_bvh_export(self.h, ptr(nodes), C.byref(nn), ptr(idx), C.byref(ni)))
+        return nodes, idx
+
+    def bvh_stats(self) -> abi.BvhStats:
+        s = abi.BvhStats()
+        self.check(self.lib.pgx_bvh_get_stats(self.h, C.byref(s)))
+        return s
+
+    # ---- rays ------------------------------------------------------------------
+    def trace_closest(self, rays: np.ndarray) -> np.ndarray:
+        rays = np.ascontiguousarray(rays, abi.RAY)
+        hits = np.zeros(len(rays), abi.HIT)
+        self.check(self.lib.pgx_trace_closest(self.h, ptr(rays), len(rays), ptr(hits)))
+        return hits
+
+    def trace_any(self, rays: np.ndarray) -> np.ndarray:
+        rays = np.ascontiguousarray(rays, abi.RAY)
+        vis = np.zeros(len(rays), np.uint8)
+        self.check(self.lib.pgx_trace_any(self.h, ptr(rays), len(rays), ptr(vis)))
+        return vis
+
+    def trace_counters(self) -> tuple[int, int]:
+        a, b = C.c_int64(), C.c_int64()
+        self.check(self.lib.pgx_trace_counters(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def camera_rays(self, px: np.ndarray, py: np.ndarray) -> np.ndarray:
+        px = np.ascontiguousarray(px, np.float32)
+        py = np.ascontiguousarray(py, np.float32)
+        out = np.zeros(len(px), abi.RAY)
+        self.check(self.lib.pgx_camera_rays(self.h, ptr(px), ptr(py), len(px), ptr(out)))
+        return out
+
+    # ---- rendering -------------------------------------------------------------
+    def render(self, frames: int = 1, mode: int = abi.MODE_PLAIN, seed: int = 1, max_depth: int = 8,
+               guide_fraction: float = 0.5, record_paths: bool = False) -> None:
+        cfg = abi.RenderConfig(mode, max_depth, seed, guide_fraction, int(record_paths), 0)
+        self.check(self.lib.pgx_render(self.h, C.byref(cfg), frames))
+
+    def clear(self) -> None:
+        self.check(self.lib.pgx_clear(self.h))
+
+    def spp(self) -> int:
+        s = C.c_int32()
+        self.check(self.lib.pgx_get_spp(self.h, C.byref(s)))
+        return s.value
+
+    def film(self, squares: bool = False) -> tuple[np.ndarray, np.ndarray | None, int]:
+        w, h = self.scene.camera["width"], self.scene.camera["height"]
+        rgb = np.zeros((h, w, 3), np.float32)
+        rgb2 = np.zeros((h, w, 3), np.float32) if squares else None
+        s = C.c_int32()
+        self.check(self.lib.pgx_film_read(self.h, ptr(rgb), ptr(rgb2), C.byref(s)))
+        return rgb, rgb2, s.value
+
+    def render_stats(self) -> abi.RenderStats:
+        s = abi.RenderStats()
+        self.check(self.lib.pgx_render_get_stats(self.h, C.byref(s)))
+        return s
+
+    # ---- radiance cache -------------------------------------------------------
+    def cache_build(self, records: np.ndarray) -> None:
+        records = np.ascontiguousarray(records, abi.PATH_VERTEX)
+        self.check(self.lib.pgx_cache_build(self.h, ptr(records), len(records)))
+
+    def cache_build_from_render(self) -> None:
+        self.check(self.lib.pgx_cache_build_from_render(self.h))
+
+    def cache_stats(self) -> abi.CacheStats:
+        s = abi.CacheStats()
+        self.check(self.lib.pgx_cache_get_stats(self.h, C.byref(s)))
+        return s
+
+    def cache_export(self) -> tuple[np.ndarray, np.ndarray]:
+        nn, nr = C.c_int64(), C.c_int64()
+        self.check(self.lib.pgx_cache_export(self.h, None, C.byref(nn), None, C.byref(nr)))
+        nodes = np.zeros(nn.value, abi.CACHE_NODE)
+        recs = np.zeros(nr.value, abi.PATH_VERTEX)
+        self.check(self.lib.pgx_cache_export(self.h, ptr(nodes), C.byref(nn), ptr(recs), C.byref(nr)))
+        return nodes, recs
+
+    def cache_knn(self, queries: np.ndarray, k: int) -> tuple[np.ndarray, np.ndarray]:
+        q = np.ascontiguousarray(queries, np.float32).reshape(-1, 3)
+        idx = np.zeros((len(q), k), np.int32)
+        d2 = np.zeros((len(q), k), np.float32)
+        self.check(self.lib.pgx_cache_knn(self.h, ptr(q), len(q), k, ptr(idx), ptr(d2)))
+        return idx, d2
+
+
+class Scene:
+    """Reference `Scene` (Scene.h:76-176) backed by a device context."""
+
+    def __init__(self, ctx: Context | None = None):
+        self.ctx = ctx or Context()
+        self.desc: SceneDesc | None = None
+
+    def init(self, desc: SceneDesc) -> None:
+        """Scene::init: triangles, materials, background (env or black)."""
+        self.desc = desc
+        self.ctx.upload(desc)
+
+    def build(self) -> None:
+        """Scene::build: BVH (on the GPU) and the light list."""
+        self.ctx.bvh_build()
+
+    def traverse(self, rays: np.ndarray) -> np.ndarray:
+        return self.ctx.trace_closest(rays)
+
+    def visible(self, p1: np.ndarray, p2: np.ndarray) -> np.ndarray:
+        """Scene::visible (Scene.h:139-146) for arrays of point pairs."""
+        p1 = np.asarray(p1, np.float32).reshape(-1, 3)
+        p2 = np.asarray(p2, np.float32).reshape(-1, 3)
+        d = p2 - p1
+        length = np.sqrt((d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]).astype(np.float32)
+        maxt = (length - np.float32(2e-4)).astype(np.float32)
+        dn = d * (np.float32(1.0) / length)[:, None]
+        rays = np.zeros(len(p1), abi.RAY)
+        rays["o"] = p1 + dn * np.float32(1e-4)
+        rays["d"] = dn
+        rays["tmax"] = maxt
+        return self.ctx.trace_any(rays).astype(bool)
+
+
+class RayTracer:
+    """Reference `RayTracer` (Renderer.h:236-752): progressive film, one
+    sample per pixel per `render()` call."""
+
+    def __init__(self, mode: int = abi.MODE_PLAIN, seed: int = 1, max_depth: int = 8):
+        self.mode = mode
+        self.seed = seed
+        self.max_depth = max_depth
+        self.scene: Scene | None = None
+
+    def init(self, scene: Scene) -> None:
+        self.scene = scene
+        self.clear()
+
+    def clear(self) -> None:
+        self.scene.ctx.clear()
+
+    def render(self) -> None:
+        self.scene.ctx.render(1, self.mode, self.seed, self.max_depth, record_paths=self.mode == abi.MODE_GUIDED_LI)
+
+    def getSPP(self) -> int:  # noqa: N802 - reference name
+        return self.scene.ctx.spp()
+
+    def saveHDR(self, filename: str) -> None:  # noqa: N802 - reference name
+        """Film::save (Imaging.h:263-272): film / SPP as Radiance HDR."""
+        rgb, _, spp = self.scene.ctx.film()
+        img = rgb * (np.float32(1.0) / np.float32(spp) if spp > 0 else np.float32(1.0))
+        write_hdr(filename, img)
+
+
+def write_hdr(filename: str, img: np.ndarray) -> None:
+    """Minimal Radiance RGBE writer (uncompressed scanlines)."""
+    h, w, _ = img.shape
+    rgb = np.asarray(img, np.float64)
+    mx = rgb.max(axis=2)
+    e = np.zeros_like(mx, dtype=np.int32)
+    m = np.zeros_like(mx)
+    nz = mx > 1e-32
+    m[nz], e[nz] = np.frexp(mx[nz])
+    scale = np.where(nz, m * 256.0 / np.where(nz, mx, 1.0), 0.0)
+    out = np.zeros((h, w, 4), np.uint8)
+    out[..., :3] = np.clip(rgb * scale[..., None], 0, 255).astype(np.uint8)
+    out[..., 3] = np.where(nz, e + 128, 0).astype(np.uint8)
+    with open(filename, "wb") as f:
+        f.write(b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n")
+        f.write(f"-Y {h} +X {w}\n".encode())
+        f.write(out.tobytes())

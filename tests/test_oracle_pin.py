@@ -1,0 +1,87 @@
+"""Pins the oracle (C restatement) to the reference: against the committed
+golden fixtures everywhere, and against the reference compiled headless
+where its sources are available."""
+from __future__ import annotations
+
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from pathguidingdissertation_gb300 import scenes
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+FIXTURES = sorted(GOLDEN.glob("traversal_*.npz"))
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=lambda p: p.stem)
+def test_oracle_bvh_matches_golden(oracle, path):
+    g = np.load(path)
+    nodes, idx = oracle.bvh_build(g["triangles"])
+    assert nodes.tobytes() == g["nodes"].tobytes()
+    assert np.array_equal(idx, g["idx"])
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=lambda p: p.stem)
+def test_oracle_hits_match_golden(oracle, path):
+    g = np.load(path)
+    hits, _, _ = oracle.trace_closest(g["triangles"], g["nodes"], g["idx"], g["rays"])
+    assert hits.tobytes() == g["hits"].tobytes()
+    vis, _, _ = oracle.trace_any(g["triangles"], g["nodes"], g["idx"], g["any_rays"])
+    assert np.array_equal(vis, g["visible"])
+
+
+SCENES = {
+    "cornell": lambda: scenes.cornell_box(seed=3),
+    "soup": lambda: scenes.triangle_soup(4000, seed=5),
+    "interior": lambda: scenes.interior(seed=9, target_tris=12000, n_objects=60, env_width=8, env_height=4),
+    "degenerate": lambda: _degenerate(),
+}
+
+
+def _degenerate():
+    # Many triangles sharing one centroid plus coplanar slabs: exercises the
+    # "all centroids equal" leaf rule and failed splits (Geometry.h:304,395).
+    d = scenes.triangle_soup(300, seed=2)
+    t = d.triangles.copy()
+    t["v"]["p"][:100] = t["v"]["p"][0]
+    t["v"]["p"][100:200, :, 2] = 1.0
+    d.triangles = t
+    return d
+
+
+@pytest.mark.parametrize("name", sorted(SCENES))
+def test_oracle_matches_reference(oracle, reference, name):
+    desc = SCENES[name]()
+    n_o, i_o = oracle.bvh_build(desc.triangles)
+    n_r, i_r = reference.bvh_build(desc.triangles)
+    assert n_o.tobytes() == n_r.tobytes()
+    assert np.array_equal(i_o, i_r)
+    bmin, bmax = desc.bounds()
+    rays = scenes.random_rays(bmin, bmax, 20000, seed=17)
+    h_o, _, _ = oracle.trace_closest(desc.triangles, n_o, i_o, rays)
+    world = reference.world(desc.triangles)
+    h_r, _ = world.trace_closest(rays)
+    assert h_o.tobytes() == h_r.tobytes()
+    rays["tmax"] = (np.where(h_o["id"] >= 0, h_o["t"], np.float32(3.0)) * np.float32(1.01)).astype(np.float32)
+    v_o, _, _ = oracle.trace_any(desc.triangles, n_o, i_o, rays)
+    v_r, _ = world.trace_any(rays)
+    assert np.array_equal(v_o, v_r)
+
+
+def test_oracle_empty_and_tiny(oracle):
+    d = scenes.triangle_soup(3, seed=1)
+    nodes, idx = oracle.bvh_build(d.triangles)
+    assert len(nodes) == 1 and nodes[0]["used"] == 3
+    assert sorted(idx.tolist()) == [0, 1, 2]
+    nodes0, _ = oracle.bvh_build(d.triangles[:0])
+    assert len(nodes0) == 0
+
+
+def test_oracle_multithreaded_matches_single(oracle):
+    d = scenes.triangle_soup(3000, seed=8)
+    nodes, idx = oracle.bvh_build(d.triangles)
+    rays = scenes.random_rays(*d.bounds(), 10000, seed=3)
+    h1, _, _ = oracle.trace_closest(d.triangles, nodes, idx, rays)
+    h2 = oracle.trace_closest_mt(d.triangles, nodes, idx, rays, 4)
+    assert h1.tobytes() == h2.tobytes()
