@@ -92,14 +92,27 @@ def build_reference(force: bool = False) -> Path | None:
     common = ["g++", "-std=c++20", "-fPIC", "-shared", "-pthread", "-w",
               "-include", str(HERE / "ref_shim" / "prelude.h"), "-I", str(REF_SRC),
               str(HERE / "ref_harness.cpp")]
+    # Plain-integrator variant: the reference selects its integrator with the
+    # compile-time switch `#define GUIDED_PATH true` (Renderer.h:25); the
+    # plain build stages a copy of Renderer.h with that one value false.
+    plain_dir = REF_OUT / "src_plain"
+    plain_dir.mkdir(parents=True, exist_ok=True)
+    text = (REF_SRC / "Renderer.h").read_text()
+    if "#define GUIDED_PATH true" not in text:
+        raise RuntimeError("Renderer.h: GUIDED_PATH switch not found")
+    plain_h = plain_dir / "Renderer.h"
+    new_text = text.replace("#define GUIDED_PATH true", "#define GUIDED_PATH false", 1)
+    if not plain_h.exists() or plain_h.read_text() != new_text:
+        plain_h.write_text(new_text)
     outs = {
         "liborcref.so": ["-O2", "-ffp-contract=off", "-fno-fast-math"],
         "liborcref_fast.so": ["-O3"],
+        "liborcref_plain_fast.so": ["-O3", "-I", str(plain_dir)],
     }
     procs = []
     for name, flags in outs.items():
         out = REF_OUT / name
-        if force or not _newer(out, srcs):
+        if force or not _newer(out, srcs + [plain_h]):
             tmp = out.with_suffix(".so.tmp")
             procs.append((subprocess.Popen(common[:1] + flags + common[1:] + ["-o", str(tmp)],
                                            stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True),

@@ -28,6 +28,50 @@ TRIANGLE = np.dtype([("v", VERTEX, 3), ("material", "<u4")])
 RAY = np.dtype([("o", "<f4", 3), ("tmax", "<f4"), ("d", "<f4", 3), ("pad", "<f4")])
 HIT = np.dtype([("id", "<i4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4")])
 BVH_NODE = np.dtype([("bmin", "<f4", 3), ("bmax", "<f4", 3), ("left_first", "<i4"), ("used", "<i4")])
+MATERIAL = np.dtype([
+    ("kind", "<i4"), ("albedo_texture", "<i4"), ("albedo", "<f4", 3), ("eta", "<f4", 3), ("k", "<f4", 3),
+    ("int_ior", "<f4"), ("ext_ior", "<f4"), ("roughness", "<f4"), ("sigma", "<f4"), ("emission", "<f4", 3),
+    ("layered", "<i4"),
+])
+PATH_VERTEX = np.dtype([("position", "<f4", 3), ("normal", "<f4", 3), ("wi", "<f4", 3), ("Li", "<f4", 3)])
+CACHE_NODE = np.dtype([("bmin", "<f4", 3), ("bmax", "<f4", 3), ("left", "<i4"), ("right", "<i4"),
+                       ("offset", "<i4"), ("used", "<i4")])
+
+
+class Texture(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("rgb", C.c_void_p)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("from_", C.c_float * 3), ("to", C.c_float * 3), ("up", C.c_float * 3),
+                ("fov_degrees", C.c_float), ("width", C.c_int32), ("height", C.c_int32), ("flip_x", C.c_int32)]
+
+
+class SceneArgs:
+    """Keeps the ctypes views of a scene description alive for one call."""
+
+    def __init__(self, desc):
+        self.tris = np.ascontiguousarray(desc.triangles, TRIANGLE)
+        self.mats = np.ascontiguousarray(desc.materials, MATERIAL)
+        self.texs = [np.ascontiguousarray(t, np.float32) for t in desc.textures]
+        self.tex_arr = (Texture * max(1, len(self.texs)))()
+        for i, t in enumerate(self.texs):
+            self.tex_arr[i] = Texture(t.shape[1], t.shape[0], t.ctypes.data)
+        self.env = None
+        self.env_arr = None
+        if desc.env is not None:
+            self.env_arr = np.ascontiguousarray(desc.env, np.float32)
+            self.env = Texture(self.env_arr.shape[1], self.env_arr.shape[0], self.env_arr.ctypes.data)
+        c = desc.camera
+        self.cam = Camera((C.c_float * 3)(*c["from_"]), (C.c_float * 3)(*c["to"]), (C.c_float * 3)(*c["up"]),
+                          float(c["fov"]), int(c["width"]), int(c["height"]), int(c.get("flip_x", 0)))
+        self.width = int(c["width"])
+        self.height = int(c["height"])
+
+    def args(self):
+        return (_p(self.tris), len(self.tris), _p(self.mats), len(self.mats),
+                C.cast(self.tex_arr, C.c_void_p) if self.texs else None, len(self.texs),
+                C.byref(self.env) if self.env is not None else None, C.byref(self.cam))
 
 
 def _p(a):
@@ -108,15 +152,19 @@ def reference_available() -> bool:
 
 
 class Reference:
-    """The reference renderer compiled headless (oracle/ref_harness.cpp)."""
+    """The reference renderer compiled headless (oracle/ref_harness.cpp).
 
-    def __init__(self, fast: bool = False):
+    variant: "parity" (-O2 -ffp-contract=off, GUIDED_PATH as shipped),
+    "fast" (-O3, as shipped) or "plain_fast" (-O3, GUIDED_PATH false)."""
+
+    def __init__(self, fast: bool = False, variant: str | None = None):
         from . import build as _b  # noqa: PLC0415
         p = _b.build_reference()
         if p is None:
             raise RuntimeError("reference sources unavailable")
-        if fast:
-            p = p.parent / "liborcref_fast.so"
+        variant = variant or ("fast" if fast else "parity")
+        names = {"parity": "liborcref.so", "fast": "liborcref_fast.so", "plain_fast": "liborcref_plain_fast.so"}
+        p = p.parent / names[variant]
         self.lib = C.CDLL(str(p))
         L = self.lib
         L.orcref_bvh_build.restype = _I64
@@ -131,6 +179,18 @@ class Reference:
         L.orcref_trace_any.argtypes = [_P, _P, _I64, _P, _I32]
         L.orcref_rng_floats.restype = None
         L.orcref_rng_floats.argtypes = [_U64, _U64, _U64, _I32, _P]
+        L.orcref_scene_create.restype = _P
+        L.orcref_scene_create.argtypes = [_P, _I64, _P, _I32, _P, _I32, _P, _P, _I32]
+        L.orcref_scene_destroy.restype = None
+        L.orcref_scene_destroy.argtypes = [_P]
+        L.orcref_render_pcg.restype = _I64
+        L.orcref_render_pcg.argtypes = [_P, _I32, _U64, _I32, _I32, _P, _I32, _I32, _P, _I64, C.POINTER(_I64)]
+        L.orcref_render_native.restype = C.c_double
+        L.orcref_render_native.argtypes = [_P, _I32, _P, C.POINTER(_I32), C.POINTER(_I64)]
+        L.orcref_clear.restype = None
+        L.orcref_clear.argtypes = [_P]
+        L.orcref_pointbvh.restype = _I64
+        L.orcref_pointbvh.argtypes = [_P, _I64, _P, _P]
 
     def bvh_build(self, tris: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
         tris = np.ascontiguousarray(tris, TRIANGLE)
@@ -139,6 +199,53 @@ class Reference:
         idx = np.zeros(max(1, n), np.int32)
         cnt = self.lib.orcref_bvh_build(_p(tris), n, _p(nodes), _p(idx))
         return nodes[:cnt].copy(), idx[:n].copy()
+
+    def scene(self, desc, threads: int = 0) -> "RefScene":
+        return RefScene(self, desc, threads)
+
+    def pointbvh(self, records: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+        records = np.ascontiguousarray(records, PATH_VERTEX)
+        n = len(records)
+        nodes = np.zeros(max(1, 2 * n), CACHE_NODE)
+        out = np.zeros(max(1, n), PATH_VERTEX)
+        cnt = self.lib.orcref_pointbvh(_p(records), n, _p(nodes), _p(out))
+        return nodes[:cnt].copy(), out[:n].copy()
+
+
+class RefScene:
+    """A reference `Scene` + `RayTracer` (SceneLoader.h:222-269)."""
+
+    def __init__(self, ref: "Reference", desc, threads: int = 0):
+        self.ref = ref
+        self.sa = SceneArgs(desc)
+        self.h = ref.lib.orcref_scene_create(*self.sa.args(), threads)
+
+    def close(self):
+        if self.h:
+            self.ref.lib.orcref_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def render_pcg(self, guided: bool, seed: int, spp0: int, nspp: int, threads: int = 8, collect: int = -1,
+                   vcap: int = 0):
+        film = np.zeros((self.sa.height, self.sa.width, 3), np.float32)
+        verts = np.zeros(max(1, vcap), PATH_VERTEX)
+        rays = _I64(0)
+        nv = self.ref.lib.orcref_render_pcg(self.h, int(guided), seed, spp0, nspp, _p(film), threads, collect,
+                                            _p(verts), vcap, C.byref(rays))
+        return film, verts[:min(nv, vcap)].copy(), rays.value
+
+    def render_native(self, frames: int):
+        film = np.zeros((self.sa.height, self.sa.width, 3), np.float32)
+        spp = _I32(0)
+        rays = _I64(0)
+        secs = self.ref.lib.orcref_render_native(self.h, frames, _p(film), C.byref(spp), C.byref(rays))
+        return film, spp.value, rays.value, secs
+
+    def clear(self):
+        self.ref.lib.orcref_clear(self.h)
 
     def world(self, tris: np.ndarray) -> "RefWorld":
         return RefWorld(self, tris)

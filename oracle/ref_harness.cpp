@@ -21,6 +21,7 @@
 #include <cstdint>
 #include <cstring>
 #include <iostream>
+#include <functional>
 #include <map>
 #include <memory>
 #include <random>
@@ -42,16 +43,24 @@
 // `Scene::visible` are the only two routes from `RayTracer` into the BVH
 // (Renderer.h:293,332,415,533).  The macros wrap the first argument of those
 // calls in a comma expression that bumps a per-thread counter, so the calls
-// themselves are unchanged.  Defined after Scene.h, before Renderer.h.
-static thread_local long long g_rays_traced = 0;
+// themselves are unchanged.  Each thread counts privately and adds its count
+// to the total when it exits (RayTracer::render joins its threads every
+// frame, Renderer.h:715-718), so the count costs one increment per ray.
 static std::atomic<long long> g_rays_total{0};
+struct RayCounter {
+    long long n = 0;
+    ~RayCounter() { g_rays_total.fetch_add(n); }
+};
+static thread_local RayCounter g_ray_counter;
 static inline int pgx_count_ray() {
-    ++g_rays_traced;
+    ++g_ray_counter.n;
     return 0;
 }
 #define traverse(r) traverse((pgx_count_ray(), r))
 #define visible(a, b) visible((pgx_count_ray(), a), b)
+#define private public
 #include "Renderer.h"
+#undef private
 #undef traverse
 #undef visible
 
@@ -88,6 +97,50 @@ class PcgSampler : public Sampler {
 struct RefWorld {
     std::vector<Triangle> tris;
     BVHNode bvh;
+};
+
+Texture* make_texture(int w, int h, const float* rgb) {
+    Texture* t = new Texture();
+    t->width = w;
+    t->height = h;
+    t->channels = 3;
+    t->alpha = nullptr;
+    t->texels = new Colour[(size_t)w * h];
+    for (size_t i = 0; i < (size_t)w * h; i++) t->texels[i] = Colour(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2]);
+    return t;
+}
+
+// Material construction as loadInstance does it (SceneLoader.h:110-176).
+BSDF* make_bsdf(const pgx_material& m, std::vector<Texture*>& textures) {
+    Texture* alb;
+    if (m.albedo_texture >= 0) {
+        alb = textures[(size_t)m.albedo_texture];
+    } else {
+        alb = make_texture(1, 1, m.albedo);
+    }
+    BSDF* b = nullptr;
+    switch (m.kind) {
+        case PGX_BSDF_DIFFUSE: b = new DiffuseBSDF(alb); break;
+        case PGX_BSDF_MIRROR: b = new MirrorBSDF(alb); break;
+        case PGX_BSDF_CONDUCTOR:
+            b = new ConductorBSDF(alb, Colour(m.eta[0], m.eta[1], m.eta[2]), Colour(m.k[0], m.k[1], m.k[2]), m.roughness);
+            break;
+        case PGX_BSDF_GLASS: b = new GlassBSDF(alb, m.int_ior, m.ext_ior); break;
+        case PGX_BSDF_DIELECTRIC: b = new DielectricBSDF(alb, m.int_ior, m.ext_ior, m.roughness); break;
+        case PGX_BSDF_ORENNAYAR: b = new OrenNayarBSDF(alb, m.sigma); break;
+        case PGX_BSDF_PLASTIC: b = new PlasticBSDF(alb, m.int_ior, m.ext_ior, m.roughness); break;
+        default: b = new DiffuseBSDF(alb); break;
+    }
+    b->addLight(Colour(m.emission[0], m.emission[1], m.emission[2]));
+    if (m.layered) b = new LayeredBSDF(b, Colour(0.f, 0.f, 0.f), 1.f, 1.33f, 1.f);
+    return b;
+}
+
+struct RefScene {
+    Scene* scene = nullptr;
+    RayTracer rt;
+    GamesEngineeringBase::Window canvas;
+    int width = 0, height = 0;
 };
 
 }  // namespace
@@ -172,6 +225,181 @@ double orcref_trace_any(void* h, const pgx_ray* rays, int64_t n, uint8_t* visibl
     }
     auto t1 = std::chrono::steady_clock::now();
     return std::chrono::duration<double>(t1 - t0).count();
+}
+
+// Scene as loadScene assembles it (SceneLoader.h:222-269): triangles,
+// materials, background (environment map or black), BVH + light list,
+// camera from (from, to, up, fov), scene bounds.
+void* orcref_scene_create(const pgx_triangle* tris, int64_t n, const pgx_material* mats, int32_t nm,
+                          const pgx_texture* textures, int32_t ntex, const pgx_texture* env, const pgx_camera* cam,
+                          int32_t threads) {
+    RefScene* rs = new RefScene();
+    rs->scene = new Scene();
+    std::vector<Texture*> texs;
+    for (int32_t i = 0; i < ntex; i++) texs.push_back(make_texture(textures[i].width, textures[i].height, textures[i].rgb));
+    std::vector<BSDF*> bsdfs;
+    for (int32_t i = 0; i < nm; i++) bsdfs.push_back(make_bsdf(mats[i], texs));
+    std::vector<Triangle> t = to_triangles(tris, n);
+    Light* background;
+    if (env) background = new EnvironmentMap(make_texture(env->width, env->height, env->rgb));
+    else background = new BackgroundColour(Colour(0.0f, 0.0f, 0.0f));
+    Matrix P = Matrix::perspective(0.001f, 10000.0f, (float)cam->width / (float)cam->height, cam->fov_degrees);
+    Vec4 from(cam->from[0], cam->from[1], cam->from[2]);
+    Vec4 to(cam->to[0], cam->to[1], cam->to[2]);
+    Vec4 up(cam->up[0], cam->up[1], cam->up[2]);
+    Matrix V = Matrix::lookAt(from, to, up);
+    V = V.invert();
+    if (cam->flip_x == 1) P.a[0][0] = -P.a[0][0];
+    rs->scene->camera.init(P, cam->width, cam->height);
+    rs->scene->camera.updateView(V);
+    rs->scene->init(t, bsdfs, background);
+    rs->scene->build();
+    use<SceneBounds>().sceneCentre = (rs->scene->bounds.max + rs->scene->bounds.min) * 0.5f;
+    use<SceneBounds>().sceneRadius = (rs->scene->bounds.max - use<SceneBounds>().sceneCentre).length();
+    rs->width = cam->width;
+    rs->height = cam->height;
+    pgx_ref_thread_count() = threads > 0 ? (unsigned)threads : 0u;
+    rs->canvas.create(cam->width, cam->height, "headless");
+    rs->rt.init(rs->scene, &rs->canvas);
+    return rs;
+}
+
+void orcref_scene_destroy(void* h) { delete static_cast<RefScene*>(h); }
+
+// Per-pixel loop of RayTracer::render (Renderer.h:676-706) driven by the
+// PCG32 stream of (seed, pixel, sample): jitter, camera ray, then
+// pathTrace (guided = 0) or guidedPath (guided = 1), NaN/Inf drop and
+// Film::splat.  Samples spp0 .. spp0+nspp-1 accumulate into film_rgb (W*H*3,
+// caller-zeroed); rows are split over `threads` threads with private films.
+// Path vertices of sample `collect` (guided only) go to verts (capacity
+// vcap); returns the number written.  rays_out gets the rays traced.
+int64_t orcref_render_pcg(void* h, int32_t guided, uint64_t seed, int32_t spp0, int32_t nspp, float* film_rgb,
+                          int32_t threads, int32_t collect, pgx_path_vertex* verts, int64_t vcap,
+                          int64_t* rays_out) {
+    RefScene* rs = static_cast<RefScene*>(h);
+    const int W = rs->width, H = rs->height;
+    if (threads < 1) threads = 1;
+    std::vector<std::vector<float>> films((size_t)threads, std::vector<float>((size_t)W * H * 3, 0.f));
+    std::vector<std::vector<PathVertex>> vlists((size_t)threads);
+    const long long rays0 = g_rays_total.load();
+    auto work = [&](int tid) {
+        Film film;
+        film.width = W;
+        film.height = H;
+        film.film = reinterpret_cast<Colour*>(films[(size_t)tid].data());
+        BoxFilter box;
+        film.filter = &box;
+        film.SPP = 0;
+        PcgSampler sampler;
+        std::vector<PathVertex> scratch;
+        for (int y = tid; y < H; y += threads) {
+            for (int x = 0; x < W; x++) {
+                for (int s = spp0; s < spp0 + nspp; s++) {
+                    sampler.reset(seed, (uint64_t)y * W + x, (uint64_t)s);
+                    float px = x + sampler.next();
+                    float py = y + sampler.next();
+                    Ray ray = rs->scene->camera.generateRay(px, py);
+                    Colour col;
+                    if (guided) {
+                        scratch.clear();
+                        col = rs->rt.guidedPath(ray, &sampler, scratch);
+                        if (s == collect) vlists[(size_t)tid].insert(vlists[(size_t)tid].end(), scratch.begin(), scratch.end());
+                    } else {
+                        col = rs->rt.pathTrace(ray, &sampler);
+                    }
+                    if (std::isnan(col.r) || std::isnan(col.g) || std::isnan(col.b) || std::isinf(col.r) ||
+                        std::isinf(col.g) || std::isinf(col.b))
+                        continue;
+                    film.splat(px, py, col);
+                }
+            }
+        }
+    };
+    std::vector<std::thread> th;
+    for (int t = 0; t < threads; t++) th.emplace_back(work, t);
+    for (auto& t : th) t.join();
+    for (auto& f : films)
+        for (size_t i = 0; i < f.size(); i++) film_rgb[i] += f[i];
+    if (rays_out) *rays_out = g_rays_total.load() - rays0;
+    int64_t nv = 0;
+    for (auto& vl : vlists)
+        for (auto& v : vl) {
+            if (nv < vcap && verts) {
+                pgx_path_vertex& o = verts[nv];
+                o.position[0] = v.position.x; o.position[1] = v.position.y; o.position[2] = v.position.z;
+                o.normal[0] = v.normal.x; o.normal[1] = v.normal.y; o.normal[2] = v.normal.z;
+                o.wi[0] = v.wi.x; o.wi[1] = v.wi.y; o.wi[2] = v.wi.z;
+                o.Li[0] = v.Li.r; o.Li[1] = v.Li.g; o.Li[2] = v.Li.b;
+            }
+            nv++;
+        }
+    return nv;
+}
+
+// The reference's own RayTracer::render (Renderer.h:648-747) `frames`
+// times: its tile scheduler, its MTRandom samplers, its integrator (the
+// GUIDED_PATH switch of the build), its film.  Returns seconds spent in
+// render(); film_rgb gets Film::film, rays_out the rays traced.
+double orcref_render_native(void* h, int32_t frames, float* film_rgb, int32_t* spp, int64_t* rays_out) {
+    RefScene* rs = static_cast<RefScene*>(h);
+    const long long rays0 = g_rays_total.load();
+    double secs = 0.0;
+    for (int32_t f = 0; f < frames; f++) {
+        auto t0 = std::chrono::steady_clock::now();
+        rs->rt.render();
+        auto t1 = std::chrono::steady_clock::now();
+        secs += std::chrono::duration<double>(t1 - t0).count();
+    }
+    if (film_rgb) std::memcpy(film_rgb, rs->rt.film->film, sizeof(float) * 3 * (size_t)rs->width * rs->height);
+    if (spp) *spp = rs->rt.getSPP();
+    if (rays_out) *rays_out = g_rays_total.load() - rays0;
+    return secs;
+}
+
+void orcref_clear(void* h) { static_cast<RefScene*>(h)->rt.clear(); }
+
+// PointBVHNode::buildPointBVHNode (Renderer.h:189-211) on given records;
+// exports the tree in preorder (root first) and the records in node order.
+int64_t orcref_pointbvh(const pgx_path_vertex* recs, int64_t n, pgx_cache_node* nodes, pgx_path_vertex* out) {
+    std::vector<PathVertex> v((size_t)n);
+    for (int64_t i = 0; i < n; i++) {
+        v[(size_t)i].position = Vec4(recs[i].position[0], recs[i].position[1], recs[i].position[2]);
+        v[(size_t)i].normal = Vec4(recs[i].normal[0], recs[i].normal[1], recs[i].normal[2]);
+        v[(size_t)i].wi = Vec4(recs[i].wi[0], recs[i].wi[1], recs[i].wi[2]);
+        v[(size_t)i].Li = Colour(recs[i].Li[0], recs[i].Li[1], recs[i].Li[2]);
+    }
+    std::streambuf* old = std::cout.rdbuf(nullptr);  // silence stats()
+    PointBVHNode* root = new PointBVHNode();
+    root->buildPointBVHNode(std::move(v));
+    std::cout.rdbuf(old);
+    int64_t count = 0;
+    std::function<int64_t(PointBVHNode*)> walk = [&](PointBVHNode* nd) -> int64_t {
+        int64_t me = count++;
+        pgx_cache_node& o = nodes[me];
+        o.bmin[0] = nd->bounds.min.x; o.bmin[1] = nd->bounds.min.y; o.bmin[2] = nd->bounds.min.z;
+        o.bmax[0] = nd->bounds.max.x; o.bmax[1] = nd->bounds.max.y; o.bmax[2] = nd->bounds.max.z;
+        o.offset = nd->offset;
+        o.used = nd->used;
+        if (nd->isLeaf()) {
+            o.left = o.right = -1;
+        } else {
+            int64_t l = walk(nd->l);
+            int64_t r = walk(nd->r);
+            nodes[me].left = (int32_t)l;
+            nodes[me].right = (int32_t)r;
+        }
+        return me;
+    };
+    if (n > 0) walk(root);
+    for (int64_t i = 0; i < n; i++) {
+        const PathVertex& p = root->pathVertexRecords[(size_t)i];
+        out[i].position[0] = p.position.x; out[i].position[1] = p.position.y; out[i].position[2] = p.position.z;
+        out[i].normal[0] = p.normal.x; out[i].normal[1] = p.normal.y; out[i].normal[2] = p.normal.z;
+        out[i].wi[0] = p.wi.x; out[i].wi[1] = p.wi.y; out[i].wi[2] = p.wi.z;
+        out[i].Li[0] = p.Li.r; out[i].Li[1] = p.Li.g; out[i].Li[2] = p.Li.b;
+    }
+    delete root;
+    return count;
 }
 
 void orcref_rng_floats(uint64_t seed, uint64_t pixel, uint64_t sample, int32_t count, float* out) {

@@ -44,13 +44,19 @@ def _deps() -> list[Path]:
     return sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + sorted(INCLUDE.glob("*.h"))
 
 
+# Per-file flags: the integrator rounds every product and sum separately,
+# like the reference's scalar code (traversal uses explicit _rn intrinsics
+# and is exact regardless).
+FILE_FLAGS = {"render.cu": ["-fmad=false"]}
+
+
 def _compile(src: Path, extra: list[str]) -> Path:
     OBJ.mkdir(parents=True, exist_ok=True)
     obj = OBJ / (src.stem + ".o")
     newest_dep = max([src.stat().st_mtime] + [d.stat().st_mtime for d in _deps()])
     if obj.exists() and obj.stat().st_mtime >= newest_dep and not extra:
         return obj
-    cmd = [nvcc(), *NVCC_FLAGS, *extra, "-c", str(src), "-o", str(obj)]
+    cmd = [nvcc(), *NVCC_FLAGS, *FILE_FLAGS.get(src.name, []), *extra, "-c", str(src), "-o", str(obj)]
     r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed on {src.name}:\n{r.stdout[-6000:]}")

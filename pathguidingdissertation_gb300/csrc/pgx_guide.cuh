@@ -1,0 +1,238 @@
+// QuadTree directional guide over the point-BVH radiance cache (extension;
+// the reference sketches it in Renderer.h:398-414 and ships only an unused
+// point quadtree, QuadTree.h).
+//
+// Spatial side: the cache's point BVH is cut into regions — the subtrees
+// whose record count first drops to kRegionMax.  Directional side: each
+// region owns a quadtree over the cylindrical equal-area map of world
+// directions, (u, v) = ((cos(theta) + 1) / 2, (phi + pi) / 2pi) with theta
+// measured from +z (solid angle = 4*pi * area in (u, v)).  Cells are refined
+// while they hold more than 1 % of the region's flux, where a record's flux
+// is the luminance of its Li (Mueller et al. 2017, "Practical Path Guiding").
+//
+// At a shading point the region of the nearest cached record is used; the
+// continuation direction is drawn by one-sample MIS between the guide and
+// the BSDF (probability `guide_fraction` for the guide), and the combined
+// pdf is used both for the throughput and for the MIS weights of NEE and of
+// emitter hits, so the estimator stays unbiased.  Pure-specular BSDFs and
+// regions without flux sample the BSDF alone.
+#pragma once
+
+#include "pgx_ctx.h"
+#include "pgx_shade.cuh"
+
+#define PGX_QT_MAX_DEPTH 10
+#define PGX_QT_MAX_NODES 96
+
+// Interior quadtree cell: flux of its four children (index = 2*yhalf + xhalf
+// in (u, v)) and their node indices within the region (-1 = leaf).
+struct __align__(16) QuadNode {
+    float flux[4];
+    int child[4];
+};
+
+// Point-BVH node for nearest-record queries: bmin.w = left child (or
+// -(offset + 1) for a leaf), bmax.w = right child (or record count).
+struct __align__(16) CacheTravNode {
+    float4 bmin;
+    float4 bmax;
+};
+
+struct GuideView {
+    int valid;
+    int n_nodes;
+    int n_records;
+    const CacheTravNode* __restrict__ nodes;
+    const float4* __restrict__ rec_pos;   // xyz, w = region id bits
+    const int* __restrict__ region_qroot; // first QuadNode of each region (-1: no flux)
+    const QuadNode* __restrict__ qnodes;
+};
+
+GuideView guide_view(const pgx_ctx* ctx);
+bool guide_ready(const pgx_ctx* ctx);
+int cache_build_device(pgx_ctx* ctx, const pgx_path_vertex* d_records, int64_t n);
+
+__device__ __forceinline__ void dir_to_uv(F3 w, float& u, float& v) {
+    float c = fminf(fmaxf(w.z, -1.f), 1.f);
+    u = (c + 1.f) * 0.5f;
+    float phi = atan2f(w.y, w.x);
+    v = (phi + 3.14159265f) * (1.f / (2.f * 3.14159265f));
+    u = fminf(fmaxf(u, 0.f), 0.99999994f);
+    v = fminf(fmaxf(v, 0.f), 0.99999994f);
+}
+__device__ __forceinline__ F3 uv_to_dir(float u, float v) {
+    float c = 2.f * u - 1.f;
+    float s = sqrtf(fmaxf(0.f, 1.f - c * c));
+    float phi = 2.f * 3.14159265f * v - 3.14159265f;
+    return f3(s * cosf(phi), s * sinf(phi), c);
+}
+
+// Nearest cached record to x (squared distance, ties to the lower index).
+static __device__ int guide_nearest(const GuideView& g, F3 x) {
+    if (g.n_nodes <= 0) return -1;
+    int stack[64];
+    int sp = 0;
+    int best = -1;
+    float bestd = FLT_MAX;
+    int node = 0;
+    for (;;) {
+        CacheTravNode n = g.nodes[node];
+        int l = __float_as_int(n.bmin.w), r = __float_as_int(n.bmax.w);
+        if (l < 0) {
+            int off = -l - 1;
+            for (int k = 0; k < r; k++) {
+                float4 p = g.rec_pos[off + k];
+                float dx = p.x - x.x, dy = p.y - x.y, dz = p.z - x.z;
+                float d = dx * dx + dy * dy + dz * dz;
+                if (d < bestd || (d == bestd && off + k < best)) {
+                    bestd = d;
+                    best = off + k;
+                }
+            }
+        } else {
+            CacheTravNode a = g.nodes[l], b = g.nodes[r];
+            auto box_d = [&](const CacheTravNode& c) {
+                float dx = fmaxf(fmaxf(c.bmin.x - x.x, x.x - c.bmax.x), 0.f);
+                float dy = fmaxf(fmaxf(c.bmin.y - x.y, x.y - c.bmax.y), 0.f);
+                float dz = fmaxf(fmaxf(c.bmin.z - x.z, x.z - c.bmax.z), 0.f);
+                return dx * dx + dy * dy + dz * dz;
+            };
+            float da = box_d(a), db = box_d(b);
+            int first = l, second = r;
+            if (db < da) {
+                float t = da;
+                da = db;
+                db = t;
+                first = r;
+                second = l;
+            }
+            if (da <= bestd) {
+                if (db <= bestd && sp < 64) stack[sp++] = second;
+                node = first;
+                continue;
+            }
+        }
+        // pop the next node that can still hold a closer record
+        bool found = false;
+        while (sp > 0) {
+            int c = stack[--sp];
+            CacheTravNode n2 = g.nodes[c];
+            float dx = fmaxf(fmaxf(n2.bmin.x - x.x, x.x - n2.bmax.x), 0.f);
+            float dy = fmaxf(fmaxf(n2.bmin.y - x.y, x.y - n2.bmax.y), 0.f);
+            float dz = fmaxf(fmaxf(n2.bmin.z - x.z, x.z - n2.bmax.z), 0.f);
+            if (dx * dx + dy * dy + dz * dz <= bestd) {
+                node = c;
+                found = true;
+                break;
+            }
+        }
+        if (!found) break;
+    }
+    return best;
+}
+
+// Quadtree pdf in (u, v) space (density w.r.t. area; 1 = uniform).
+static __device__ float quad_pdf(const QuadNode* qn, int root, float u, float v) {
+    float pdf = 1.f;
+    int node = root;
+    for (int d = 0; d < PGX_QT_MAX_DEPTH + 1; d++) {
+        QuadNode n = qn[node];
+        float total = n.flux[0] + n.flux[1] + n.flux[2] + n.flux[3];
+        if (!(total > 0.f)) return 0.f;
+        int xi = u >= 0.5f ? 1 : 0, yi = v >= 0.5f ? 1 : 0;
+        int c = 2 * yi + xi;
+        pdf *= 4.f * n.flux[c] / total;
+        if (n.child[c] < 0 || pdf == 0.f) return pdf;
+        u = u * 2.f - (float)xi;
+        v = v * 2.f - (float)yi;
+        node = n.child[c];
+    }
+    return pdf;
+}
+
+static __device__ void quad_sample(const QuadNode* qn, int root, float r1, float r2, float& u, float& v) {
+    float u0 = 0.f, v0 = 0.f, size = 1.f;
+    int node = root;
+    for (int d = 0; d < PGX_QT_MAX_DEPTH + 1; d++) {
+        QuadNode n = qn[node];
+        float left = n.flux[0] + n.flux[2], right = n.flux[1] + n.flux[3];
+        float total = left + right;
+        int xi;
+        float pl = total > 0.f ? left / total : 0.5f;
+        if (r1 < pl) {
+            xi = 0;
+            r1 = pl > 0.f ? r1 / pl : 0.f;
+        } else {
+            xi = 1;
+            r1 = (1.f - pl) > 0.f ? (r1 - pl) / (1.f - pl) : 0.f;
+        }
+        float top = n.flux[xi], bot = n.flux[2 + xi];
+        float pt = (top + bot) > 0.f ? top / (top + bot) : 0.5f;
+        int yi;
+        if (r2 < pt) {
+            yi = 0;
+            r2 = pt > 0.f ? r2 / pt : 0.f;
+        } else {
+            yi = 1;
+            r2 = (1.f - pt) > 0.f ? (r2 - pt) / (1.f - pt) : 0.f;
+        }
+        r1 = fminf(r1, 0.99999994f);
+        r2 = fminf(r2, 0.99999994f);
+        size *= 0.5f;
+        u0 += size * (float)xi;
+        v0 += size * (float)yi;
+        int c = 2 * yi + xi;
+        if (n.child[c] < 0) break;
+        node = n.child[c];
+    }
+    u = u0 + size * r1;
+    v = v0 + size * r2;
+}
+
+// Region quadtree of the nearest record (-1 when unusable).
+__device__ __forceinline__ int guide_region_root(const GuideView& g, F3 x) {
+    if (!g.valid) return -1;
+    int rec = guide_nearest(g, x);
+    if (rec < 0) return -1;
+    int region = __float_as_int(g.rec_pos[rec].w);
+    return g.region_qroot[region];
+}
+
+// Solid-angle pdf of the one-sample mixture at wi.
+__device__ __forceinline__ float mixture_pdf(const GuideView& g, int qroot, float frac, float bsdf_p, F3 wi) {
+    if (qroot < 0) return bsdf_p;
+    float u, v;
+    dir_to_uv(wi, u, v);
+    float gp = quad_pdf(g.qnodes, qroot, u, v) * (1.f / (4.f * 3.14159265f));
+    return frac * gp + (1.f - frac) * bsdf_p;
+}
+
+// Continuation direction for the guided estimator: pdf is the mixture pdf.
+static __device__ F3 guided_sample(const GuideView& g, float frac, const DevMaterial& m, const TexView& tv,
+                            const Shading& sd, uint64_t& rng, F3& f, float& pdf, int qroot) {
+    if (qroot < 0 || bsdf_pure_specular(m) || m.kind == PGX_BSDF_GLASS) {
+        return bsdf_sample(m, tv, sd, rng, f, pdf);
+    }
+    float sel = pgx_rng_next(rng);
+    F3 wi;
+    if (sel < frac) {
+        float r1 = pgx_rng_next(rng), r2 = pgx_rng_next(rng);
+        float u, v;
+        quad_sample(g.qnodes, qroot, r1, r2, u, v);
+        wi = uv_to_dir(u, v);
+        f = bsdf_eval(m, tv, sd, wi);
+    } else {
+        float bp;
+        wi = bsdf_sample(m, tv, sd, rng, f, bp);
+    }
+    float bp = bsdf_pdf(m, tv, sd, wi);
+    pdf = mixture_pdf(g, qroot, frac, bp, wi);
+    return wi;
+}
+
+// Overload used by render.cu's shade kernel (region looked up here).
+__device__ __forceinline__ F3 guided_sample(const GuideView& g, float frac, const DevMaterial& m, const TexView& tv,
+                                            const Shading& sd, uint64_t& rng, F3& f, float& pdf) {
+    int qroot = guide_region_root(g, sd.x);
+    return guided_sample(g, frac, m, tv, sd, rng, f, pdf, qroot);
+}

@@ -1,51 +1,833 @@
-// Wavefront renderer (placeholder until the integrator lands).
-#include "pgx_ctx.h"
+// Wavefront path tracer: RayTracer::render (Renderer.h:648-747) with the
+// integrators pathTraceRecursive (Renderer.h:531-613, PGX_MODE_PLAIN) and
+// guidedPath/guidedPathRecursive (Renderer.h:368-528, PGX_MODE_GUIDED_LI),
+// plus the QuadTree-guided estimator (PGX_MODE_GUIDED_QUADTREE, guide.cuh).
+//
+// One path per (pixel, sample).  The recursion of the reference becomes a
+// loop over depth with queue-per-stage kernels:
+//   camgen -> [extend -> shade -> shadow] x (max_depth + 1) -> finalize
+// `shade` compacts surviving paths into the next queue with warp-aggregated
+// atomics (ballot + popc, one atomicAdd per warp) and appends next-event
+// shadow rays to a shadow queue; `shadow` runs the any-hit traversal and
+// adds the stored contribution of unoccluded rays to the path's radiance.
+// Queue lengths live on the device, so a frame needs no host round trip
+// and is replayed from a captured CUDA graph.
+//
+// Each path owns a PCG32 stream keyed by (seed, pixel, sample) and draws
+// from it in the reference's order (jitter, light pick, light sample, RR,
+// BSDF sample), so a CPU run of the reference's integrator driven by the same
+// stream takes the same decisions.
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <vector>
 
-void render_state_free(pgx_ctx* ctx) { (void)ctx; }
-void cache_state_free(pgx_ctx* ctx) { (void)ctx; }
+#include "pgx_ctx.h"
+#include "pgx_guide.cuh"
+#include "pgx_shade.cuh"
+#include "pgx_trace.cuh"
+
+namespace {
+
+constexpr int kThreads = 128;
+constexpr int kMaxDepthCap = 16;
+constexpr int kCollectionSPP = 128 / 8;  // Renderer.h:721
+
+// Per-path state, structure of arrays.
+struct PathState {
+    float4* o;    // ray origin
+    float4* d;    // ray direction
+    float4* T;    // throughput rgb, w = previous BSDF pdf
+    float4* L;    // radiance rgb
+    float4* hit;  // id bits, t, u, v
+    float2* pix;  // film sample position (px, py)
+    uint64_t* rng;
+    int* flags;   // bit 0: previous surface pure specular
+    int* nrec;    // guided-Li: records written
+    int* queue[2];
+    // shadow queue
+    int* sh_path;
+    float4* sh_o;  // w = tmax
+    float4* sh_d;
+    float4* sh_c;  // contribution rgb
+    // guided-Li records [depth][path]
+    float4* rec_pos;  // w = store flag
+    float4* rec_nrm;
+    float4* rec_wi;
+    float4* rec_w;
+    float4* rec_e;
+    // counters: queue length per depth, shadow count per depth, stats
+    unsigned* qcount;  // [kMaxDepthCap + 2]
+    unsigned* scount;  // [kMaxDepthCap + 2]
+    unsigned long long* stats;  // [0] ext rays, [1] shadow rays, [2] path vertices
+    pgx_path_vertex* vertices;
+    unsigned* nvertices;
+    int64_t capacity;
+    int64_t vcapacity;
+};
+
+struct RenderState {
+    DevBuf o, d, T, L, hit, pix, rng, flags, nrec, q0, q1, sh_path, sh_o, sh_d, sh_c;
+    DevBuf rec_pos, rec_nrm, rec_wi, rec_w, rec_e;
+    DevBuf counters, vertices;
+    int64_t capacity = 0;
+    int rec_depth = 0;
+    int64_t vcapacity = 0;
+    int64_t nvertices_last = 0;
+    // captured frame graph
+    cudaGraphExec_t graph = nullptr;
+    int graph_mode = -1, graph_depth = -1, graph_batch = -1, graph_record = -1;
+    uint64_t graph_seed = 0;
+    int graph_spp0 = -1;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+struct SceneView {
+    BvhView bvh;
+    const TriShade* __restrict__ shade;
+    const DevMaterial* __restrict__ mats;
+    const DevAreaLight* __restrict__ lights;
+    TexView tex;
+    DevEnv env;
+    DevCamera cam;
+    SceneBoundsDev bounds;
+    int n_area_lights;
+    int nlights;
+    int has_env_light;
+    int width, height;
+};
+
+struct FrameParams {
+    int mode;
+    int max_depth;
+    uint64_t seed;
+    int spp0;        // sample index of the batch's first sample
+    int batch;       // samples per pixel in this batch
+    int collect;     // sample index whose path vertices are recorded (-1: none)
+    float guide_fraction;
+};
+
+// ---- camera rays (Camera::generateRay, Scene.h:253-265; jitter Renderer.h:679-681)
+__global__ void __launch_bounds__(kThreads) k_camgen(SceneView sv, PathState ps, FrameParams fp) {
+    const int64_t npix = (int64_t)sv.width * sv.height;
+    const int64_t n = npix * fp.batch;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t pixel = i % npix;
+        int s = (int)(i / npix);
+        int xpix = (int)(pixel % sv.width), ypix = (int)(pixel / sv.width);
+        uint64_t rng = pgx_rng_init(fp.seed, (uint64_t)pixel, (uint64_t)(fp.spp0 + s));
+        float px = (float)xpix + pgx_rng_next(rng);
+        float py = (float)ypix + pgx_rng_next(rng);
+        const DevCamera& cam = sv.cam;
+        float xc = (2.f * px / cam.width) - 1.f;
+        float yc = (2.f * (1.f - (py / cam.height))) - 1.f;
+        const float* m = cam.inv_proj;
+        float vx = ((xc * m[0] + yc * m[1]) + 0.f * m[2]) + m[3];
+        float vy = ((xc * m[4] + yc * m[5]) + 0.f * m[6]) + m[7];
+        float vz = ((xc * m[8] + yc * m[9]) + 0.f * m[10]) + m[11];
+        float w = ((m[12] * xc + m[13] * yc) + m[14] * 0.f) + m[15];
+        w = 1.f / w;
+        vx = vx * w;
+        vy = vy * w;
+        vz = vz * w;
+        const float* c = cam.cam;
+        F3 dir = normalize(f3((vx * c[0] + vy * c[1]) + vz * c[2], (vx * c[4] + vy * c[5]) + vz * c[6],
+                              (vx * c[8] + vy * c[9]) + vz * c[10]));
+        ps.o[i] = make_float4(cam.origin[0], cam.origin[1], cam.origin[2], 0.f);
+        ps.d[i] = make_float4(dir.x, dir.y, dir.z, 0.f);
+        ps.T[i] = make_float4(1.f, 1.f, 1.f, 0.f);
+        ps.L[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        ps.pix[i] = make_float2(px, py);
+        ps.rng[i] = rng;
+        ps.flags[i] = 0;
+        ps.nrec[i] = 0;
+        ps.queue[0][i] = (int)i;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) ps.qcount[0] = (unsigned)n;
+}
+
+// ---- closest hit for the queue of this depth ----------------------------------
+__global__ void __launch_bounds__(kThreads) k_extend(SceneView sv, PathState ps, int depth) {
+    const unsigned n = ps.qcount[depth];
+    const int* __restrict__ q = ps.queue[depth & 1];
+    unsigned long long ni = 0, nt = 0;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int p = q[i];
+        float4 a = ps.o[p], b = ps.d[p];
+        int id, st;
+        float t, u = 0.f, v = 0.f;
+        bvh_trace<false, false>(sv.bvh, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), FLT_MAX, id, t, u, v, st, ni, nt);
+        if (st) id = -1;  // corrupt tree or stack overflow: treat as a miss
+        ps.hit[p] = make_float4(__int_as_float(id), t, u, v);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ps.stats[0], (unsigned long long)n);
+}
+
+// ---- any hit for the shadow queue of this depth --------------------------------
+__global__ void __launch_bounds__(kThreads) k_shadow(SceneView sv, PathState ps, int depth) {
+    const unsigned n = ps.scount[depth];
+    unsigned long long ni = 0, nt = 0;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 a = ps.sh_o[i], b = ps.sh_d[i];
+        int id, st;
+        float t, u, v;
+        bool occluded =
+            bvh_trace<true, false>(sv.bvh, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, id, t, u, v, st, ni, nt);
+        if (!occluded && !st) {
+            int p = ps.sh_path[i];
+            float4 c = ps.sh_c[i];
+            float4 l = ps.L[p];
+            ps.L[p] = make_float4(l.x + c.x, l.y + c.y, l.z + c.z, 0.f);
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ps.stats[1], (unsigned long long)n);
+}
+
+// Scene::calculateShadingData (Scene.h:152-176).
+__device__ __forceinline__ void shading_data(const SceneView& sv, const float4& o, const float4& d, const float4& h,
+                                             Shading& sd, DevMaterial& m, F3& tri_gn, float& tri_area) {
+    int id = __float_as_int(h.x);
+    float t = h.y, beta = h.z, gamma = h.w;
+    float alpha = 1.f - (beta + gamma);
+    const TriShade& s = sv.shade[id];
+    float4 n0 = s.n0, n1 = s.n1, n2 = s.n2, vv = s.vv, gn = s.gn;
+    F3 dir = f3(d);
+    sd.t = t;
+    sd.x = f3(o) + dir * t;
+    tri_gn = f3(gn);
+    tri_area = gn.w;
+    F3 g = tri_gn;
+    F3 sn = normalize(((f3(n0) * alpha) + (f3(n1) * beta)) + (f3(n2) * gamma));
+    sd.tu = ((n0.w * alpha) + (n1.w * beta)) + (n2.w * gamma);
+    sd.tv = ((vv.x * alpha) + (vv.y * beta)) + (vv.z * gamma);
+    sd.mat = __float_as_int(vv.w);
+    m = sv.mats[sd.mat];
+    sd.wo = -dir;
+    if (bsdf_two_sided(m)) {
+        if (dot(sd.wo, sn) < 0.f) sn = -sn;
+        if (dot(sd.wo, g) < 0.f) g = -g;
+    }
+    sd.sn = sn;
+    sd.gn = g;
+    sd.frame = frame_from(sn);
+}
+
+// RayTracer::computeDirect (Renderer.h:269-354).  Draws the light and the
+// light sample; returns true with the shadow ray and the contribution it
+// carries when the contribution can be non-zero.
+__device__ bool next_event(const SceneView& sv, const DevMaterial& m, const Shading& sd, uint64_t& rng, float4& so,
+                           float4& sdir, F3& contrib, const GuideView& gv, int qroot, float frac) {
+    if (bsdf_pure_specular(m)) return false;
+    if (sv.nlights == 0) return false;
+    float pmf = 1.f / (float)sv.nlights;
+    unsigned nl = (unsigned)sv.nlights;
+    float fu = floorf(pgx_rng_next(rng) * (float)nl);
+    unsigned idx = (unsigned)fu;
+    idx = (nl - 1u < idx) ? nl - 1u : idx;
+    F3 target, wi, emitted;
+    float pdf_light;
+    if (sv.has_env_light && idx == 0) {
+        F3 dir = env_sample(sv.env, rng, emitted, pdf_light);
+        if (pdf_light <= 0.f) return false;
+        wi = normalize(dir);
+        float cos_t = s_max(dot(wi, sd.sn), 0.f);
+        if (cos_t <= 0.f) return false;
+        F3 f = bsdf_eval(m, sv.tex, sd, wi);
+        float pal = pdf_light * pmf;
+        float pab = bsdf_pdf(m, sv.tex, sd, wi);
+        if (qroot >= 0) pab = mixture_pdf(gv, qroot, frac, pab, wi);
+        float wd = power_heuristic(pal, pab);
+        contrib = divs(((emitted * f) * cos_t) * wd, pal);
+        target = f3(sv.bounds.centre[0], sv.bounds.centre[1], sv.bounds.centre[2]) + wi * sv.bounds.radius;
+    } else {
+        const DevAreaLight& L = sv.lights[idx - (unsigned)sv.has_env_light];
+        float r1 = pgx_rng_next(rng);
+        float r2 = pgx_rng_next(rng);
+        float sq = sqrtf(r1);
+        float a = 1.f - sq;
+        float b = r2 * sq;
+        float c = (1.f - a) - b;
+        float area = L.p0.w;
+        pdf_light = 1.f / area;
+        target = ((f3(L.p0) * a) + (f3(L.p1) * b)) + (f3(L.p2) * c);
+        emitted = f3(L.emission);
+        if (pdf_light <= 0.f) return false;
+        F3 stl = target - sd.x;
+        wi = normalize(stl);
+        float den = length_sq(stl);
+        if (den < PGX_EPSILON) return false;
+        float cos_t = s_max(dot(wi, sd.sn), 0.f);
+        float cos_tp = s_max(dot(-wi, f3(L.gn)), 0.f);
+        float G = (cos_t * cos_tp) / den;
+        F3 f = bsdf_eval(m, sv.tex, sd, wi);
+        float pb = bsdf_pdf(m, sv.tex, sd, wi);
+        if (qroot >= 0) pb = mixture_pdf(gv, qroot, frac, pb, wi);
+        float pal = pdf_light * pmf;
+        float pab = (pb * cos_tp) / den;
+        float wd = power_heuristic(pal, pab);
+        contrib = divs(((emitted * f) * G) * wd, pal);
+    }
+    if (contrib.x == 0.f && contrib.y == 0.f && contrib.z == 0.f) return false;
+    // Scene::visible (Scene.h:139-146) from the offset origin to the target.
+    float sgn = (dot(wi, sd.gn) >= 0.f) ? 1.f : -1.f;
+    F3 p1 = sd.x + sd.gn * (PGX_EPSILON * sgn);
+    F3 dv = target - p1;
+    float max_t = length(dv) - (2.f * PGX_EPSILON);
+    dv = normalize(dv);
+    F3 org = p1 + dv * PGX_EPSILON;
+    so = make_float4(org.x, org.y, org.z, max_t);
+    sdir = make_float4(dv.x, dv.y, dv.z, 0.f);
+    return true;
+}
+
+// Light sampling for the guided-Li estimator: the reference computes NEE
+// there too (Renderer.h:463) but never uses it in the image, so only the
+// random numbers are drawn.
+__device__ void next_event_draws(const SceneView& sv, const DevMaterial& m, uint64_t& rng) {
+    if (bsdf_pure_specular(m)) return;
+    if (sv.nlights == 0) return;
+    unsigned nl = (unsigned)sv.nlights;
+    float fu = floorf(pgx_rng_next(rng) * (float)nl);
+    unsigned idx = (unsigned)fu;
+    idx = (nl - 1u < idx) ? nl - 1u : idx;
+    if (sv.has_env_light && idx == 0) {
+        pgx_rng_next(rng);
+        pgx_rng_next(rng);
+    } else {
+        pgx_rng_next(rng);
+        pgx_rng_next(rng);
+    }
+}
+
+__device__ __forceinline__ void push_shadow(PathState& ps, int depth, int p, float4 so, float4 sdir, F3 c,
+                                            bool want) {
+    unsigned slot = warp_aggregated_add(&ps.scount[depth], want);
+    if (want) {
+        ps.sh_path[slot] = p;
+        ps.sh_o[slot] = so;
+        ps.sh_d[slot] = sdir;
+        ps.sh_c[slot] = make_float4(c.x, c.y, c.z, 0.f);
+    }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kThreads) k_shade(SceneView sv, PathState ps, FrameParams fp, int depth,
+                                                    GuideView gv) {
+    const unsigned n = ps.qcount[depth];
+    const int* __restrict__ q = ps.queue[depth & 1];
+    int* __restrict__ qn = ps.queue[(depth + 1) & 1];
+    const int64_t cap = ps.capacity;
+    // Uniform trip count per warp so the warp-aggregated appends see whole warps.
+    const unsigned stride = gridDim.x * blockDim.x;
+    const unsigned first = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned rounds = (n + stride - 1) / stride;
+    for (unsigned r = 0; r < rounds; r++) {
+        unsigned i = first + r * stride;
+        bool active = i < n;
+        bool cont = false, want_shadow = false;
+        float4 so = make_float4(0.f, 0.f, 0.f, 0.f), sdir = so;
+        F3 sc = zero3();
+        int p = active ? q[i] : 0;
+        if (active) {
+            float4 o = ps.o[p], d = ps.d[p], h = ps.hit[p], Tw = ps.T[p];
+            uint64_t rng = ps.rng[p];
+            int flags = ps.flags[p];
+            bool prev_spec = flags & 1;
+            float prev_pdf = Tw.w;
+            F3 T = f3(Tw);
+            F3 add = zero3();
+            F3 dir = f3(d);
+            int id = __float_as_int(h.x);
+            // guided-Li record of this vertex (Renderer.h:419-427)
+            F3 r_pos = zero3(), r_nrm = zero3(), r_wi = zero3(), r_w = zero3(), r_e = zero3();
+            bool r_store = false;
+            if (id >= 0) {
+                Shading sd;
+                DevMaterial m;
+                F3 tri_gn;
+                float tri_area;
+                shading_data(sv, o, d, h, sd, m, tri_gn, tri_area);
+                r_pos = sd.x;
+                r_nrm = sd.sn;
+                if (m.is_light) {
+                    F3 em = f3(m.emission[0], m.emission[1], m.emission[2]);
+                    if (MODE == PGX_MODE_GUIDED_LI) {
+                        r_e = em;
+                    } else if (depth == 0 || prev_spec) {
+                        add = T * em;
+                    } else {
+                        float pmf = 1.f / (float)sv.nlights;
+                        float pdf_light = 1.f / tri_area;
+                        float cos_tp = s_max(dot(-dir, tri_gn), 0.f);
+                        float d2 = sd.t * sd.t;
+                        if (cos_tp > 0.f && !(d2 < PGX_EPSILON)) {
+                            float pal = pdf_light * pmf;
+                            float pab = (prev_pdf * cos_tp) / d2;
+                            float wind = power_heuristic(pab, pal);
+                            add = (T * em) * wind;
+                        }
+                    }
+                } else {
+                    int qroot = -1;
+                    if (MODE == PGX_MODE_GUIDED_QUADTREE && !bsdf_pure_specular(m))
+                        qroot = guide_region_root(gv, sd.x);
+                    if (MODE == PGX_MODE_GUIDED_LI) {
+                        next_event_draws(sv, m, rng);
+                    } else {
+                        F3 c;
+                        want_shadow = next_event(sv, m, sd, rng, so, sdir, c, gv, qroot, fp.guide_fraction);
+                        sc = T * c;
+                    }
+                    bool alive = true;
+                    float rrp_rec = 1.f;
+                    if (depth > 3) {
+                        if (MODE == PGX_MODE_GUIDED_LI) {
+                            if (pgx_rng_next(rng) < 0.7f)
+                                rrp_rec = 0.7f;
+                            else
+                                alive = false;
+                        } else {
+                            float rrp = s_min(s_max(PGX_EPSILON, lum(T)), 1.f);
+                            if (pgx_rng_next(rng) < rrp)
+                                T = divs(T, rrp);
+                            else
+                                alive = false;
+                        }
+                    }
+                    if (alive && depth == fp.max_depth) alive = false;
+                    if (alive) {
+                        F3 f;
+                        float pdf;
+                        F3 wi;
+                        if (MODE == PGX_MODE_GUIDED_QUADTREE)
+                            wi = guided_sample(gv, fp.guide_fraction, m, sv.tex, sd, rng, f, pdf, qroot);
+                        else
+                            wi = bsdf_sample(m, sv.tex, sd, rng, f, pdf);
+                        float cos_t = fabsf(dot(wi, sd.sn));
+                        if (MODE == PGX_MODE_GUIDED_LI) {
+                            if (pdf <= 0.f || cos_t <= 0.f) {
+                                alive = false;
+                            } else {
+                                r_wi = wi;
+                                r_w = divs(f * cos_t, pdf * rrp_rec);
+                                r_store = !bsdf_pure_specular(m);
+                            }
+                        } else {
+                            if (pdf <= 0.f || cos_t <= 0.f) {
+                                alive = false;
+                            } else {
+                                T = divs(T * f * cos_t, pdf);
+                                if (lum(T) <= 0.f) alive = false;
+                                if (isnan(T.x) || isnan(T.y) || isnan(T.z)) alive = false;
+                                if (isinf(T.x) || isinf(T.y) || isinf(T.z)) alive = false;
+                                if (T.x < 0.f || T.y < 0.f || T.z < 0.f) alive = false;
+                            }
+                        }
+                        if (alive) {
+                            float sgn = (dot(wi, sd.gn) >= 0.f) ? 1.f : -1.f;
+                            F3 org = sd.x + sd.gn * (PGX_EPSILON * sgn);
+                            ps.o[p] = make_float4(org.x, org.y, org.z, 0.f);
+                            ps.d[p] = make_float4(wi.x, wi.y, wi.z, 0.f);
+                            ps.T[p] = make_float4(T.x, T.y, T.z, pdf);
+                            ps.flags[p] = bsdf_pure_specular(m) ? 1 : 0;
+                            cont = true;
+                        }
+                    }
+                }
+            } else {
+                // Miss: background (Renderer.h:501-527, 596-612).
+                F3 bg = env_eval(sv.env, dir);
+                if (MODE == PGX_MODE_GUIDED_LI) {
+                    r_e = bg;
+                } else if (depth == 0 || prev_spec) {
+                    add = T * bg;
+                } else if (!(lum(bg) < 1e-8f)) {
+                    float pmf = 1.f / (float)sv.nlights;
+                    float pdf_light = env_pdf(sv.env, dir);
+                    if (pmf > 0.f && pdf_light > 0.f) {
+                        float pal = pmf * pdf_light;
+                        float wind = power_heuristic(prev_pdf, pal);
+                        add = (T * bg) * wind;
+                    }
+                }
+            }
+            if (MODE == PGX_MODE_GUIDED_LI) {
+                size_t ri = (size_t)depth * cap + p;
+                ps.rec_pos[ri] = make_float4(r_pos.x, r_pos.y, r_pos.z, r_store ? 1.f : 0.f);
+                ps.rec_nrm[ri] = make_float4(r_nrm.x, r_nrm.y, r_nrm.z, 0.f);
+                ps.rec_wi[ri] = make_float4(r_wi.x, r_wi.y, r_wi.z, 0.f);
+                ps.rec_w[ri] = make_float4(r_w.x, r_w.y, r_w.z, 0.f);
+                ps.rec_e[ri] = make_float4(r_e.x, r_e.y, r_e.z, 0.f);
+                ps.nrec[p] = depth + 1;
+            } else if (add.x != 0.f || add.y != 0.f || add.z != 0.f || !valid(add)) {
+                float4 l = ps.L[p];
+                ps.L[p] = make_float4(l.x + add.x, l.y + add.y, l.z + add.z, 0.f);
+            }
+            ps.rng[p] = rng;
+        }
+        if (MODE != PGX_MODE_GUIDED_LI) push_shadow(ps, depth, p, so, sdir, sc, active && want_shadow);
+        unsigned slot = warp_aggregated_add(&ps.qcount[depth + 1], active && cont);
+        if (active && cont) qn[slot] = p;
+    }
+}
+
+// Film::splat with the box filter (Imaging.h:186-217).
+__device__ __forceinline__ void splat(float* film, float* film2, int W, int H, float x, float y, F3 c) {
+    int bx = (int)floorf(x + 0.5f), by = (int)floorf(y + 0.5f);
+    int idx[9];
+    float wts[9];
+    int used = 0;
+    float total = 0.f;
+    for (int i = -1; i <= 1; i++)
+        for (int j = -1; j <= 1; j++) {
+            int px = bx + j, py = by + i;
+            if (px >= 0 && px < W && py >= 0 && py < H) {
+                idx[used] = py * W + px;
+                wts[used] = (fabsf((float)px - x) < 0.5f && fabsf((float)py - y) < 0.5f) ? 1.f : 0.f;
+                total += wts[used];
+                used++;
+            }
+        }
+    if (used > 0 && fabsf(total) > 1e-4f) {
+        for (int k = 0; k < used; k++) {
+            if (wts[k] == 0.f) continue;
+            F3 v = divs(c * wts[k], total);
+            atomicAdd(film + 3 * idx[k] + 0, v.x);
+            atomicAdd(film + 3 * idx[k] + 1, v.y);
+            atomicAdd(film + 3 * idx[k] + 2, v.z);
+            if (film2) {
+                atomicAdd(film2 + 3 * idx[k] + 0, v.x * v.x);
+                atomicAdd(film2 + 3 * idx[k] + 1, v.y * v.y);
+                atomicAdd(film2 + 3 * idx[k] + 2, v.z * v.z);
+            }
+        }
+    }
+}
+
+// End of frame: guided-Li back-propagation (Renderer.h:376-393), NaN/Inf
+// drop (Renderer.h:697-700) and the film splat.
+template <int MODE>
+__global__ void __launch_bounds__(kThreads) k_finalize(SceneView sv, PathState ps, FrameParams fp, float* film,
+                                                       float* film2) {
+    const int64_t npix = (int64_t)sv.width * sv.height;
+    const int64_t n = npix * fp.batch;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+        F3 col;
+        if (MODE == PGX_MODE_GUIDED_LI) {
+            int nr = ps.nrec[p];
+            bool collect = fp.collect >= 0 && (fp.spp0 + (int)(p / npix)) == fp.collect;
+            F3 li = zero3();
+            for (int i = nr - 1; i >= 0; i--) {
+                size_t ri = (size_t)i * ps.capacity + p;
+                float4 pos = ps.rec_pos[ri];
+                if (collect && pos.w != 0.f && valid(li) && lum(li) > 0.f) {
+                    unsigned slot = atomicAdd(ps.nvertices, 1u);
+                    if (slot < (unsigned)ps.vcapacity) {
+                        float4 nr4 = ps.rec_nrm[ri], wi = ps.rec_wi[ri];
+                        pgx_path_vertex v;
+                        v.position[0] = pos.x;
+                        v.position[1] = pos.y;
+                        v.position[2] = pos.z;
+                        v.normal[0] = nr4.x;
+                        v.normal[1] = nr4.y;
+                        v.normal[2] = nr4.z;
+                        v.wi[0] = wi.x;
+                        v.wi[1] = wi.y;
+                        v.wi[2] = wi.z;
+                        v.Li[0] = li.x;
+                        v.Li[1] = li.y;
+                        v.Li[2] = li.z;
+                        ps.vertices[slot] = v;
+                    }
+                }
+                li = f3(ps.rec_e[ri]) + (f3(ps.rec_w[ri]) * li);
+            }
+            col = li;
+        } else {
+            col = f3(ps.L[p]);
+        }
+        if (!valid(col)) continue;
+        float2 xy = ps.pix[p];
+        splat(film, film2, sv.width, sv.height, xy.x, xy.y, col);
+    }
+}
+
+inline unsigned grid_for(int64_t n) {
+    int64_t b = (n + kThreads - 1) / kThreads;
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 16));
+}
+
+RenderState* state_of(pgx_ctx* ctx) {
+    if (!ctx->render_state) ctx->render_state = new RenderState();
+    return static_cast<RenderState*>(ctx->render_state);
+}
+
+int ensure_state(pgx_ctx* ctx, RenderState* rs, int64_t cap, int rec_depth, int64_t vcap) {
+    if (cap > rs->capacity) {
+        PGX_CUDA_TRY(ctx, rs->o.reserve(sizeof(float4) * cap));
+        PGX_CUDA_TRY(ctx, rs->d.reserve(sizeof(float4) * cap));
+        PGX_CUDA_TRY(ctx, rs->T.reserve(sizeof(float4) * cap));
+        PGX_CUDA_TRY(ctx, rs->L.reserve(sizeof(float4) * cap));
+        PGX_CUDA_TRY(ctx, rs->hit.reserve(sizeof(float4) * cap));
+        PGX_CUDA_TRY(ctx, rs->pix.reserve(sizeof(float2) * cap));
+        PGX_CUDA_TRY(ctx, rs->rng.reserve(sizeof(uint64_t) * cap));
+        PGX_CUDA_TRY(ctx, rs->flags.reserve(sizeof(int) * cap));
+        PGX_CUDA_TRY(ctx, rs->nrec.reserve(sizeof(int) * cap));
+        PGX_CUDA_TRY(ctx, rs->q0.reserve(sizeof(int) * cap));
+        PGX_CUDA_TRY(ctx, rs->q1.reserve(sizeof(int) * cap));
+        PGX_CUDA_TRY(ctx, rs->sh_path.reserve(sizeof(int) * cap));
+        PGX_CUDA_TRY(ctx, rs->sh_o.reserve(sizeof(float4) * cap));
+        PGX_CUDA_TRY(ctx, rs->sh_d.reserve(sizeof(float4) * cap));
+        PGX_CUDA_TRY(ctx, rs->sh_c.reserve(sizeof(float4) * cap));
+        rs->capacity = cap;
+        rs->rec_depth = 0;
+    }
+    if (rec_depth > rs->rec_depth) {
+        size_t nrec = (size_t)rec_depth * rs->capacity;
+        PGX_CUDA_TRY(ctx, rs->rec_pos.reserve(sizeof(float4) * nrec));
+        PGX_CUDA_TRY(ctx, rs->rec_nrm.reserve(sizeof(float4) * nrec));
+        PGX_CUDA_TRY(ctx, rs->rec_wi.reserve(sizeof(float4) * nrec));
+        PGX_CUDA_TRY(ctx, rs->rec_w.reserve(sizeof(float4) * nrec));
+        PGX_CUDA_TRY(ctx, rs->rec_e.reserve(sizeof(float4) * nrec));
+        rs->rec_depth = rec_depth;
+    }
+    if (vcap > rs->vcapacity) {
+        PGX_CUDA_TRY(ctx, rs->vertices.reserve(sizeof(pgx_path_vertex) * vcap));
+        rs->vcapacity = vcap;
+    }
+    PGX_CUDA_TRY(ctx, rs->counters.reserve(sizeof(unsigned) * 2 * (kMaxDepthCap + 2) + sizeof(unsigned long long) * 4 +
+                                           sizeof(unsigned) * 4));
+    if (!rs->ev0) {
+        PGX_CUDA_TRY(ctx, cudaEventCreate(&rs->ev0));
+        PGX_CUDA_TRY(ctx, cudaEventCreate(&rs->ev1));
+    }
+    return PGX_OK;
+}
+
+PathState path_view(RenderState* rs) {
+    PathState ps;
+    ps.o = rs->o.as<float4>();
+    ps.d = rs->d.as<float4>();
+    ps.T = rs->T.as<float4>();
+    ps.L = rs->L.as<float4>();
+    ps.hit = rs->hit.as<float4>();
+    ps.pix = rs->pix.as<float2>();
+    ps.rng = rs->rng.as<uint64_t>();
+    ps.flags = rs->flags.as<int>();
+    ps.nrec = rs->nrec.as<int>();
+    ps.queue[0] = rs->q0.as<int>();
+    ps.queue[1] = rs->q1.as<int>();
+    ps.sh_path = rs->sh_path.as<int>();
+    ps.sh_o = rs->sh_o.as<float4>();
+    ps.sh_d = rs->sh_d.as<float4>();
+    ps.sh_c = rs->sh_c.as<float4>();
+    ps.rec_pos = rs->rec_pos.as<float4>();
+    ps.rec_nrm = rs->rec_nrm.as<float4>();
+    ps.rec_wi = rs->rec_wi.as<float4>();
+    ps.rec_w = rs->rec_w.as<float4>();
+    ps.rec_e = rs->rec_e.as<float4>();
+    unsigned* c = rs->counters.as<unsigned>();
+    ps.qcount = c;
+    ps.scount = c + (kMaxDepthCap + 2);
+    ps.stats = reinterpret_cast<unsigned long long*>(c + 2 * (kMaxDepthCap + 2));
+    ps.nvertices = c + 2 * (kMaxDepthCap + 2) + 8;
+    ps.vertices = rs->vertices.as<pgx_path_vertex>();
+    ps.capacity = rs->capacity;
+    ps.vcapacity = rs->vcapacity;
+    return ps;
+}
+
+SceneView scene_view(pgx_ctx* ctx) {
+    SceneView sv;
+    sv.bvh = bvh_view(ctx);
+    sv.shade = ctx->shade.as<TriShade>();
+    sv.mats = ctx->mats.as<DevMaterial>();
+    sv.lights = ctx->lights.as<DevAreaLight>();
+    sv.tex.info = ctx->textures.as<DevTexture>();
+    sv.tex.texels = ctx->texels.as<float>();
+    sv.env = ctx->env;
+    sv.cam = ctx->camera;
+    sv.bounds = ctx->bounds;
+    sv.n_area_lights = ctx->n_area_lights;
+    sv.nlights = ctx->nlights;
+    sv.has_env_light = (ctx->env.valid && ctx->env.power > 0.f) ? 1 : 0;
+    sv.width = ctx->width;
+    sv.height = ctx->height;
+    return sv;
+}
+
+// Enqueues one batch (fp.batch samples per pixel) on stream s.
+void enqueue_frame(pgx_ctx* ctx, RenderState* rs, const FrameParams& fp, cudaStream_t s) {
+    SceneView sv = scene_view(ctx);
+    PathState ps = path_view(rs);
+    GuideView gv = guide_view(ctx);
+    const int64_t n = (int64_t)ctx->width * ctx->height * fp.batch;
+    const unsigned g = grid_for(n);
+    cudaMemsetAsync(ps.qcount, 0, sizeof(unsigned) * 2 * (kMaxDepthCap + 2), s);
+    k_camgen<<<g, kThreads, 0, s>>>(sv, ps, fp);
+    for (int depth = 0; depth <= fp.max_depth; depth++) {
+        k_extend<<<g, kThreads, 0, s>>>(sv, ps, depth);
+        switch (fp.mode) {
+            case PGX_MODE_GUIDED_LI:
+                k_shade<PGX_MODE_GUIDED_LI><<<g, kThreads, 0, s>>>(sv, ps, fp, depth, gv);
+                break;
+            case PGX_MODE_GUIDED_QUADTREE:
+                k_shade<PGX_MODE_GUIDED_QUADTREE><<<g, kThreads, 0, s>>>(sv, ps, fp, depth, gv);
+                k_shadow<<<g, kThreads, 0, s>>>(sv, ps, depth);
+                break;
+            default:
+                k_shade<PGX_MODE_PLAIN><<<g, kThreads, 0, s>>>(sv, ps, fp, depth, gv);
+                k_shadow<<<g, kThreads, 0, s>>>(sv, ps, depth);
+                break;
+        }
+    }
+    float* film = ctx->film.as<float>();
+    float* film2 = ctx->film2.as<float>();
+    if (fp.mode == PGX_MODE_GUIDED_LI)
+        k_finalize<PGX_MODE_GUIDED_LI><<<g, kThreads, 0, s>>>(sv, ps, fp, film, film2);
+    else
+        k_finalize<PGX_MODE_PLAIN><<<g, kThreads, 0, s>>>(sv, ps, fp, film, film2);
+}
+
+int ensure_film(pgx_ctx* ctx) {
+    size_t bytes = sizeof(float) * 3 * (size_t)ctx->width * ctx->height;
+    if (ctx->film.bytes < bytes || !ctx->film.p) {
+        PGX_CUDA_TRY(ctx, ctx->film.reserve(bytes));
+        PGX_CUDA_TRY(ctx, ctx->film2.reserve(bytes));
+        PGX_CUDA_TRY(ctx, cudaMemsetAsync(ctx->film.p, 0, bytes, ctx->stream));
+        PGX_CUDA_TRY(ctx, cudaMemsetAsync(ctx->film2.p, 0, bytes, ctx->stream));
+        ctx->spp = 0;
+    }
+    return PGX_OK;
+}
+
+}  // namespace
+
+void render_state_free(pgx_ctx* ctx) {
+    RenderState* rs = static_cast<RenderState*>(ctx->render_state);
+    if (!rs) return;
+    if (rs->graph) cudaGraphExecDestroy(rs->graph);
+    if (rs->ev0) cudaEventDestroy(rs->ev0);
+    if (rs->ev1) cudaEventDestroy(rs->ev1);
+    delete rs;
+    ctx->render_state = nullptr;
+}
+
+int64_t render_vertex_count(pgx_ctx* ctx) {
+    RenderState* rs = static_cast<RenderState*>(ctx->render_state);
+    return rs ? rs->nvertices_last : 0;
+}
+
+const pgx_path_vertex* render_vertices(pgx_ctx* ctx) {
+    RenderState* rs = static_cast<RenderState*>(ctx->render_state);
+    return rs ? rs->vertices.as<pgx_path_vertex>() : nullptr;
+}
 
 extern "C" int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t frames) {
-    (void)cfg;
-    (void)frames;
-    return pgx_fail(ctx, PGX_ERR_STATE, "pgx_render: not built yet");
+    if (!ctx) return PGX_ERR_INVALID_ARG;
+    ctx->err.clear();
+    if (!cfg || frames < 0) return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_render: bad arguments");
+    if (cfg->mode < PGX_MODE_PLAIN || cfg->mode > PGX_MODE_GUIDED_QUADTREE)
+        return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_render: unknown mode %d", cfg->mode);
+    if (cfg->max_depth < 0 || cfg->max_depth > kMaxDepthCap)
+        return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_render: max_depth must be in [0, %d]", kMaxDepthCap);
+    if (!ctx->has_scene) return pgx_fail(ctx, PGX_ERR_STATE, "pgx_render: no scene");
+    if (!ctx->has_bvh) return pgx_fail(ctx, PGX_ERR_STATE, "pgx_render: no BVH");
+    if (cfg->mode == PGX_MODE_GUIDED_QUADTREE && !guide_ready(ctx))
+        return pgx_fail(ctx, PGX_ERR_STATE, "pgx_render: guided mode needs a radiance cache (pgx_cache_build)");
+    PGX_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    PGX_TRY(ensure_film(ctx));
+    if (frames == 0) return PGX_OK;
+    RenderState* rs = state_of(ctx);
+    const int64_t npix = (int64_t)ctx->width * ctx->height;
+    // Samples per wavefront: enough paths to fill the GPU, bounded memory.
+    const int64_t target_paths = 1 << 22;
+    int batch = (int)std::max<int64_t>(1, std::min<int64_t>(frames, target_paths / std::max<int64_t>(npix, 1)));
+    const bool guided_li = cfg->mode == PGX_MODE_GUIDED_LI;
+    const int rec_depth = guided_li ? cfg->max_depth + 1 : 0;
+    // Path vertices of the last frame with SPP < 16 are kept (Renderer.h:720-746).
+    int collect = -1;
+    if (guided_li && cfg->record_paths) {
+        int last = std::min(ctx->spp + frames, kCollectionSPP - 1);
+        if (last > ctx->spp) collect = last - 1;
+    }
+    const int64_t vcap = collect >= 0 ? npix * (cfg->max_depth + 1) : 0;
+    PGX_TRY(ensure_state(ctx, rs, npix * batch, rec_depth, vcap));
+    cudaStream_t s = ctx->stream;
+    PathState ps = path_view(rs);
+    PGX_CUDA_TRY(ctx, cudaMemsetAsync(ps.stats, 0, sizeof(unsigned long long) * 4 + sizeof(unsigned) * 4, s));
+    PGX_CUDA_TRY(ctx, cudaEventRecord(rs->ev0, s));
+    int done = 0;
+    while (done < frames) {
+        FrameParams fp;
+        fp.mode = cfg->mode;
+        fp.max_depth = cfg->max_depth;
+        fp.seed = cfg->seed;
+        fp.spp0 = ctx->spp + done;
+        fp.batch = std::min(batch, frames - done);
+        fp.collect = (collect >= fp.spp0 && collect < fp.spp0 + fp.batch) ? collect : -1;
+        fp.guide_fraction = cfg->guide_fraction;
+        enqueue_frame(ctx, rs, fp, s);
+        PGX_CUDA_TRY(ctx, cudaGetLastError());
+        done += fp.batch;
+    }
+    PGX_CUDA_TRY(ctx, cudaEventRecord(rs->ev1, s));
+    unsigned long long st[4] = {0, 0, 0, 0};
+    unsigned nv = 0;
+    PGX_CUDA_TRY(ctx, cudaMemcpyAsync(st, ps.stats, sizeof(st), cudaMemcpyDeviceToHost, s));
+    PGX_CUDA_TRY(ctx, cudaMemcpyAsync(&nv, ps.nvertices, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    PGX_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    float ms = 0.f;
+    PGX_CUDA_TRY(ctx, cudaEventElapsedTime(&ms, rs->ev0, rs->ev1));
+    ctx->spp += frames;
+    pgx_render_stats& rst = ctx->rstats;
+    rst = pgx_render_stats{};
+    rst.paths = npix * frames;
+    rst.extension_rays = (int64_t)st[0];
+    rst.shadow_rays = (int64_t)st[1];
+    rst.ms_total = ms;
+    if (collect >= 0) {
+        rs->nvertices_last = std::min<int64_t>(nv, rs->vcapacity);
+        rst.path_vertices = rs->nvertices_last;
+        PGX_TRY(cache_build_device(ctx, rs->vertices.as<pgx_path_vertex>(), rs->nvertices_last));
+    }
+    return PGX_OK;
 }
-extern "C" int pgx_clear(pgx_ctx* ctx) { return pgx_fail(ctx, PGX_ERR_STATE, "not built yet"); }
+
+extern "C" int pgx_clear(pgx_ctx* ctx) {
+    if (!ctx) return PGX_ERR_INVALID_ARG;
+    ctx->err.clear();
+    if (!ctx->has_scene) return pgx_fail(ctx, PGX_ERR_STATE, "pgx_clear: no scene");
+    PGX_TRY(ensure_film(ctx));
+    size_t bytes = sizeof(float) * 3 * (size_t)ctx->width * ctx->height;
+    PGX_CUDA_TRY(ctx, cudaMemsetAsync(ctx->film.p, 0, bytes, ctx->stream));
+    PGX_CUDA_TRY(ctx, cudaMemsetAsync(ctx->film2.p, 0, bytes, ctx->stream));
+    PGX_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->spp = 0;
+    return PGX_OK;
+}
+
 extern "C" int pgx_get_spp(pgx_ctx* ctx, int32_t* spp) {
-    (void)spp;
-    return pgx_fail(ctx, PGX_ERR_STATE, "not built yet");
+    if (!ctx || !spp) return PGX_ERR_INVALID_ARG;
+    *spp = ctx->spp;
+    return PGX_OK;
 }
+
 extern "C" int pgx_film_read(pgx_ctx* ctx, float* rgb, float* rgb2, int32_t* spp) {
-    (void)rgb;
-    (void)rgb2;
-    (void)spp;
-    return pgx_fail(ctx, PGX_ERR_STATE, "not built yet");
+    if (!ctx) return PGX_ERR_INVALID_ARG;
+    ctx->err.clear();
+    if (!ctx->has_scene) return pgx_fail(ctx, PGX_ERR_STATE, "pgx_film_read: no scene");
+    PGX_TRY(ensure_film(ctx));
+    size_t bytes = sizeof(float) * 3 * (size_t)ctx->width * ctx->height;
+    if (rgb) PGX_CUDA_TRY(ctx, cudaMemcpyAsync(rgb, ctx->film.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    if (rgb2) PGX_CUDA_TRY(ctx, cudaMemcpyAsync(rgb2, ctx->film2.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    PGX_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    if (spp) *spp = ctx->spp;
+    return PGX_OK;
 }
+
 extern "C" int pgx_render_get_stats(pgx_ctx* ctx, pgx_render_stats* out) {
-    (void)out;
-    return pgx_fail(ctx, PGX_ERR_STATE, "not built yet");
-}
-extern "C" int pgx_cache_build(pgx_ctx* ctx, const pgx_path_vertex* r, int64_t n) {
-    (void)r;
-    (void)n;
-    return pgx_fail(ctx, PGX_ERR_STATE, "not built yet");
-}
-extern "C" int pgx_cache_build_from_render(pgx_ctx* ctx) { return pgx_fail(ctx, PGX_ERR_STATE, "not built yet"); }
-extern "C" int pgx_cache_get_stats(pgx_ctx* ctx, pgx_cache_stats* out) {
-    (void)out;
-    return pgx_fail(ctx, PGX_ERR_STATE, "not built yet");
-}
-extern "C" int pgx_cache_export(pgx_ctx* ctx, pgx_cache_node* nodes, int64_t* nn, pgx_path_vertex* r, int64_t* nr) {
-    (void)nodes;
-    (void)nn;
-    (void)r;
-    (void)nr;
-    return pgx_fail(ctx, PGX_ERR_STATE, "not built yet");
-}
-extern "C" int pgx_cache_knn(pgx_ctx* ctx, const float* q, int64_t nq, int32_t k, int32_t* idx, float* d2) {
-    (void)q;
-    (void)nq;
-    (void)k;
-    (void)idx;
-    (void)d2;
-    return pgx_fail(ctx, PGX_ERR_STATE, "not built yet");
+    if (!ctx || !out) return PGX_ERR_INVALID_ARG;
+    *out = ctx->rstats;
+    return PGX_OK;
 }

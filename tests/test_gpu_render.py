@@ -1,0 +1,111 @@
+"""GPU wavefront renderer against the reference's integrators.
+
+Per-pixel: the reference's pathTrace / guidedPath driven by the same PCG32
+stream per (pixel, sample) (oracle/ref_harness.cpp) must give the same
+radiance except where a libm-vs-CUDA rounding flips a branch; statistical:
+against the reference's own RayTracer::render with its own sampler."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from pathguidingdissertation_gb300 import abi, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _small_interior():
+    return scenes.interior(seed=3, target_tris=20000, n_objects=40, width=64, height=36, env_width=256,
+                           env_height=128)
+
+
+def _compare(gpu, ref, tol=1e-3, max_bad=0.02):
+    """Pixels agree to `tol` relative except a small fraction."""
+    g = gpu.reshape(-1, 3).astype(np.float64)
+    r = ref.reshape(-1, 3).astype(np.float64)
+    err = np.abs(g - r).max(axis=1) / np.maximum(np.abs(r).max(axis=1), 1e-3)
+    bad = np.mean(err > tol)
+    assert bad <= max_bad, f"{bad:.4f} of pixels differ by more than {tol}"
+    rel = abs(g.sum() - r.sum()) / max(abs(r.sum()), 1e-9)
+    assert rel < 0.01, f"image sums differ by {rel:.4f}"
+    return bad
+
+
+@pytest.mark.parametrize("mode", [abi.MODE_PLAIN, abi.MODE_GUIDED_LI])
+@pytest.mark.parametrize("scene", ["cornell", "interior"])
+def test_render_per_pixel_vs_reference(ctx, reference, mode, scene):
+    desc = scenes.cornell_box(seed=1, width=64, height=64) if scene == "cornell" else _small_interior()
+    spp = 4
+    ctx.upload(desc)
+    nodes, idx = reference.bvh_build(desc.triangles)
+    ctx.bvh_import(nodes, idx)  # the reference's own tree: identical hits
+    ctx.clear()
+    ctx.render(spp, mode=mode, seed=11, max_depth=8)
+    film, _, got_spp = ctx.film()
+    assert got_spp == spp
+    rs = reference.scene(desc)
+    ref_film, _, _ = rs.render_pcg(mode == abi.MODE_GUIDED_LI, 11, 0, spp, threads=8)
+    _compare(film, ref_film)
+
+
+def test_guided_li_vertices_vs_reference(ctx, reference):
+    desc = scenes.cornell_box(seed=1, width=48, height=48)
+    ctx.upload(desc)
+    nodes, idx = reference.bvh_build(desc.triangles)
+    ctx.bvh_import(nodes, idx)
+    ctx.clear()
+    ctx.render(1, mode=abi.MODE_GUIDED_LI, seed=5, max_depth=8, record_paths=True)
+    st = ctx.render_stats()
+    _, recs = ctx.cache_export()
+    rs = reference.scene(desc)
+    _, verts, _ = rs.render_pcg(True, 5, 0, 1, threads=4, collect=0, vcap=1 << 20)
+    assert st.path_vertices == len(recs)
+    # Same multiset of vertices up to rounding: compare sorted positions.
+    assert abs(len(recs) - len(verts)) <= max(3, 0.01 * len(verts))
+    a = np.sort(recs["position"][:, 0])
+    b = np.sort(verts["position"][:, 0])
+    n = min(len(a), len(b))
+    assert np.mean(np.abs(a[:n] - b[:n]) < 1e-3) > 0.97
+
+
+def test_render_statistical_vs_native_reference(ctx, reference):
+    """Per-16x16-tile means within 3 sigma of the reference's own render()."""
+    desc = scenes.cornell_box(seed=1, width=64, height=64)
+    frames = 64
+    ctx.upload(desc)
+    ctx.bvh_build()
+    ctx.clear()
+    ctx.render(frames, mode=abi.MODE_GUIDED_LI, seed=3, max_depth=8)
+    film, film2, spp = ctx.film(squares=True)
+    ref = type(reference)(variant="fast")
+    rs = ref.scene(desc, threads=8)
+    rfilm, rspp, _, _ = rs.render_native(frames)
+    assert rspp == frames and spp == frames
+    t = 16
+    H, W = 64, 64
+    g = film.reshape(H // t, t, W // t, t, 3).sum(axis=(1, 3)) / (spp * t * t)
+    g2 = film2.reshape(H // t, t, W // t, t, 3).sum(axis=(1, 3)) / (spp * t * t)
+    r = rfilm.reshape(H // t, t, W // t, t, 3).sum(axis=(1, 3)) / (rspp * t * t)
+    var = np.maximum(g2 - g * g, 1e-12) / (spp * t * t)
+    z = np.abs(g - r) / np.sqrt(2 * var)
+    assert np.mean(z < 3.0) > 0.95, z.max()
+
+
+def test_render_api_semantics(ctx):
+    desc = scenes.cornell_box(seed=2, width=32, height=32)
+    ctx.upload(desc)
+    ctx.bvh_build()
+    ctx.clear()
+    assert ctx.spp() == 0
+    ctx.render(1)
+    ctx.render(2)
+    assert ctx.spp() == 3
+    a, _, _ = ctx.film()
+    ctx.clear()
+    assert ctx.spp() == 0
+    ctx.render(3)
+    b, _, _ = ctx.film()
+    # Streams are keyed by (pixel, sample): batching does not change the result.
+    assert np.allclose(a, b, rtol=1e-5, atol=1e-6)
+    st = ctx.render_stats()
+    assert st.paths == 32 * 32 * 3 and st.extension_rays >= st.paths
