@@ -1,0 +1,302 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the wavefront path tracer (one JSON line).
+
+Workload (default): the procedural interior — an 8x4x6 room with a 1.5x1
+window, 400 boxes and UV-spheres tessellated to 201,792 triangles (40 %
+Lambert, 40 % GGX conductor, 20 % glass), a 2048x1024 HDR sky with a sun
+lobe, 1280x720 pixels, maximum depth 10.  One step renders one sample per
+pixel (921,600 paths) with NEE + MIS (`RayTracer::pathTrace`,
+Renderer.h:531-613).  The metric is Mrays/s: extension plus shadow rays
+traced per second of device time.
+
+  python bench.py [--steps K] [--warmup W] [--impl pgx|reference]
+                  [--mode plain|guided_quadtree] [--workload interior|cornell]
+
+`--impl reference` times the reference's own CPU renderer
+(`RayTracer::render`, Renderer.h:648-747, plain build) on all host cores
+over the same scene, one frame per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+L2_FLUSH_BYTES = 256 << 20  # > 129 MB L2
+
+
+def make_workload(name: str):
+    from pathguidingdissertation_gb300 import scenes
+    if name == "cornell":
+        return scenes.cornell_box(seed=1, width=256, height=256), 8, "cornell box, 36 tris, 256x256, depth 8"
+    desc = scenes.interior(seed=2)
+    return desc, 10, (f"procedural interior, {desc.ntris} tris, env 2048x1024, "
+                      f"{desc.camera['width']}x{desc.camera['height']}, depth 10")
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during a region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self) -> dict:
+        rows = []
+        try:
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        except OSError:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d.get("hbm_gbs", 6800.0), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def profile_traffic(kernel: str) -> tuple[float | None, str | None]:
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary."""
+    p = ROOT / "profiles" / "traffic.json"
+    if not p.exists():
+        return None, None
+    d = json.loads(p.read_text())
+    e = d.get(kernel)
+    if not e:
+        return None, None
+    return float(e["bytes_per_launch"]), e.get("note")
+
+
+def cpu_baseline_reference(desc, frames_budget_s: float = 12.0) -> dict | None:
+    """The reference's own plain renderer on all host cores, bounded sample."""
+    try:
+        from oracle.ffi import Reference, reference_available
+        if not reference_available():
+            return None
+        ref = Reference(variant="plain_fast")
+    except Exception as e:  # noqa: BLE001
+        return {"unavailable": f"reference harness: {e}"}
+    cores = os.cpu_count() or 1
+    rs = ref.scene(desc, threads=cores)
+    _, _, rays1, s1 = rs.render_native(1)
+    frames = max(1, min(20, int(frames_budget_s / max(s1, 1e-3))))
+    _, _, rays, secs = rs.render_native(frames)
+    rs.close()
+    return {"value": rays / secs / 1e6, "unit": "Mrays/s", "cores": cores, "kind": "reference",
+            "sample": f"{frames} frame(s) of RayTracer::render (plain build, -O3) on the same scene, "
+                      f"{rays} rays in {secs:.2f} s"}
+
+
+def run_pgx(args) -> dict:
+    import torch
+
+    from pathguidingdissertation_gb300 import abi
+    from pathguidingdissertation_gb300 import build as pkg_build
+    from pathguidingdissertation_gb300.api import Context
+
+    pkg_build.build()
+    desc, depth, wl = make_workload(args.workload)
+    mode = {"plain": abi.MODE_PLAIN, "guided_quadtree": abi.MODE_GUIDED_QUADTREE}[args.mode]
+    ctx = Context(0)
+    ctx.upload(desc)
+    ctx.bvh_build()
+    if mode == abi.MODE_GUIDED_QUADTREE:
+        # Radiance cache from a 1-spp guided-Li pass (the reference's records).
+        ctx.render(1, mode=abi.MODE_GUIDED_LI, seed=99, max_depth=depth, record_paths=True)
+    ctx.clear()
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    for i in range(args.warmup):
+        ctx.render(1, mode=mode, seed=1, max_depth=depth, profile=True)
+    torch.cuda.synchronize()
+    rays = paths = 0
+    ms = ms_ext = 0.0
+    ext_visits = ext_tris = ext_launches = launches = 0
+    with ClockSampler() as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            ctx.render(1, mode=mode, seed=1, max_depth=depth, profile=True)
+            st = ctx.render_stats()
+            rays += st.extension_rays + st.shadow_rays
+            paths += st.paths
+            ms += st.ms_total
+            ms_ext += st.ms_extend
+            ext_visits += st.extend_interior_visits
+            ext_tris += st.extend_tri_tests
+            ext_launches += st.extend_launches
+            launches += st.kernel_launches
+        torch.cuda.synchronize()
+    clocks = clk.summary()
+    value = rays / (ms * 1e-3) / 1e6
+
+    # End to end through the C ABI: camera from host, render, film to pinned host memory.
+    H, W = desc.camera["height"], desc.camera["width"]
+    host_film = torch.empty((H, W, 3), dtype=torch.float32, pin_memory=True)
+    import ctypes as C
+    from pathguidingdissertation_gb300.api import camera_struct
+    cam = camera_struct(desc.camera)
+    cfg = abi.RenderConfig(mode, depth, 1, 0.5, 0, 0)
+    spp = C.c_int32()
+    e2e_rays = 0
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        ctx.check(ctx.lib.pgx_set_camera(ctx.h, C.byref(cam)))
+        ctx.check(ctx.lib.pgx_render(ctx.h, C.byref(cfg), 1))
+        ctx.check(ctx.lib.pgx_film_read(ctx.h, host_film.data_ptr(), None, C.byref(spp)))
+        st = ctx.render_stats()
+        e2e_rays += st.extension_rays + st.shadow_rays
+    e2e_s = time.perf_counter() - t0
+    ctx.close()
+
+    peaks = measured_peaks()
+    alg_bytes = ext_visits * 64 + ext_tris * 48
+    achieved = alg_bytes / (ms_ext * 1e-3) / 1e9 if ms_ext > 0 else None
+    traffic, traffic_note = profile_traffic("k_extend")
+    roofline = {
+        "kernel": "k_extend (closest-hit traversal)",
+        "bound": "hbm",
+        "achieved": achieved,
+        "peak": peaks["hbm_gbs"],
+        "peak_source": peaks["source"],
+        "unit": "GB/s",
+        "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
+        "traffic": traffic,
+        "traffic_note": traffic_note,
+        "alg_bytes_per_launch": alg_bytes / max(ext_launches, 1),
+        "avg_launch_ms": ms_ext / max(ext_launches, 1),
+        "extend_share_of_step": ms_ext / ms if ms else None,
+    }
+    cpu = cpu_baseline_reference(desc) if not args.no_cpu_baseline else None
+    return {
+        "metric": "Mrays/s",
+        "value": value,
+        "unit": "Mrays/s",
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded procedural scene)",
+        "config": {"workload": wl, "mode": args.mode, "paths_per_step": paths // max(args.steps, 1),
+                   "spp_per_step": 1, "l2": "flushed (256 MiB write) before every timed step"},
+        "mpaths_per_s": paths / (ms * 1e-3) / 1e6,
+        "rays_per_path": rays / max(paths, 1),
+        "gpu_launches": launches,
+        "e2e": {"value": e2e_rays / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": C.sizeof(abi.Camera),
+                "d2h_bytes_per_step": H * W * 3 * 4},
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+    }
+
+
+def run_reference(args) -> dict:
+    from oracle.ffi import Reference, reference_available
+    desc, _, wl = make_workload(args.workload)
+    if not reference_available():
+        return {"impl": "reference", "unavailable": "reference sources not staged on this machine"}
+    ref = Reference(variant="plain_fast")
+    cores = os.cpu_count() or 1
+    rs = ref.scene(desc, threads=cores)
+    if args.warmup:
+        rs.render_native(args.warmup)
+    rays = 0
+    secs = 0.0
+    for _ in range(args.steps):
+        _, _, r, s = rs.render_native(1)
+        rays += r
+        secs += s
+    rs.close()
+    value = rays / secs / 1e6
+    return {
+        "impl": "reference",
+        "metric": "Mrays/s",
+        "value": value,
+        "unit": "Mrays/s",
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": secs * 1e3 / max(args.steps, 1),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded procedural scene)",
+        "config": {"workload": wl + " (reference: its fixed depth 8)", "mode": "plain"},
+        "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": cores, "kind": "reference",
+                         "sample": f"{args.steps} frame(s) of RayTracer::render (plain build, -O3)"},
+        "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["pgx", "reference"], default="pgx")
+    ap.add_argument("--mode", choices=["plain", "guided_quadtree"], default="plain")
+    ap.add_argument("--workload", choices=["interior", "cornell"], default="interior")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    if args.gpus != 1 or int(os.environ.get("WORLD_SIZE", "1")) != 1:
+        # The path is replicated, not sharded; this build runs on one GPU.
+        if rank == 0:
+            print(json.dumps({"impl": args.impl, "unavailable": "one GPU per run: use --gpus 1"}))
+        return
+    if args.warmup < 0 or args.steps < 1:
+        raise SystemExit("--steps must be >= 1 and --warmup >= 0")
+    out = run_reference(args) if args.impl == "reference" else run_pgx(args)
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

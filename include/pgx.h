@@ -174,14 +174,25 @@ typedef struct pgx_render_config {
     uint64_t seed;         /* PCG32 streams are hash(seed, pixel, sample)  */
     float guide_fraction;  /* probability of sampling the guide (0.5)      */
     int32_t record_paths;  /* keep path vertices for the cache (guided Li) */
-    int32_t reserved;
+    int32_t flags;         /* PGX_RENDER_PROFILE: per-stage events/counters */
 } pgx_render_config;
 
+/* pgx_render_config.flags */
+#define PGX_RENDER_PROFILE 1
+
+/* Statistics of the last pgx_render call.  The per-stage times and the
+ * node/triangle fetch counts are filled only with PGX_RENDER_PROFILE. */
 typedef struct pgx_render_stats {
     int64_t paths;
     int64_t extension_rays;
     int64_t shadow_rays;
     int64_t path_vertices;
+    int64_t kernel_launches;
+    int64_t extend_launches;
+    int64_t extend_interior_visits; /* 64-byte node records fetched        */
+    int64_t extend_tri_tests;       /* 48-byte triangles fetched           */
+    int64_t shadow_interior_visits;
+    int64_t shadow_tri_tests;
     double ms_total;
     double ms_extend;
     double ms_shadow;
@@ -272,6 +283,11 @@ int pgx_trace_counters(pgx_ctx* ctx, int64_t* nodes_visited, int64_t* tris_teste
 /* Camera rays (`Camera::generateRay`, Scene.h:253-265) for pixel sample
  * positions px, py (n of each). */
 int pgx_camera_rays(pgx_ctx* ctx, const float* px, const float* py, int64_t n, pgx_ray* rays);
+
+/* Moves the camera (RTCamera::updateCamera -> Camera::updateView,
+ * SceneLoader.h:85-89, Scene.h:32-43).  The image size must stay the same;
+ * the film is not cleared (call pgx_clear as the reference's viewer does). */
+int pgx_set_camera(pgx_ctx* ctx, const pgx_camera* camera);
 
 /* `RayTracer::render` (Renderer.h:648-747) called `frames` times: each frame
  * is one sample per pixel accumulated into the film. */

@@ -200,6 +200,9 @@ class Reference:
         cnt = self.lib.orcref_bvh_build(_p(tris), n, _p(nodes), _p(idx))
         return nodes[:cnt].copy(), idx[:n].copy()
 
+    def world(self, tris: np.ndarray) -> "RefWorld":
+        return RefWorld(self, tris)
+
     def scene(self, desc, threads: int = 0) -> "RefScene":
         return RefScene(self, desc, threads)
 
@@ -246,9 +249,6 @@ class RefScene:
 
     def clear(self):
         self.ref.lib.orcref_clear(self.h)
-
-    def world(self, tris: np.ndarray) -> "RefWorld":
-        return RefWorld(self, tris)
 
 
 class RefWorld:

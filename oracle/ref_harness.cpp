@@ -344,12 +344,16 @@ double orcref_render_native(void* h, int32_t frames, float* film_rgb, int32_t* s
     RefScene* rs = static_cast<RefScene*>(h);
     const long long rays0 = g_rays_total.load();
     double secs = 0.0;
+    // The guided build prints cache statistics after every cache rebuild
+    // (Renderer.h:224-231); keep stdout quiet while timing.
+    std::streambuf* old = std::cout.rdbuf(nullptr);
     for (int32_t f = 0; f < frames; f++) {
         auto t0 = std::chrono::steady_clock::now();
         rs->rt.render();
         auto t1 = std::chrono::steady_clock::now();
         secs += std::chrono::duration<double>(t1 - t0).count();
     }
+    std::cout.rdbuf(old);
     if (film_rgb) std::memcpy(film_rgb, rs->rt.film->film, sizeof(float) * 3 * (size_t)rs->width * rs->height);
     if (spp) *spp = rs->rt.getSPP();
     if (rays_out) *rays_out = g_rays_total.load() - rays0;

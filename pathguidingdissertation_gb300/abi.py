@@ -63,15 +63,21 @@ class BvhStats(C.Structure):
                 ("max_leaf_size", C.c_int32), ("sah_cost", C.c_double), ("build_ms", C.c_double)]
 
 
+RENDER_PROFILE = 1
+
+
 class RenderConfig(C.Structure):
     _fields_ = [("mode", C.c_int32), ("max_depth", C.c_int32), ("seed", C.c_uint64),
-                ("guide_fraction", C.c_float), ("record_paths", C.c_int32), ("reserved", C.c_int32)]
+                ("guide_fraction", C.c_float), ("record_paths", C.c_int32), ("flags", C.c_int32)]
 
 
 class RenderStats(C.Structure):
     _fields_ = [("paths", C.c_int64), ("extension_rays", C.c_int64), ("shadow_rays", C.c_int64),
-                ("path_vertices", C.c_int64), ("ms_total", C.c_double), ("ms_extend", C.c_double),
-                ("ms_shadow", C.c_double), ("ms_shade", C.c_double)]
+                ("path_vertices", C.c_int64), ("kernel_launches", C.c_int64), ("extend_launches", C.c_int64),
+                ("extend_interior_visits", C.c_int64), ("extend_tri_tests", C.c_int64),
+                ("shadow_interior_visits", C.c_int64), ("shadow_tri_tests", C.c_int64),
+                ("ms_total", C.c_double), ("ms_extend", C.c_double), ("ms_shadow", C.c_double),
+                ("ms_shade", C.c_double)]
 
 
 class CacheStats(C.Structure):
@@ -101,6 +107,7 @@ SIGNATURES = {
     "pgx_trace_any_device": (C.c_int, [_P, _P, _I64, _P, _P]),
     "pgx_trace_counters": (C.c_int, [_P, C.POINTER(_I64), C.POINTER(_I64)]),
     "pgx_camera_rays": (C.c_int, [_P, _P, _P, _I64, _P]),
+    "pgx_set_camera": (C.c_int, [_P, C.POINTER(Camera)]),
     "pgx_render": (C.c_int, [_P, C.POINTER(RenderConfig), _I32]),
     "pgx_clear": (C.c_int, [_P]),
     "pgx_get_spp": (C.c_int, [_P, C.POINTER(_I32)]),

@@ -61,9 +61,7 @@ class Context:
         if scene.env is not None:
             env_keep = np.ascontiguousarray(scene.env, dtype=np.float32)
             env = abi.Texture(env_keep.shape[1], env_keep.shape[0], env_keep.ctypes.data)
-        c = scene.camera
-        cam = abi.Camera((C.c_float * 3)(*c["from_"]), (C.c_float * 3)(*c["to"]), (C.c_float * 3)(*c["up"]),
-                         float(c["fov"]), int(c["width"]), int(c["height"]), int(c.get("flip_x", 0)))
+        cam = camera_struct(scene.camera)
         self.check(self.lib.pgx_scene_upload(self.h, ptr(tris), len(tris), ptr(mats), len(mats),
                                              C.cast(tex_arr, C.c_void_p) if texs else None, len(texs),
                                              C.byref(env) if env is not None else None, C.byref(cam)))
@@ -117,9 +115,13 @@ class Context:
         return out
 
     # ---- rendering -------------------------------------------------------------
+    def set_camera(self, camera: dict) -> None:
+        self.check(self.lib.pgx_set_camera(self.h, C.byref(camera_struct(camera))))
+
     def render(self, frames: int = 1, mode: int = abi.MODE_PLAIN, seed: int = 1, max_depth: int = 8,
-               guide_fraction: float = 0.5, record_paths: bool = False) -> None:
-        cfg = abi.RenderConfig(mode, max_depth, seed, guide_fraction, int(record_paths), 0)
+               guide_fraction: float = 0.5, record_paths: bool = False, profile: bool = False) -> None:
+        cfg = abi.RenderConfig(mode, max_depth, seed, guide_fraction, int(record_paths),
+                               abi.RENDER_PROFILE if profile else 0)
         self.check(self.lib.pgx_render(self.h, C.byref(cfg), frames))
 
     def clear(self) -> None:
@@ -170,6 +172,11 @@ class Context:
         d2 = np.zeros((len(q), k), np.float32)
         self.check(self.lib.pgx_cache_knn(self.h, ptr(q), len(q), k, ptr(idx), ptr(d2)))
         return idx, d2
+
+
+def camera_struct(c: dict) -> abi.Camera:
+    return abi.Camera((C.c_float * 3)(*c["from_"]), (C.c_float * 3)(*c["to"]), (C.c_float * 3)(*c["up"]),
+                      float(c["fov"]), int(c["width"]), int(c["height"]), int(c.get("flip_x", 0)))
 
 
 class Scene:

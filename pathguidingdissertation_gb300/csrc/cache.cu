@@ -376,8 +376,8 @@ __device__ void quickselect(int* idx, int lo, int hi, int nth, const float4* pos
         float piv = (a < b) ? ((b < c) ? b : ((a < c) ? c : a)) : ((a < c) ? a : ((b < c) ? c : b));
         int i = left, j = right;
         while (i <= j) {
-            while (axis_of(pos[idx[i]], ax) < piv) i++;
-            while (piv < axis_of(pos[idx[j]], ax)) j--;
+            while (i <= right && axis_of(pos[idx[i]], ax) < piv) i++;
+            while (j >= left && piv < axis_of(pos[idx[j]], ax)) j--;
             if (i <= j) {
                 int t = idx[i];
                 idx[i] = idx[j];

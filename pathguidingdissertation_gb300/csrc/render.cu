@@ -32,6 +32,8 @@ namespace {
 constexpr int kThreads = 128;
 constexpr int kMaxDepthCap = 16;
 constexpr int kCollectionSPP = 128 / 8;  // Renderer.h:721
+constexpr int kStats = 8;                 // 64-bit statistics counters
+constexpr int kProfEvents = 4 * (kMaxDepthCap + 2);
 
 // Per-path state, structure of arrays.
 struct PathState {
@@ -59,7 +61,7 @@ struct PathState {
     // counters: queue length per depth, shadow count per depth, stats
     unsigned* qcount;  // [kMaxDepthCap + 2]
     unsigned* scount;  // [kMaxDepthCap + 2]
-    unsigned long long* stats;  // [0] ext rays, [1] shadow rays, [2] path vertices
+    unsigned long long* stats;  // [0] ext rays [1] shadow rays [2,3] extend nodes/tris [4,5] shadow nodes/tris
     pgx_path_vertex* vertices;
     unsigned* nvertices;
     int64_t capacity;
@@ -80,6 +82,7 @@ struct RenderState {
     uint64_t graph_seed = 0;
     int graph_spp0 = -1;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t prof[kProfEvents] = {};
 };
 
 struct SceneView {
@@ -105,6 +108,7 @@ struct FrameParams {
     int batch;       // samples per pixel in this batch
     int collect;     // sample index whose path vertices are recorded (-1: none)
     float guide_fraction;
+    int profile;     // count node/triangle fetches
 };
 
 // ---- camera rays (Camera::generateRay, Scene.h:253-265; jitter Renderer.h:679-681)
@@ -147,39 +151,64 @@ __global__ void __launch_bounds__(kThreads) k_camgen(SceneView sv, PathState ps,
 }
 
 // ---- closest hit for the queue of this depth ----------------------------------
+__device__ __forceinline__ void add_counts(unsigned long long* dst, unsigned long long a, unsigned long long b) {
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xFFFFFFFFu, a, o);
+        b += __shfl_xor_sync(0xFFFFFFFFu, b, o);
+    }
+    if ((threadIdx.x & 31) == 0 && (a | b)) {
+        atomicAdd(dst, a);
+        atomicAdd(dst + 1, b);
+    }
+}
+
+template <bool COUNT>
 __global__ void __launch_bounds__(kThreads) k_extend(SceneView sv, PathState ps, int depth) {
     const unsigned n = ps.qcount[depth];
     const int* __restrict__ q = ps.queue[depth & 1];
     unsigned long long ni = 0, nt = 0;
-    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        int p = q[i];
-        float4 a = ps.o[p], b = ps.d[p];
-        int id, st;
-        float t, u = 0.f, v = 0.f;
-        bvh_trace<false, false>(sv.bvh, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), FLT_MAX, id, t, u, v, st, ni, nt);
-        if (st) id = -1;  // corrupt tree or stack overflow: treat as a miss
-        ps.hit[p] = make_float4(__int_as_float(id), t, u, v);
+    const unsigned stride = gridDim.x * blockDim.x;
+    const unsigned rounds = (n + stride - 1) / stride;
+    for (unsigned r = 0; r < rounds; r++) {
+        unsigned i = blockIdx.x * blockDim.x + threadIdx.x + r * stride;
+        if (i < n) {
+            int p = q[i];
+            float4 a = ps.o[p], b = ps.d[p];
+            int id, st;
+            float t, u = 0.f, v = 0.f;
+            bvh_trace<false, COUNT>(sv.bvh, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), FLT_MAX, id, t, u, v, st, ni, nt);
+            if (st) id = -1;  // corrupt tree or stack overflow: treat as a miss
+            ps.hit[p] = make_float4(__int_as_float(id), t, u, v);
+        }
     }
+    if (COUNT) add_counts(&ps.stats[2], ni, nt);
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ps.stats[0], (unsigned long long)n);
 }
 
 // ---- any hit for the shadow queue of this depth --------------------------------
+template <bool COUNT>
 __global__ void __launch_bounds__(kThreads) k_shadow(SceneView sv, PathState ps, int depth) {
     const unsigned n = ps.scount[depth];
     unsigned long long ni = 0, nt = 0;
-    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float4 a = ps.sh_o[i], b = ps.sh_d[i];
-        int id, st;
-        float t, u, v;
-        bool occluded =
-            bvh_trace<true, false>(sv.bvh, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, id, t, u, v, st, ni, nt);
-        if (!occluded && !st) {
-            int p = ps.sh_path[i];
-            float4 c = ps.sh_c[i];
-            float4 l = ps.L[p];
-            ps.L[p] = make_float4(l.x + c.x, l.y + c.y, l.z + c.z, 0.f);
+    const unsigned stride = gridDim.x * blockDim.x;
+    const unsigned rounds = (n + stride - 1) / stride;
+    for (unsigned r = 0; r < rounds; r++) {
+        unsigned i = blockIdx.x * blockDim.x + threadIdx.x + r * stride;
+        if (i < n) {
+            float4 a = ps.sh_o[i], b = ps.sh_d[i];
+            int id, st;
+            float t, u, v;
+            bool occluded =
+                bvh_trace<true, COUNT>(sv.bvh, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, id, t, u, v, st, ni, nt);
+            if (!occluded && !st) {
+                int p = ps.sh_path[i];
+                float4 c = ps.sh_c[i];
+                float4 l = ps.L[p];
+                ps.L[p] = make_float4(l.x + c.x, l.y + c.y, l.z + c.z, 0.f);
+            }
         }
     }
+    if (COUNT) add_counts(&ps.stats[4], ni, nt);
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ps.stats[1], (unsigned long long)n);
 }
 
@@ -595,11 +624,12 @@ int ensure_state(pgx_ctx* ctx, RenderState* rs, int64_t cap, int rec_depth, int6
         PGX_CUDA_TRY(ctx, rs->vertices.reserve(sizeof(pgx_path_vertex) * vcap));
         rs->vcapacity = vcap;
     }
-    PGX_CUDA_TRY(ctx, rs->counters.reserve(sizeof(unsigned) * 2 * (kMaxDepthCap + 2) + sizeof(unsigned long long) * 4 +
+    PGX_CUDA_TRY(ctx, rs->counters.reserve(sizeof(unsigned) * 2 * (kMaxDepthCap + 2) + sizeof(unsigned long long) * kStats +
                                            sizeof(unsigned) * 4));
     if (!rs->ev0) {
         PGX_CUDA_TRY(ctx, cudaEventCreate(&rs->ev0));
         PGX_CUDA_TRY(ctx, cudaEventCreate(&rs->ev1));
+        for (int i = 0; i < kProfEvents; i++) PGX_CUDA_TRY(ctx, cudaEventCreate(&rs->prof[i]));
     }
     return PGX_OK;
 }
@@ -630,7 +660,7 @@ PathState path_view(RenderState* rs) {
     ps.qcount = c;
     ps.scount = c + (kMaxDepthCap + 2);
     ps.stats = reinterpret_cast<unsigned long long*>(c + 2 * (kMaxDepthCap + 2));
-    ps.nvertices = c + 2 * (kMaxDepthCap + 2) + 8;
+    ps.nvertices = c + 2 * (kMaxDepthCap + 2) + 2 * kStats;
     ps.vertices = rs->vertices.as<pgx_path_vertex>();
     ps.capacity = rs->capacity;
     ps.vcapacity = rs->vcapacity;
@@ -656,30 +686,53 @@ SceneView scene_view(pgx_ctx* ctx) {
     return sv;
 }
 
-// Enqueues one batch (fp.batch samples per pixel) on stream s.
-void enqueue_frame(pgx_ctx* ctx, RenderState* rs, const FrameParams& fp, cudaStream_t s) {
+// Stage times of one profiled batch (milliseconds).
+struct StageTimes {
+    double extend = 0, shade = 0, shadow = 0;
+};
+
+// Enqueues one batch (fp.batch samples per pixel) on stream s; returns the
+// number of kernels launched.  With fp.profile, events bracket every stage
+// (read back by stage_times after the stream is synchronised).
+int enqueue_frame(pgx_ctx* ctx, RenderState* rs, const FrameParams& fp, cudaStream_t s) {
     SceneView sv = scene_view(ctx);
     PathState ps = path_view(rs);
     GuideView gv = guide_view(ctx);
     const int64_t n = (int64_t)ctx->width * ctx->height * fp.batch;
     const unsigned g = grid_for(n);
+    const bool prof = fp.profile != 0;
+    int launches = 0;
     cudaMemsetAsync(ps.qcount, 0, sizeof(unsigned) * 2 * (kMaxDepthCap + 2), s);
     k_camgen<<<g, kThreads, 0, s>>>(sv, ps, fp);
+    launches++;
     for (int depth = 0; depth <= fp.max_depth; depth++) {
-        k_extend<<<g, kThreads, 0, s>>>(sv, ps, depth);
+        if (prof) cudaEventRecord(rs->prof[4 * depth + 0], s);
+        if (prof)
+            k_extend<true><<<g, kThreads, 0, s>>>(sv, ps, depth);
+        else
+            k_extend<false><<<g, kThreads, 0, s>>>(sv, ps, depth);
+        if (prof) cudaEventRecord(rs->prof[4 * depth + 1], s);
         switch (fp.mode) {
             case PGX_MODE_GUIDED_LI:
                 k_shade<PGX_MODE_GUIDED_LI><<<g, kThreads, 0, s>>>(sv, ps, fp, depth, gv);
                 break;
             case PGX_MODE_GUIDED_QUADTREE:
                 k_shade<PGX_MODE_GUIDED_QUADTREE><<<g, kThreads, 0, s>>>(sv, ps, fp, depth, gv);
-                k_shadow<<<g, kThreads, 0, s>>>(sv, ps, depth);
                 break;
             default:
                 k_shade<PGX_MODE_PLAIN><<<g, kThreads, 0, s>>>(sv, ps, fp, depth, gv);
-                k_shadow<<<g, kThreads, 0, s>>>(sv, ps, depth);
                 break;
         }
+        launches += 2;
+        if (prof) cudaEventRecord(rs->prof[4 * depth + 2], s);
+        if (fp.mode != PGX_MODE_GUIDED_LI) {
+            if (prof)
+                k_shadow<true><<<g, kThreads, 0, s>>>(sv, ps, depth);
+            else
+                k_shadow<false><<<g, kThreads, 0, s>>>(sv, ps, depth);
+            launches++;
+        }
+        if (prof) cudaEventRecord(rs->prof[4 * depth + 3], s);
     }
     float* film = ctx->film.as<float>();
     float* film2 = ctx->film2.as<float>();
@@ -687,6 +740,19 @@ void enqueue_frame(pgx_ctx* ctx, RenderState* rs, const FrameParams& fp, cudaStr
         k_finalize<PGX_MODE_GUIDED_LI><<<g, kThreads, 0, s>>>(sv, ps, fp, film, film2);
     else
         k_finalize<PGX_MODE_PLAIN><<<g, kThreads, 0, s>>>(sv, ps, fp, film, film2);
+    return launches + 1;
+}
+
+void stage_times(RenderState* rs, int max_depth, StageTimes& t) {
+    for (int depth = 0; depth <= max_depth; depth++) {
+        float a = 0.f, b = 0.f, c = 0.f;
+        cudaEventElapsedTime(&a, rs->prof[4 * depth + 0], rs->prof[4 * depth + 1]);
+        cudaEventElapsedTime(&b, rs->prof[4 * depth + 1], rs->prof[4 * depth + 2]);
+        cudaEventElapsedTime(&c, rs->prof[4 * depth + 2], rs->prof[4 * depth + 3]);
+        t.extend += a;
+        t.shade += b;
+        t.shadow += c;
+    }
 }
 
 int ensure_film(pgx_ctx* ctx) {
@@ -709,6 +775,8 @@ void render_state_free(pgx_ctx* ctx) {
     if (rs->graph) cudaGraphExecDestroy(rs->graph);
     if (rs->ev0) cudaEventDestroy(rs->ev0);
     if (rs->ev1) cudaEventDestroy(rs->ev1);
+    for (int i = 0; i < kProfEvents; i++)
+        if (rs->prof[i]) cudaEventDestroy(rs->prof[i]);
     delete rs;
     ctx->render_state = nullptr;
 }
@@ -755,7 +823,10 @@ extern "C" int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t fr
     PGX_TRY(ensure_state(ctx, rs, npix * batch, rec_depth, vcap));
     cudaStream_t s = ctx->stream;
     PathState ps = path_view(rs);
-    PGX_CUDA_TRY(ctx, cudaMemsetAsync(ps.stats, 0, sizeof(unsigned long long) * 4 + sizeof(unsigned) * 4, s));
+    PGX_CUDA_TRY(ctx, cudaMemsetAsync(ps.stats, 0, sizeof(unsigned long long) * kStats + sizeof(unsigned) * 4, s));
+    const bool prof = (cfg->flags & PGX_RENDER_PROFILE) != 0;
+    StageTimes times;
+    int64_t launches = 0, batches = 0;
     PGX_CUDA_TRY(ctx, cudaEventRecord(rs->ev0, s));
     int done = 0;
     while (done < frames) {
@@ -767,12 +838,18 @@ extern "C" int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t fr
         fp.batch = std::min(batch, frames - done);
         fp.collect = (collect >= fp.spp0 && collect < fp.spp0 + fp.batch) ? collect : -1;
         fp.guide_fraction = cfg->guide_fraction;
-        enqueue_frame(ctx, rs, fp, s);
+        fp.profile = prof ? 1 : 0;
+        launches += enqueue_frame(ctx, rs, fp, s);
+        batches++;
         PGX_CUDA_TRY(ctx, cudaGetLastError());
+        if (prof) {
+            PGX_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+            stage_times(rs, fp.max_depth, times);
+        }
         done += fp.batch;
     }
     PGX_CUDA_TRY(ctx, cudaEventRecord(rs->ev1, s));
-    unsigned long long st[4] = {0, 0, 0, 0};
+    unsigned long long st[kStats] = {};
     unsigned nv = 0;
     PGX_CUDA_TRY(ctx, cudaMemcpyAsync(st, ps.stats, sizeof(st), cudaMemcpyDeviceToHost, s));
     PGX_CUDA_TRY(ctx, cudaMemcpyAsync(&nv, ps.nvertices, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
@@ -785,13 +862,34 @@ extern "C" int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t fr
     rst.paths = npix * frames;
     rst.extension_rays = (int64_t)st[0];
     rst.shadow_rays = (int64_t)st[1];
+    rst.extend_interior_visits = (int64_t)st[2];
+    rst.extend_tri_tests = (int64_t)st[3];
+    rst.shadow_interior_visits = (int64_t)st[4];
+    rst.shadow_tri_tests = (int64_t)st[5];
+    rst.kernel_launches = launches;
+    rst.extend_launches = batches * (cfg->max_depth + 1);
     rst.ms_total = ms;
+    rst.ms_extend = times.extend;
+    rst.ms_shade = times.shade;
+    rst.ms_shadow = times.shadow;
     if (collect >= 0) {
         rs->nvertices_last = std::min<int64_t>(nv, rs->vcapacity);
         rst.path_vertices = rs->nvertices_last;
         PGX_TRY(cache_build_device(ctx, rs->vertices.as<pgx_path_vertex>(), rs->nvertices_last));
     }
     return PGX_OK;
+}
+
+int camera_setup(pgx_ctx* ctx, const pgx_camera* camera);
+
+extern "C" int pgx_set_camera(pgx_ctx* ctx, const pgx_camera* camera) {
+    if (!ctx) return PGX_ERR_INVALID_ARG;
+    ctx->err.clear();
+    if (!camera) return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_set_camera: null camera");
+    if (!ctx->has_scene) return pgx_fail(ctx, PGX_ERR_STATE, "pgx_set_camera: no scene");
+    if (camera->width != ctx->width || camera->height != ctx->height)
+        return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_set_camera: image size differs from the scene's");
+    return camera_setup(ctx, camera);
 }
 
 extern "C" int pgx_clear(pgx_ctx* ctx) {

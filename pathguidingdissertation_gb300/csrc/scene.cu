@@ -205,6 +205,8 @@ inline unsigned blocks_for(int64_t n, int t) { return (unsigned)((n + t - 1) / t
 
 }  // namespace
 
+int camera_setup(pgx_ctx* ctx, const pgx_camera* camera);
+
 extern "C" int pgx_scene_upload(pgx_ctx* ctx, const pgx_triangle* tris, int64_t ntris, const pgx_material* mats,
                                 int32_t nmats, const pgx_texture* textures, int32_t ntextures,
                                 const pgx_texture* envmap, const pgx_camera* camera) {
@@ -384,9 +386,17 @@ extern "C" int pgx_scene_upload(pgx_ctx* ctx, const pgx_triangle* tris, int64_t 
         PGX_CUDA_TRY(ctx, cudaStreamSynchronize(s));
     }
 
-    // Camera (loadScene, SceneLoader.h:226-243; Camera::init/updateView,
-    // Scene.h:25-43).
+    PGX_TRY(camera_setup(ctx, camera));
+    ctx->has_scene = true;
+    PGX_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    return PGX_OK;
+}
+
+// Camera (loadScene, SceneLoader.h:226-243; Camera::init/updateView,
+// Scene.h:25-43).
+int camera_setup(pgx_ctx* ctx, const pgx_camera* camera) {
     const pgx_camera& c = *camera;
+    if (c.width <= 0 || c.height <= 0) return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "camera: bad image size");
     ctx->host_camera = c;
     HMat P = hm_perspective(0.001f, 10000.0f, (float)c.width / (float)c.height, c.fov_degrees);
     HMat V = hm_invert(hm_lookat(HV{c.from[0], c.from[1], c.from[2]}, HV{c.to[0], c.to[1], c.to[2]},
@@ -403,7 +413,5 @@ extern "C" int pgx_scene_upload(pgx_ctx* ctx, const pgx_triangle* tris, int64_t 
     dc.height = (float)c.height;
     ctx->width = c.width;
     ctx->height = c.height;
-    ctx->has_scene = true;
-    PGX_CUDA_TRY(ctx, cudaStreamSynchronize(s));
     return PGX_OK;
 }

@@ -88,25 +88,26 @@ class MeshBuilder:
         """Planar quad origin + s*du + t*dv, split into res x res cells."""
         origin, du, dv = (np.asarray(x, np.float64) for x in (origin, du, dv))
         s = np.linspace(0.0, 1.0, res + 1)
-        tris, uvs = [], []
-        for i in range(res):
-            for j in range(res):
-                c00 = origin + s[i] * du + s[j] * dv
-                c10 = origin + s[i + 1] * du + s[j] * dv
-                c01 = origin + s[i] * du + s[j + 1] * dv
-                c11 = origin + s[i + 1] * du + s[j + 1] * dv
-                tris += [[c00, c10, c11], [c00, c11, c01]]
-                uvs += [[[s[i], s[j]], [s[i + 1], s[j]], [s[i + 1], s[j + 1]]],
-                        [[s[i], s[j]], [s[i + 1], s[j + 1]], [s[i], s[j + 1]]]]
-        tris = np.asarray(tris)
+        i, j = np.meshgrid(np.arange(res), np.arange(res), indexing="ij")
+        i = i.ravel()
+        j = j.ravel()
+        s0, s1, t0, t1 = s[i], s[i + 1], s[j], s[j + 1]
+
+        def pt(a, b):
+            return origin + a[:, None] * du + b[:, None] * dv
+
+        c00, c10, c01, c11 = pt(s0, t0), pt(s1, t0), pt(s0, t1), pt(s1, t1)
+        tris = np.stack([np.stack([c00, c10, c11], 1), np.stack([c00, c11, c01], 1)], 1).reshape(-1, 3, 3)
+        uv = np.stack([np.stack([np.stack([s0, t0], -1), np.stack([s1, t0], -1), np.stack([s1, t1], -1)], 1),
+                       np.stack([np.stack([s0, t0], -1), np.stack([s1, t1], -1), np.stack([s0, t1], -1)], 1)],
+                      1).reshape(-1, 3, 2)
         # Orient the winding so the face normal agrees with `normal`.
         fn = np.cross(tris[:, 1] - tris[:, 0], tris[:, 2] - tris[:, 0])
         flip = (fn @ np.asarray(normal, np.float64)) < 0
         tris[flip] = tris[flip][:, [0, 2, 1]]
-        uvs = np.asarray(uvs)
-        uvs[flip] = uvs[flip][:, [0, 2, 1]]
+        uv[flip] = uv[flip][:, [0, 2, 1]]
         nrm = np.broadcast_to(np.asarray(normal, np.float64), tris.shape)
-        self.add(tris, nrm, uvs, mat)
+        self.add(tris, nrm, uv, mat)
 
     def box(self, centre, size, yaw: float, mat: int, res: int = 1, inward: bool = False) -> None:
         """Box rotated by `yaw` about +y; faces split into res x res cells."""
@@ -129,33 +130,33 @@ class MeshBuilder:
                 self.quad_grid(c + R @ o, R @ du, R @ dv, sgn * (R @ n), res, mat)
 
     def sphere(self, centre, radius: float, slices: int, stacks: int, mat: int) -> None:
+        """UV sphere: 2 * slices * (stacks - 1) triangles, smooth normals."""
         c = np.asarray(centre, np.float64)
         th = np.linspace(0, math.pi, stacks + 1)
         ph = np.linspace(0, 2 * math.pi, slices + 1)
         T, P = np.meshgrid(th, ph, indexing="ij")
         dirs = np.stack([np.sin(T) * np.cos(P), np.cos(T), np.sin(T) * np.sin(P)], -1)
         pts = c + radius * dirs
-        uv = np.stack([P / (2 * math.pi), T / math.pi], -1)
+        uvg = np.stack([P / (2 * math.pi), T / math.pi], -1)
+        i, j = np.meshgrid(np.arange(stacks), np.arange(slices), indexing="ij")
+        i = i.ravel()
+        j = j.ravel()
+        upper = i != 0            # triangle (a, d, c) exists below the north cap row
+        lower = i != stacks - 1   # triangle (a, c, b) exists above the south cap row
+        quads = [((i, j), (i, j + 1), (i + 1, j + 1), upper), ((i, j), (i + 1, j + 1), (i + 1, j), lower)]
         tris, nrms, uvs = [], [], []
-        for i in range(stacks):
-            for j in range(slices):
-                a, b, cc, d = (i, j), (i + 1, j), (i + 1, j + 1), (i, j + 1)
-                quads = []
-                if i != 0:
-                    quads.append((a, d, cc))
-                if i != stacks - 1:
-                    quads.append((a, cc, b))
-                for q in quads:
-                    tris.append([pts[x] for x in q])
-                    nrms.append([dirs[x] for x in q])
-                    uvs.append([uv[x] for x in q])
-        tris = np.asarray(tris)
+        for a, b, cc, keep in quads:
+            idx = [(x[0][keep], x[1][keep]) for x in (a, b, cc)]
+            tris.append(np.stack([pts[x] for x in idx], 1))
+            nrms.append(np.stack([dirs[x] for x in idx], 1))
+            uvs.append(np.stack([uvg[x] for x in idx], 1))
+        tris = np.concatenate(tris)
+        nrms = np.concatenate(nrms)
+        uvs = np.concatenate(uvs)
         fn = np.cross(tris[:, 1] - tris[:, 0], tris[:, 2] - tris[:, 0])
-        flip = np.einsum("ij,ij->i", fn, np.asarray(nrms)[:, 0]) < 0
+        flip = np.einsum("ij,ij->i", fn, nrms[:, 0]) < 0
         tris[flip] = tris[flip][:, [0, 2, 1]]
-        nrms = np.asarray(nrms)
         nrms[flip] = nrms[flip][:, [0, 2, 1]]
-        uvs = np.asarray(uvs)
         uvs[flip] = uvs[flip][:, [0, 2, 1]]
         self.add(tris, nrms, uvs, mat)
 
@@ -249,11 +250,15 @@ def interior(seed: int = 2, target_tris: int = 200_000, n_objects: int = 400, wi
         mb.quad_grid((X, y0, z0), (0, 0, z1 - z0), (0, y1 - y0, 0), (-1, 0, 0), 2, wall)
     base_tris = sum(len(p) for p in mb.p)
 
-    # Furniture: half boxes, half spheres, tessellated to the triangle budget.
-    per_obj = max(12, (target_tris - base_tris) // n_objects)
-    sphere_slices = max(4, int(round(math.sqrt(per_obj / 2.0) * 1.41)))
-    sphere_stacks = max(3, int(round(per_obj / (2.0 * sphere_slices))) + 1)
+    # Furniture: half boxes, half spheres, tessellated to the triangle budget
+    # (a box has 12 res^2 triangles, a sphere 2 slices (stacks - 1)).
+    n_box = (n_objects + 1) // 2
+    n_sph = n_objects // 2
+    per_obj = max(12.0, (target_tris - base_tris) / max(n_objects, 1))
     box_res = max(1, int(round(math.sqrt(per_obj / 12.0))))
+    rest = max(4.0, (target_tris - base_tris - n_box * 12 * box_res * box_res) / max(n_sph, 1))
+    sphere_slices = max(4, int(round(math.sqrt(rest))))
+    sphere_stacks = max(3, int(round(rest / (2.0 * sphere_slices))) + 1)
     kinds = rng.choice(3, size=n_objects, p=[0.4, 0.4, 0.2])
     sizes = np.exp(rng.normal(-1.0, 0.5, n_objects))
     for i in range(n_objects):
