@@ -272,6 +272,25 @@ int pgx_trace_closest(pgx_ctx* ctx, const pgx_ray* rays, int64_t n, pgx_hit* hit
 /* `BVHNode::traverseVisible` (Geometry.h:514-567): visible[i] = 1 when no
  * triangle is hit in (1e-4, tmax). */
 int pgx_trace_any(pgx_ctx* ctx, const pgx_ray* rays, int64_t n, uint8_t* visible);
+/* Allocation-free variant of pgx_trace_closest.  No counterpart in the
+ * reference (whose BVH queries are plain CPU calls).  It is meant for
+ * callers that cannot have the library allocate device memory while they
+ * run: for example an application whose device memory is handed out by its
+ * own pool allocator (or by another framework that reserved the GPU's memory
+ * up front), where a cudaMalloc inside the library would fail or break the
+ * memory budget, or a frame loop that must not wait on the allocator.
+ * The call allocates and frees nothing: rays and hits are staged in a fixed
+ * device array of PGX_NOALLOC_MAX_RAYS rays that libpgx declares at file
+ * scope, so the memory is reserved on every GPU that loads the library for
+ * the life of the process.  Larger batches are rejected with
+ * PGX_ERR_INVALID_ARG (split them).  Hits are identical to pgx_trace_closest.
+ * The first call on a device looks up the array's device address (set-up);
+ * make that first call before any stream capture starts.  All
+ * calls, from every context on a device, share the one array: calls that
+ * overlap on the GPU (another thread, another context) race on it and must
+ * be serialised by the caller. */
+#define PGX_NOALLOC_MAX_RAYS 65536
+int pgx_trace_closest_noalloc(pgx_ctx* ctx, const pgx_ray* rays, int64_t n, pgx_hit* hits);
 /* Device-pointer variants on a caller stream (cudaStream_t or NULL). */
 int pgx_trace_closest_device(pgx_ctx* ctx, const pgx_ray* d_rays, int64_t n,
                              pgx_hit* d_hits, void* stream);

@@ -23,6 +23,7 @@ PGX_ERR_CUDA = 3
 PGX_ERR_OVERFLOW = 4
 PGX_ERR_TIMEOUT = 5
 PGX_ERR_STATE = 6
+NOALLOC_MAX_RAYS = 65536  # PGX_NOALLOC_MAX_RAYS
 
 # BSDF kinds
 BSDF_DIFFUSE, BSDF_MIRROR, BSDF_CONDUCTOR, BSDF_GLASS, BSDF_DIELECTRIC, BSDF_ORENNAYAR, BSDF_PLASTIC = range(7)
@@ -103,6 +104,7 @@ SIGNATURES = {
     "pgx_bvh_get_stats": (C.c_int, [_P, C.POINTER(BvhStats)]),
     "pgx_trace_closest": (C.c_int, [_P, _P, _I64, _P]),
     "pgx_trace_any": (C.c_int, [_P, _P, _I64, _P]),
+    "pgx_trace_closest_noalloc": (C.c_int, [_P, _P, _I64, _P]),
     "pgx_trace_closest_device": (C.c_int, [_P, _P, _I64, _P, _P]),
     "pgx_trace_any_device": (C.c_int, [_P, _P, _I64, _P, _P]),
     "pgx_trace_counters": (C.c_int, [_P, C.POINTER(_I64), C.POINTER(_I64)]),

@@ -96,6 +96,14 @@ class Context:
         self.check(self.lib.pgx_trace_closest(self.h, ptr(rays), len(rays), ptr(hits)))
         return hits
 
+    def trace_closest_noalloc(self, rays: np.ndarray) -> np.ndarray:
+        """pgx_trace_closest_noalloc: same hits, no device allocation, at
+        most abi.NOALLOC_MAX_RAYS rays per call."""
+        rays = np.ascontiguousarray(rays, abi.RAY)
+        hits = np.zeros(len(rays), abi.HIT)
+        self.check(self.lib.pgx_trace_closest_noalloc(self.h, ptr(rays), len(rays), ptr(hits)))
+        return hits
+
     def trace_any(self, rays: np.ndarray) -> np.ndarray:
         rays = np.ascontiguousarray(rays, abi.RAY)
         vis = np.zeros(len(rays), np.uint8)

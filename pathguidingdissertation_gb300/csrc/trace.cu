@@ -2,6 +2,7 @@
 // BVHNode::traverseVisible, Geometry.h:448-567) and camera rays
 // (Camera::generateRay, Scene.h:253-265).
 #include <algorithm>
+#include <mutex>
 
 #include "pgx_ctx.h"
 #include "pgx_trace.cuh"
@@ -128,6 +129,76 @@ int trace_host(pgx_ctx* ctx, const pgx_ray* rays, int64_t n, void* out, bool any
 }
 
 }  // namespace
+
+// ---- allocation-free batch query -------------------------------------------
+// Fixed device scratch for pgx_trace_closest_noalloc: trace counters, then
+// room for PGX_NOALLOC_MAX_RAYS rays and as many hits (3 MiB + 256 B).  It is
+// a file-scope device array, so every GPU that loads libpgx holds it until
+// the process exits, and all calls share it.
+constexpr size_t kNoAllocCounterBytes = 256;
+constexpr size_t kNoAllocRayBytes = sizeof(pgx_ray) * (size_t)PGX_NOALLOC_MAX_RAYS;
+constexpr size_t kNoAllocHitBytes = sizeof(pgx_hit) * (size_t)PGX_NOALLOC_MAX_RAYS;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocCounterBytes + kNoAllocRayBytes +
+                                                                 kNoAllocHitBytes];
+static_assert(sizeof(TraceCounters) <= kNoAllocCounterBytes, "counters must fit their slot");
+
+namespace {
+constexpr int kMaxDevices = 256;
+std::mutex g_noalloc_mutex;
+unsigned char* g_noalloc_base[kMaxDevices] = {};
+
+// Device address of the scratch on ctx's device.  In host code the array's
+// name only stands in for the symbol, so its address must be asked for with
+// the device current; it is looked up once per device and cached.
+int noalloc_scratch(pgx_ctx* ctx, unsigned char** out) {
+    if (ctx->device < 0 || ctx->device >= kMaxDevices)
+        return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_trace_closest_noalloc: device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_base[ctx->device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return pgx_fail(ctx, PGX_ERR_CUDA, "pgx_trace_closest_noalloc: cudaGetSymbolAddress failed: %s",
+                            cudaGetErrorString(e));
+        g_noalloc_base[ctx->device] = static_cast<unsigned char*>(p);
+    }
+    *out = g_noalloc_base[ctx->device];
+    return PGX_OK;
+}
+}  // namespace
+
+extern "C" int pgx_trace_closest_noalloc(pgx_ctx* ctx, const pgx_ray* rays, int64_t n, pgx_hit* hits) {
+    PGX_TRY(check_trace_args(ctx, rays, n, hits));
+    if (n > PGX_NOALLOC_MAX_RAYS)
+        return pgx_fail(ctx, PGX_ERR_INVALID_ARG,
+                        "pgx_trace_closest_noalloc: %lld rays exceed the fixed scratch of %d rays; split the batch",
+                        (long long)n, PGX_NOALLOC_MAX_RAYS);
+    PGX_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    unsigned char* base = nullptr;
+    PGX_TRY(noalloc_scratch(ctx, &base));
+    TraceCounters* counters = reinterpret_cast<TraceCounters*>(base);
+    pgx_ray* d_rays = reinterpret_cast<pgx_ray*>(base + kNoAllocCounterBytes);
+    pgx_hit* d_hits = reinterpret_cast<pgx_hit*>(base + kNoAllocCounterBytes + kNoAllocRayBytes);
+    cudaStream_t s = ctx->stream;
+    // The array keeps the previous call's contents: the counters must start at zero.
+    PGX_CUDA_TRY(ctx, cudaMemsetAsync(counters, 0, sizeof(TraceCounters), s));
+    if (n > 0) {
+        PGX_CUDA_TRY(ctx, cudaMemcpyAsync(d_rays, rays, sizeof(pgx_ray) * n, cudaMemcpyHostToDevice, s));
+        int64_t blocks = (n + kTraceThreads - 1) / kTraceThreads;
+        unsigned grid = (unsigned)std::min<int64_t>(blocks, 152 * 64);
+        k_trace<false, true><<<grid, kTraceThreads, 0, s>>>(bvh_view(ctx), d_rays, n, d_hits, nullptr, counters);
+        PGX_CUDA_TRY(ctx, cudaGetLastError());
+    }
+    TraceCounters hc{};
+    PGX_CUDA_TRY(ctx, cudaMemcpyAsync(&hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, s));
+    if (n > 0) PGX_CUDA_TRY(ctx, cudaMemcpyAsync(hits, d_hits, sizeof(pgx_hit) * n, cudaMemcpyDeviceToHost, s));
+    PGX_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    ctx->last_interior = hc.interior_visits;
+    ctx->last_tris = hc.tri_tests;
+    if (hc.overflow & 2u) return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "traversal met a reference outside the BVH");
+    if (hc.overflow) return pgx_fail(ctx, PGX_ERR_OVERFLOW, "traversal stack overflow (depth > %d)", PGX_STACK_SIZE);
+    return PGX_OK;
+}
 
 extern "C" int pgx_trace_closest(pgx_ctx* ctx, const pgx_ray* rays, int64_t n, pgx_hit* hits) {
     return trace_host(ctx, rays, n, hits, false);
