@@ -120,6 +120,8 @@ SIGNATURES = {
     "pgx_cache_get_stats": (C.c_int, [_P, C.POINTER(CacheStats)]),
     "pgx_cache_export": (C.c_int, [_P, _P, C.POINTER(_I64), _P, C.POINTER(_I64)]),
     "pgx_cache_knn": (C.c_int, [_P, _P, _I64, _I32, _P, _P]),
+    "pgx_guide_pdf": (C.c_int, [_P, _P, _P, _I64, _P]),
+    "pgx_guide_sample": (C.c_int, [_P, _P, _P, _I64, _P, _P]),
 }
 
 _lib: C.CDLL | None = None

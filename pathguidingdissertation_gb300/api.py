@@ -174,6 +174,21 @@ class Context:
         self.check(self.lib.pgx_cache_export(self.h, ptr(nodes), C.byref(nn), ptr(recs), C.byref(nr)))
         return nodes, recs
 
+    def guide_pdf(self, positions: np.ndarray, dirs: np.ndarray) -> np.ndarray:
+        p = np.ascontiguousarray(positions, np.float32).reshape(-1, 3)
+        d = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+        out = np.zeros(len(p), np.float32)
+        self.check(self.lib.pgx_guide_pdf(self.h, ptr(p), ptr(d), len(p), ptr(out)))
+        return out
+
+    def guide_sample(self, positions: np.ndarray, u2: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+        p = np.ascontiguousarray(positions, np.float32).reshape(-1, 3)
+        u = np.ascontiguousarray(u2, np.float32).reshape(-1, 2)
+        dirs = np.zeros((len(p), 3), np.float32)
+        pdf = np.zeros(len(p), np.float32)
+        self.check(self.lib.pgx_guide_sample(self.h, ptr(p), ptr(u), len(p), ptr(dirs), ptr(pdf)))
+        return dirs, pdf
+
     def cache_knn(self, queries: np.ndarray, k: int) -> tuple[np.ndarray, np.ndarray]:
         q = np.ascontiguousarray(queries, np.float32).reshape(-1, 3)
         idx = np.zeros((len(q), k), np.int32)

@@ -44,10 +44,10 @@ def _deps() -> list[Path]:
     return sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + sorted(INCLUDE.glob("*.h"))
 
 
-# Per-file flags: the integrator rounds every product and sum separately,
-# like the reference's scalar code (traversal uses explicit _rn intrinsics
-# and is exact regardless).
-FILE_FLAGS = {"render.cu": ["-fmad=false"]}
+# Per-file flags: the integrator and the cache round every product and sum
+# separately, like the reference's scalar code and the float32 checks
+# (traversal uses explicit _rn intrinsics and is exact regardless).
+FILE_FLAGS = {"render.cu": ["-fmad=false"], "cache.cu": ["-fmad=false"]}
 
 
 def _compile(src: Path, extra: list[str]) -> Path:

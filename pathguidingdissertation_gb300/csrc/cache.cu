@@ -615,6 +615,40 @@ __global__ void k_knn(const CacheTravNode* __restrict__ nodes, const float4* __r
     }
 }
 
+// Guide pdf / sample for explicit positions (pgx_guide_pdf / _sample).
+__global__ void k_guide_query(GuideView g, const float* __restrict__ pos, const float* __restrict__ in, int64_t n,
+                              int sample, float* __restrict__ dirs, float* __restrict__ pdf) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    F3 x = f3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+    int root = guide_region_root(g, x);
+    const float inv4pi = 1.f / (4.f * 3.14159265f);
+    if (sample) {
+        F3 w = f3(0.f, 0.f, 1.f);
+        float p = 0.f;
+        if (root >= 0) {
+            float u, v;
+            quad_sample(g.qnodes, root, in[2 * i], in[2 * i + 1], u, v);
+            w = uv_to_dir(u, v);
+            float pu, pv;
+            dir_to_uv(w, pu, pv);
+            p = quad_pdf(g.qnodes, root, pu, pv) * inv4pi;
+        }
+        dirs[3 * i] = w.x;
+        dirs[3 * i + 1] = w.y;
+        dirs[3 * i + 2] = w.z;
+        pdf[i] = p;
+    } else {
+        float p = 0.f;
+        if (root >= 0) {
+            float u, v;
+            dir_to_uv(normalize(f3(in[3 * i], in[3 * i + 1], in[3 * i + 2])), u, v);
+            p = quad_pdf(g.qnodes, root, u, v) * inv4pi;
+        }
+        pdf[i] = p;
+    }
+}
+
 inline unsigned blocks_for(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
 CacheState* cstate(pgx_ctx* ctx) {
@@ -863,4 +897,39 @@ extern "C" int pgx_cache_knn(pgx_ctx* ctx, const float* queries, int64_t nq, int
     PGX_CUDA_TRY(ctx, cudaMemcpyAsync(d2, cs->knn_d.p, sizeof(float) * k * nq, cudaMemcpyDeviceToHost, s));
     PGX_CUDA_TRY(ctx, cudaStreamSynchronize(s));
     return PGX_OK;
+}
+
+static int guide_query(pgx_ctx* ctx, const float* positions, const float* in, int64_t n, int sample, float* dirs,
+                       float* pdf) {
+    if (!ctx) return PGX_ERR_INVALID_ARG;
+    ctx->err.clear();
+    if (n < 0 || (n > 0 && (!positions || !in || !pdf || (sample && !dirs))))
+        return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_guide_*: bad arguments");
+    if (!guide_ready(ctx)) return pgx_fail(ctx, PGX_ERR_STATE, "pgx_guide_*: no radiance cache");
+    if (n == 0) return PGX_OK;
+    cudaStream_t s = ctx->stream;
+    const size_t in_floats = sample ? 2 : 3;
+    DevBuf dp, di, dd, dpdf;
+    PGX_CUDA_TRY(ctx, dp.reserve(sizeof(float) * 3 * n));
+    PGX_CUDA_TRY(ctx, di.reserve(sizeof(float) * in_floats * n));
+    PGX_CUDA_TRY(ctx, dd.reserve(sizeof(float) * 3 * n));
+    PGX_CUDA_TRY(ctx, dpdf.reserve(sizeof(float) * n));
+    PGX_CUDA_TRY(ctx, cudaMemcpyAsync(dp.p, positions, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, s));
+    PGX_CUDA_TRY(ctx, cudaMemcpyAsync(di.p, in, sizeof(float) * in_floats * n, cudaMemcpyHostToDevice, s));
+    k_guide_query<<<blocks_for(n, 128), 128, 0, s>>>(guide_view(ctx), dp.as<float>(), di.as<float>(), n, sample,
+                                                      dd.as<float>(), dpdf.as<float>());
+    PGX_CUDA_TRY(ctx, cudaGetLastError());
+    if (sample) PGX_CUDA_TRY(ctx, cudaMemcpyAsync(dirs, dd.p, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, s));
+    PGX_CUDA_TRY(ctx, cudaMemcpyAsync(pdf, dpdf.p, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
+    PGX_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    return PGX_OK;
+}
+
+extern "C" int pgx_guide_pdf(pgx_ctx* ctx, const float* positions, const float* dirs, int64_t n, float* pdf) {
+    return guide_query(ctx, positions, dirs, n, 0, nullptr, pdf);
+}
+
+extern "C" int pgx_guide_sample(pgx_ctx* ctx, const float* positions, const float* u2, int64_t n, float* dirs,
+                                float* pdf) {
+    return guide_query(ctx, positions, u2, n, 1, dirs, pdf);
 }

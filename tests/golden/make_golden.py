@@ -8,6 +8,9 @@ Each fixture stores its inputs (triangles, rays) next to the reference's
 outputs, so the tests never regenerate inputs with a possibly different
 numpy on another machine.
 
+* render_<scene>.npz — scene inputs and the films of the reference's own
+  integrators (`pathTrace`, `guidedPath`) driven by the PCG32 stream of
+  (seed, pixel, sample) through oracle/ref_harness.cpp.
 * traversal_<scene>.npz — triangles; the reference's BVH (`BVHNode::build`,
   Geometry.h:419-446) as nodes + triangle indexes; rays; closest hits from
   `BVHNode::traverse` (Geometry.h:455-512); any-hit visibility from
@@ -50,8 +53,29 @@ def traversal_fixture(ref: Reference, name: str, desc, nrays: int, seed: int) ->
           f"hit {np.mean(hits['id'] >= 0):.3f}, visible {vis.mean():.3f}")
 
 
+def render_fixture(ref: Reference, name: str, desc, spp: int, seed: int) -> None:
+    """Reference integrators (pathTrace and guidedPath, Renderer.h:368-613)
+    driven by the PCG32 stream, `spp` samples per pixel."""
+    rs = ref.scene(desc)
+    plain, _, rays_p = rs.render_pcg(False, seed, 0, spp, threads=8)
+    guided, _, rays_g = rs.render_pcg(True, seed, 0, spp, threads=8)
+    rs.close()
+    c = desc.camera
+    env = desc.env if desc.env is not None else np.zeros((0, 0, 3), np.float32)
+    np.savez_compressed(HERE / f"render_{name}.npz", triangles=desc.triangles, materials=desc.materials, env=env,
+                        cam_from=np.array(c["from_"], np.float32), cam_to=np.array(c["to"], np.float32),
+                        cam_up=np.array(c["up"], np.float32), cam_fov=np.float32(c["fov"]),
+                        size=np.array([c["width"], c["height"]], np.int32), spp=np.int32(spp), seed=np.int64(seed),
+                        plain=plain, guided=guided)
+    print(f"render_{name}: {desc.ntris} tris, {c['width']}x{c['height']} x {spp} spp, "
+          f"plain mean {plain.mean() / spp:.4f}, guided mean {guided.mean() / spp:.4f}")
+
+
 def main() -> None:
     ref = Reference()
+    render_fixture(ref, "cornell", scenes.cornell_box(seed=1, width=32, height=32), 4, seed=11)
+    render_fixture(ref, "interior", scenes.interior(seed=5, target_tris=3000, n_objects=24, width=48, height=27,
+                                                    env_width=64, env_height=32), 4, seed=12)
     traversal_fixture(ref, "cornell", scenes.cornell_box(seed=1), 2000, seed=101)
     traversal_fixture(ref, "soup", scenes.triangle_soup(1500, seed=11), 2000, seed=102)
     traversal_fixture(ref, "interior", scenes.interior(seed=5, target_tris=3000, n_objects=24, env_width=8,

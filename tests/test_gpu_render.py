@@ -109,3 +109,28 @@ def test_render_api_semantics(ctx):
     assert np.allclose(a, b, rtol=1e-5, atol=1e-6)
     st = ctx.render_stats()
     assert st.paths == 32 * 32 * 3 and st.extension_rays >= st.paths
+
+
+GOLDEN = __import__("pathlib").Path(__file__).resolve().parent / "golden"
+
+
+def _fixture_desc(g):
+    env = g["env"]
+    cam = dict(from_=tuple(g["cam_from"]), to=tuple(g["cam_to"]), up=tuple(g["cam_up"]), fov=float(g["cam_fov"]),
+               width=int(g["size"][0]), height=int(g["size"][1]))
+    return scenes.SceneDesc(g["triangles"], g["materials"], cam, env=env if env.size else None)
+
+
+@pytest.mark.parametrize("mode", [abi.MODE_PLAIN, abi.MODE_GUIDED_LI])
+@pytest.mark.parametrize("path", sorted(GOLDEN.glob("render_*.npz")), ids=lambda p: p.stem)
+def test_render_matches_golden(ctx, oracle, path, mode):
+    """Films of the reference's integrators (tests/golden/make_golden.py)."""
+    g = np.load(path)
+    desc = _fixture_desc(g)
+    ctx.upload(desc)
+    nodes, idx = oracle.bvh_build(desc.triangles)  # byte-identical to the reference's tree
+    ctx.bvh_import(nodes, idx)
+    ctx.clear()
+    ctx.render(int(g["spp"]), mode=mode, seed=int(g["seed"]), max_depth=8)
+    film, _, _ = ctx.film()
+    _compare(film, g["plain"] if mode == abi.MODE_PLAIN else g["guided"])

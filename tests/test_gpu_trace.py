@@ -97,7 +97,7 @@ def test_gpu_any_hit_bit_exact(ctx, oracle):
     h, _, _ = oracle.trace_closest(desc.triangles, nodes, idx, rays)
     for scale in (0.5, 1.0, 2.0):
         r = rays.copy()
-        r["tmax"] = np.where(h["id"] >= 0, h["t"] * np.float32(scale), np.float32(4.0)).astype(np.float32)
+        r["tmax"] = (np.where(h["id"] >= 0, h["t"], np.float32(4.0)) * np.float32(scale)).astype(np.float32)
         vis = ctx.trace_any(r)
         ref, _, _ = oracle.trace_any(desc.triangles, nodes, idx, r)
         assert np.array_equal(vis, ref)

@@ -85,3 +85,21 @@ def test_oracle_multithreaded_matches_single(oracle):
     h1, _, _ = oracle.trace_closest(d.triangles, nodes, idx, rays)
     h2 = oracle.trace_closest_mt(d.triangles, nodes, idx, rays, 4)
     assert h1.tobytes() == h2.tobytes()
+
+
+RENDERS = sorted(GOLDEN.glob("render_*.npz"))
+
+
+@pytest.mark.parametrize("path", RENDERS, ids=lambda p: p.stem)
+def test_reference_reproduces_render_fixture(reference, path):
+    """The harness is deterministic: re-rendering gives the fixture bits."""
+    g = np.load(path)
+    env = g["env"]
+    cam = dict(from_=tuple(g["cam_from"]), to=tuple(g["cam_to"]), up=tuple(g["cam_up"]), fov=float(g["cam_fov"]),
+               width=int(g["size"][0]), height=int(g["size"][1]))
+    desc = scenes.SceneDesc(g["triangles"], g["materials"], cam, env=env if env.size else None)
+    rs = reference.scene(desc)
+    plain, _, _ = rs.render_pcg(False, int(g["seed"]), 0, int(g["spp"]), threads=4)
+    guided, _, _ = rs.render_pcg(True, int(g["seed"]), 0, int(g["spp"]), threads=4)
+    assert np.array_equal(plain, g["plain"])
+    assert np.array_equal(guided, g["guided"])
