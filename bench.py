@@ -237,6 +237,101 @@ def run_pgx(args) -> dict:
     }
 
 
+def relmse(img: np.ndarray, ref: np.ndarray, eps: float = 1e-2) -> float:
+    """Mean of (x - r)^2 / (r^2 + eps) over pixels and channels."""
+    d = img.astype(np.float64) - ref
+    return float(np.mean(d * d / (ref * ref + eps)))
+
+
+def rrmse_reference_metric(img: np.ndarray, ref: np.ndarray) -> float:
+    """Metrics::calculateRRMSE (Metrics.h:48-68): RMSE / (sqrt(sum ref^2) + 1e-2)."""
+    d = img.astype(np.float64) - ref
+    return float(np.sqrt(np.mean(d * d)) / (np.sqrt(np.sum(ref.astype(np.float64) ** 2)) + 1e-2))
+
+
+def run_relmse_study(args) -> dict:
+    """Equal-time relMSE of QuadTree-guided vs plain path tracing against a
+    converged plain render of the same view."""
+    from pathguidingdissertation_gb300 import abi
+    from pathguidingdissertation_gb300 import build as pkg_build
+    from pathguidingdissertation_gb300.api import Context
+
+    pkg_build.build()
+    w, h = (int(x) for x in args.study_res.split("x"))
+    desc, depth, _ = make_workload(args.workload)
+    desc.camera = dict(desc.camera, width=w, height=h)
+    ctx = Context(0)
+    ctx.upload(desc)
+    ctx.bvh_build()
+
+    def render_ms(frames, mode, seed, **kw):
+        ms = 0.0
+        left = frames
+        while left > 0:
+            n = min(left, 256)
+            ctx.render(n, mode=mode, seed=seed, max_depth=depth, **kw)
+            ms += ctx.render_stats().ms_total
+            left -= n
+        return ms
+
+    ctx.clear()
+    ref_ms = render_ms(args.ref_spp, abi.MODE_PLAIN, 1000)
+    rgb, _, spp = ctx.film()
+    ref = rgb.astype(np.float64) / spp
+
+    # Plain: its error at plain_spp and the time it takes.
+    ctx.clear()
+    plain_ms = render_ms(args.plain_spp, abi.MODE_PLAIN, 7)
+    rgb, _, spp = ctx.film()
+    plain_img = rgb / spp
+    plain_err = relmse(plain_img, ref)
+
+    # Guided: train the cache from `train_spp` plain frames (timed), then
+    # render guided frames until the plain error is reached.
+    ctx.clear()
+    train_ms = render_ms(args.train_spp, abi.MODE_PLAIN, 11, record_paths=args.train_spp)
+    cst = ctx.cache_stats()
+    train_ms += cst.build_ms
+    ctx.clear()
+    guided_ms = 0.0
+    curve = []
+    reached_ms = None
+    chunk = max(1, args.plain_spp // 32)
+    total = 0
+    while total < 4 * args.plain_spp:
+        guided_ms += render_ms(chunk, abi.MODE_GUIDED_QUADTREE, 13, guide_fraction=args.guide_fraction)
+        total += chunk
+        rgb, _, spp = ctx.film()
+        err = relmse(rgb / spp, ref)
+        curve.append((total, train_ms + guided_ms, err))
+        if reached_ms is None and err <= plain_err:
+            reached_ms = train_ms + guided_ms
+        if train_ms + guided_ms >= 2.0 * plain_ms and reached_ms is not None:
+            break
+        if train_ms + guided_ms >= 4.0 * plain_ms:
+            break
+    # Guided error at the plain render's wall time (linear in 1/time between points).
+    eq_err = None
+    for (s0, t0, e0), (s1, t1, e1) in zip(curve, curve[1:]):
+        if t0 <= plain_ms <= t1:
+            eq_err = e0 + (e1 - e0) * (plain_ms - t0) / max(t1 - t0, 1e-9)
+    guided_img = rgb / spp
+    ctx.close()
+    return {
+        "study": "equal-time relMSE, QuadTree-guided vs plain GPU path tracing",
+        "workload": f"{args.workload} {w}x{h}, depth {depth}",
+        "reference": {"spp": args.ref_spp, "ms": ref_ms},
+        "plain": {"spp": args.plain_spp, "ms": plain_ms, "relmse": plain_err,
+                  "rrmse_metrics_h": rrmse_reference_metric(plain_img, ref)},
+        "guided": {"train_spp": args.train_spp, "cache_records": cst.records, "train_ms": train_ms,
+                   "guide_fraction": args.guide_fraction, "spp_rendered": total,
+                   "ms_to_plain_error": reached_ms, "relmse_at_plain_time": eq_err,
+                   "rrmse_metrics_h_final": rrmse_reference_metric(guided_img, ref),
+                   "curve": [{"spp": a, "ms": b, "relmse": c} for a, b, c in curve]},
+        "time_ratio_guided_over_plain": (reached_ms / plain_ms) if reached_ms else None,
+    }
+
+
 def run_reference(args) -> dict:
     from oracle.ffi import Reference, reference_available
     desc, _, wl = make_workload(args.workload)
@@ -285,6 +380,13 @@ def main() -> None:
     ap.add_argument("--mode", choices=["plain", "guided_quadtree"], default="plain")
     ap.add_argument("--workload", choices=["interior", "cornell"], default="interior")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--study", choices=["relmse"], default=None,
+                    help="instead of the throughput line, run the equal-time relMSE study")
+    ap.add_argument("--study-res", default="640x360")
+    ap.add_argument("--ref-spp", type=int, default=16384)
+    ap.add_argument("--plain-spp", type=int, default=1024)
+    ap.add_argument("--train-spp", type=int, default=4)
+    ap.add_argument("--guide-fraction", type=float, default=0.5)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     if args.gpus != 1 or int(os.environ.get("WORLD_SIZE", "1")) != 1:
@@ -294,6 +396,9 @@ def main() -> None:
         return
     if args.warmup < 0 or args.steps < 1:
         raise SystemExit("--steps must be >= 1 and --warmup >= 0")
+    if args.study == "relmse":
+        print(json.dumps(run_relmse_study(args)))
+        return
     out = run_reference(args) if args.impl == "reference" else run_pgx(args)
     print(json.dumps(out))
 

@@ -173,7 +173,12 @@ typedef struct pgx_render_config {
     int32_t max_depth;     /* reference: 8                                 */
     uint64_t seed;         /* PCG32 streams are hash(seed, pixel, sample)  */
     float guide_fraction;  /* probability of sampling the guide (0.5)      */
-    int32_t record_paths;  /* keep path vertices for the cache (guided Li) */
+    int32_t record_paths;  /* cache training: guided Li — non-zero keeps the
+                            * vertices of the last frame with SPP < 16, as the
+                            * reference does; plain / QuadTree — N > 0 records
+                            * the last N frames of the call with the full
+                            * NEE+MIS incident radiance.  The cache is rebuilt
+                            * from the records when the call ends. */
     int32_t flags;         /* PGX_RENDER_PROFILE: per-stage events/counters */
 } pgx_render_config;
 

@@ -127,7 +127,7 @@ class Context:
         self.check(self.lib.pgx_set_camera(self.h, C.byref(camera_struct(camera))))
 
     def render(self, frames: int = 1, mode: int = abi.MODE_PLAIN, seed: int = 1, max_depth: int = 8,
-               guide_fraction: float = 0.5, record_paths: bool = False, profile: bool = False) -> None:
+               guide_fraction: float = 0.5, record_paths: int | bool = 0, profile: bool = False) -> None:
         cfg = abi.RenderConfig(mode, max_depth, seed, guide_fraction, int(record_paths),
                                abi.RENDER_PROFILE if profile else 0)
         self.check(self.lib.pgx_render(self.h, C.byref(cfg), frames))

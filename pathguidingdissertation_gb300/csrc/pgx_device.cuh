@@ -71,6 +71,27 @@ __device__ __forceinline__ bool ray_box(float bminx, float bminy, float bminz, f
     return true;
 }
 
+// Same test for rays whose inverse direction is finite in every component.
+// Then no slab bound is NaN (a finite difference times a finite inverse), so
+// the hardware min/max (which differ from std::min/std::max only for NaN
+// operands and in the sign of a zero result) give the same accept/reject
+// decision; the entry distance may differ from the exact version only in the
+// sign of a zero, which compares equal everywhere it is used.
+__device__ __forceinline__ bool ray_box_finite(float bminx, float bminy, float bminz, float bmaxx, float bmaxy,
+                                               float bmaxz, const xv3& o, const xv3& inv, float& t) {
+    float t0x = x_mul(x_sub(bminx, o.x), inv.x);
+    float t0y = x_mul(x_sub(bminy, o.y), inv.y);
+    float t0z = x_mul(x_sub(bminz, o.z), inv.z);
+    float t1x = x_mul(x_sub(bmaxx, o.x), inv.x);
+    float t1y = x_mul(x_sub(bmaxy, o.y), inv.y);
+    float t1z = x_mul(x_sub(bmaxz, o.z), inv.z);
+    float fen = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z));
+    float fex = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
+    if (fen > fex || fex < 0.f) return false;
+    t = fmaxf(0.f, fen);
+    return true;
+}
+
 // ---- Möller–Trumbore, Triangle::rayIntersect (Geometry.h:101-130), exact --
 // e0 = v1 - v0 and e1 = v2 - v0 are precomputed with the same subtraction the
 // reference performs per call.
@@ -114,7 +135,7 @@ struct TraceCounters {
     unsigned long long interior_visits;
     unsigned long long tri_tests;
     unsigned int overflow;
-    unsigned int pad;
+    unsigned int next;  // work counter of the persistent traversal
 };
 
 // ---- PCG32 stream (same definition as the oracle's pgx_oracle_rng.h) ------

@@ -144,7 +144,7 @@ static __device__ float fresnel_dielectric(float cos_theta, float ior_int, float
     return (par * par + perp * perp) * 0.5f;
 }
 
-static __device__ F3 fresnel_conductor(float cos_theta, const float* ior, const float* k) {
+static __device__ __noinline__ F3 fresnel_conductor(float cos_theta, const float* ior, const float* k) {
     float ci = s_max(s_min(cos_theta, 1.f), -1.f);
     float ci_sq = s_max(ci * ci, 0.f);
     float si_sq = s_max(1.f - ci_sq, 0.f);
@@ -222,7 +222,7 @@ __device__ __forceinline__ bool bsdf_two_sided(const DevMaterial& m) {
     return !(m.kind == PGX_BSDF_GLASS || m.kind == PGX_BSDF_DIELECTRIC);
 }
 
-static __device__ F3 conductor_eval(const DevMaterial& m, F3 alb, F3 wil, F3 wol) {
+static __device__ __noinline__ F3 conductor_eval(const DevMaterial& m, F3 alb, F3 wil, F3 wol) {
     if (wil.z <= 0.f || wol.z <= 0.f) return zero3();
     if (m.alpha < PGX_EPSILON) return zero3();
     F3 h = wil + wol;
@@ -248,7 +248,7 @@ static __device__ float conductor_pdf(const DevMaterial& m, F3 wil, F3 wol) {
 }
 
 // Rough dielectric eval/pdf (Materials.h:545-634).
-static __device__ void dielectric_eval_pdf(const DevMaterial& m, F3 alb, F3 wol, F3 wil, F3* f, float* pdf) {
+static __device__ __noinline__ void dielectric_eval_pdf(const DevMaterial& m, F3 alb, F3 wol, F3 wil, F3* f, float* pdf) {
     if (f) *f = zero3();
     if (pdf) *pdf = 0.f;
     if (wol.z == 0.f || wil.z == 0.f) return;
@@ -291,7 +291,7 @@ __device__ __forceinline__ float plastic_exponent(float alpha) {
 }
 
 // BSDF::evaluate for all kinds.
-static __device__ F3 bsdf_eval(const DevMaterial& m, const TexView& tv, const Shading& sd, F3 wi) {
+static __device__ __noinline__ F3 bsdf_eval(const DevMaterial& m, const TexView& tv, const Shading& sd, F3 wi) {
     switch (m.kind) {
         case PGX_BSDF_DIFFUSE: {
             F3 wl = to_local(sd.frame, wi);
@@ -343,7 +343,7 @@ static __device__ F3 bsdf_eval(const DevMaterial& m, const TexView& tv, const Sh
 }
 
 // BSDF::PDF for all kinds.
-static __device__ float bsdf_pdf(const DevMaterial& m, const TexView& tv, const Shading& sd, F3 wi) {
+static __device__ __noinline__ float bsdf_pdf(const DevMaterial& m, const TexView& tv, const Shading& sd, F3 wi) {
     switch (m.kind) {
         case PGX_BSDF_DIFFUSE:
         case PGX_BSDF_ORENNAYAR:
@@ -376,7 +376,7 @@ static __device__ float bsdf_pdf(const DevMaterial& m, const TexView& tv, const 
 }
 
 // BSDF::sample for all kinds; consumes random numbers like the reference.
-static __device__ F3 bsdf_sample(const DevMaterial& m, const TexView& tv, const Shading& sd, uint64_t& rng, F3& f,
+static __device__ __noinline__ F3 bsdf_sample(const DevMaterial& m, const TexView& tv, const Shading& sd, uint64_t& rng, F3& f,
                           float& pdf) {
     switch (m.kind) {
         case PGX_BSDF_DIFFUSE:
@@ -575,12 +575,12 @@ __device__ __forceinline__ F3 env_eval(const DevEnv& e, F3 wi) {
 }
 
 // Distribution2D::PDF (Sampling.h:203-208) via EnvironmentMap::PDF.
-static __device__ float env_pdf(const DevEnv& e, F3 wi) {
+static __device__ __noinline__ float env_pdf(const DevEnv& e, F3 wi) {
     float u = atan2f(wi.z, wi.x);
     u = (u < 0.f) ? (float)((double)u + 2.0 * PGX_PI_D) : u;
     u = (float)((double)u / (2.0 * PGX_PI_D));
     float v = (float)((double)acosf(wi.y) / PGX_PI_D);
-    float st = (float)sin(PGX_PI_D * (double)v);
+    float st = (float)sinpi((double)v);  // sin(pi * v) of EnvironmentMap::PDF (Lights.h:188)
     if (st <= 0.f) return 0.f;
     float p;
     if (e.marg_int == 0.f) {
@@ -594,7 +594,7 @@ static __device__ float env_pdf(const DevEnv& e, F3 wi) {
 }
 
 // EnvironmentMap::sample: direction (y-up), emitted colour and solid-angle pdf.
-static __device__ F3 env_sample(const DevEnv& e, uint64_t& rng, F3& col, float& pdf) {
+static __device__ __noinline__ F3 env_sample(const DevEnv& e, uint64_t& rng, F3& col, float& pdf) {
     float ru = pgx_rng_next(rng);
     float rv = pgx_rng_next(rng);
     float pv, pu;

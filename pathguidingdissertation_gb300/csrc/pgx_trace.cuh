@@ -136,3 +136,190 @@ __device__ __forceinline__ bool bvh_trace(const BvhView& bvh, const xv3& o, cons
     }
     return false;
 }
+
+// ---- persistent traversal with lane refill ----------------------------------
+// The same per-ray algorithm as bvh_trace, cut into steps (one interior node
+// or one triangle) so that a warp can keep stepping while its lanes finish at
+// different times: every few steps, lanes whose ray is done fetch the next
+// ray index from a global counter (warp-aggregated atomicAdd).  Each ray still
+// visits its nodes and triangles in exactly bvh_trace's order, so results are
+// identical; only which rays share a warp instruction changes.
+struct TraceLane {
+    xv3 o, d, inv;
+    float tmax;   // ANY: the visibility limit; closest: the current best t
+    float hu, hv;
+    int hit_id;
+    int ref, cnt, k;  // current node reference; for leaves, next triangle k
+    int sp;
+    int status;
+    bool finite;  // every component of inv is finite (see ray_box_finite)
+};
+
+// Starts a ray; returns false when the root box is missed (finished).
+__device__ __forceinline__ bool lane_start(const BvhView& bvh, TraceLane& L, xv3 o, xv3 d, float tmax) {
+    L.o = o;
+    L.d = d;
+    L.tmax = tmax;
+    L.hit_id = -1;
+    L.hu = 0.f;
+    L.hv = 0.f;
+    L.sp = 0;
+    L.k = 0;
+    L.status = 0;
+    if (!bvh.root.valid) return false;
+    L.inv = mk(x_div(1.f, d.x), x_div(1.f, d.y), x_div(1.f, d.z));
+    L.finite = isfinite(L.inv.x) && isfinite(L.inv.y) && isfinite(L.inv.z);
+    float tb;
+    if (!ray_box(bvh.root.bmin[0], bvh.root.bmin[1], bvh.root.bmin[2], bvh.root.bmax[0], bvh.root.bmax[1],
+                 bvh.root.bmax[2], o, L.inv, tb))
+        return false;
+    if (tb > tmax) return false;
+    L.ref = bvh.root.ref;
+    L.cnt = bvh.root.count;
+    return true;
+}
+
+// One step; returns true when the ray is finished (for ANY, hit_id >= 0
+// marks an occluder).
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ bool lane_step(const BvhView& bvh, TraceLane& L, int2* stack, unsigned long long& n_interior,
+                                          unsigned long long& n_tris) {
+    if (L.cnt > 0) {
+        if ((unsigned)L.ref > (unsigned)bvh.n_tris || L.cnt > bvh.n_tris - L.ref) {
+            L.status = 2;
+            return true;
+        }
+        const float4* tp = reinterpret_cast<const float4*>(bvh.tris + L.ref + L.k);
+        float4 a = __ldg(tp + 0);
+        float4 b = __ldg(tp + 1);
+        float4 c = __ldg(tp + 2);
+        if (COUNT) n_tris++;
+        float t, u, v;
+        if (ray_tri(mk(a), mk(b), mk(c), L.o, L.d, t, u, v)) {
+            if (ANY) {
+                if (t > PGX_EPSILON && t < L.tmax) {
+                    L.hit_id = __float_as_int(a.w);
+                    return true;
+                }
+            } else if (t > PGX_EPSILON && t < L.tmax) {
+                L.tmax = t;
+                L.hit_id = __float_as_int(a.w);
+                L.hu = u;
+                L.hv = v;
+            }
+        }
+        if (++L.k < L.cnt) return false;
+        L.k = 0;
+        if (L.sp == 0) return true;
+        --L.sp;
+        L.ref = stack[L.sp].x;
+        L.cnt = stack[L.sp].y;
+        return false;
+    }
+    if (COUNT) n_interior++;
+    if ((unsigned)L.ref >= (unsigned)bvh.n_records) {
+        L.status = 2;
+        return true;
+    }
+    TravNode n = load_node(bvh.nodes, L.ref);
+    const float lim = L.tmax;
+    float dl = 0.f, dr = 0.f;
+    bool hl, hr;
+    if (L.finite) {
+        hl = ray_box_finite(n.lmin.x, n.lmin.y, n.lmin.z, n.lmax.x, n.lmax.y, n.lmax.z, L.o, L.inv, dl);
+        hr = ray_box_finite(n.rmin.x, n.rmin.y, n.rmin.z, n.rmax.x, n.rmax.y, n.rmax.z, L.o, L.inv, dr);
+    } else {
+        hl = ray_box(n.lmin.x, n.lmin.y, n.lmin.z, n.lmax.x, n.lmax.y, n.lmax.z, L.o, L.inv, dl);
+        hr = ray_box(n.rmin.x, n.rmin.y, n.rmin.z, n.rmax.x, n.rmax.y, n.rmax.z, L.o, L.inv, dr);
+    }
+    if (!hl || dl >= lim) dl = FLT_MAX;
+    if (!hr || dr >= lim) dr = FLT_MAX;
+    int nref = __float_as_int(n.lmin.w), ncnt = __float_as_int(n.lmax.w);
+    int fref = __float_as_int(n.rmin.w), fcnt = __float_as_int(n.rmax.w);
+    if (dl > dr) {
+        float tf = dl;
+        dl = dr;
+        dr = tf;
+        int t0 = nref;
+        nref = fref;
+        fref = t0;
+        t0 = ncnt;
+        ncnt = fcnt;
+        fcnt = t0;
+    }
+    if (dl == FLT_MAX) {
+        if (L.sp == 0) return true;
+        --L.sp;
+        L.ref = stack[L.sp].x;
+        L.cnt = stack[L.sp].y;
+        return false;
+    }
+    L.ref = nref;
+    L.cnt = ncnt;
+    if (dr != FLT_MAX) {
+        if (L.sp >= PGX_STACK_SIZE) {
+            L.status = 1;
+            return true;
+        }
+        stack[L.sp] = make_int2(fref, fcnt);
+        L.sp++;
+    }
+    return false;
+}
+
+// Persistent warp loop over rays [0, n): `load(i, o, d, tmax)` fetches ray i,
+// `store(i, lane)` consumes a finished ray.  `next` is a zeroed counter.
+// Must be called by whole warps (all 32 lanes).
+template <bool ANY, bool COUNT, class Load, class Store>
+__device__ __forceinline__ void trace_persistent(const BvhView& bvh, unsigned n, unsigned* next, Load load,
+                                                 Store store, unsigned long long& n_interior,
+                                                 unsigned long long& n_tris, unsigned& status_or) {
+    constexpr unsigned kFull = 0xFFFFFFFFu;
+    constexpr int kRefillBelow = 24;  // refill when fewer lanes than this are busy
+    constexpr int kMaxSteps = 64;
+    const int lane = threadIdx.x & 31;
+    int2 stack[PGX_STACK_SIZE];
+    TraceLane L;
+    int ray = -1;
+    bool exhausted = false;
+    for (;;) {
+        // Refill idle lanes (possibly several rounds when roots are missed).
+        for (;;) {
+            bool need = ray < 0 && !exhausted;
+            unsigned m = __ballot_sync(kFull, need);
+            if (!m) break;
+            int leader = __ffs(m) - 1;
+            unsigned base = 0;
+            if (lane == leader) base = atomicAdd(next, (unsigned)__popc(m));
+            base = __shfl_sync(kFull, base, leader);
+            if (need) {
+                unsigned idx = base + __popc(m & ((1u << lane) - 1u));
+                if (idx < n) {
+                    xv3 o, d;
+                    float tmax;
+                    load(idx, o, d, tmax);
+                    if (lane_start(bvh, L, o, d, tmax)) {
+                        ray = (int)idx;
+                    } else {
+                        store(idx, L);  // missed the root: finished
+                    }
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        if (__all_sync(kFull, ray < 0)) break;  // every lane idle and the queue is drained
+        for (int s = 0; s < kMaxSteps; s++) {
+            if (ray >= 0) {
+                if (lane_step<ANY, COUNT>(bvh, L, stack, n_interior, n_tris)) {
+                    status_or |= (unsigned)L.status;
+                    store((unsigned)ray, L);
+                    ray = -1;
+                }
+            }
+            unsigned busy = __ballot_sync(kFull, ray >= 0);
+            if (__popc(busy) < kRefillBelow && !__all_sync(kFull, exhausted || ray >= 0)) break;
+            if (busy == 0) break;
+        }
+    }
+}

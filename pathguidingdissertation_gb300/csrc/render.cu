@@ -61,6 +61,7 @@ struct PathState {
     // counters: queue length per depth, shadow count per depth, stats
     unsigned* qcount;  // [kMaxDepthCap + 2]
     unsigned* scount;  // [kMaxDepthCap + 2]
+    unsigned* wcount;  // [2 * (kMaxDepthCap + 2)] persistent-traversal work counters
     unsigned long long* stats;  // [0] ext rays [1] shadow rays [2,3] extend nodes/tris [4,5] shadow nodes/tris
     pgx_path_vertex* vertices;
     unsigned* nvertices;
@@ -106,7 +107,8 @@ struct FrameParams {
     uint64_t seed;
     int spp0;        // sample index of the batch's first sample
     int batch;       // samples per pixel in this batch
-    int collect;     // sample index whose path vertices are recorded (-1: none)
+    int collect_lo;  // path vertices of samples [collect_lo, collect_hi) are recorded
+    int collect_hi;
     float guide_fraction;
     int profile;     // count node/triangle fetches
 };
@@ -162,54 +164,62 @@ __device__ __forceinline__ void add_counts(unsigned long long* dst, unsigned lon
     }
 }
 
+constexpr int kPersistentBlocksPerSM = 8;
+
+// Closest hit for the queue of this depth: persistent warps with lane refill
+// (trace_persistent) over qcount[depth] rays.
 template <bool COUNT>
-__global__ void __launch_bounds__(kThreads) k_extend(SceneView sv, PathState ps, int depth) {
+__global__ void __launch_bounds__(kThreads, kPersistentBlocksPerSM) k_extend(SceneView sv, PathState ps, int depth) {
     const unsigned n = ps.qcount[depth];
     const int* __restrict__ q = ps.queue[depth & 1];
     unsigned long long ni = 0, nt = 0;
-    const unsigned stride = gridDim.x * blockDim.x;
-    const unsigned rounds = (n + stride - 1) / stride;
-    for (unsigned r = 0; r < rounds; r++) {
-        unsigned i = blockIdx.x * blockDim.x + threadIdx.x + r * stride;
-        if (i < n) {
-            int p = q[i];
-            float4 a = ps.o[p], b = ps.d[p];
-            int id, st;
-            float t, u = 0.f, v = 0.f;
-            bvh_trace<false, COUNT>(sv.bvh, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), FLT_MAX, id, t, u, v, st, ni, nt);
-            if (st) id = -1;  // corrupt tree or stack overflow: treat as a miss
-            ps.hit[p] = make_float4(__int_as_float(id), t, u, v);
-        }
-    }
+    unsigned status = 0;
+    auto load = [&](unsigned i, xv3& o, xv3& d, float& tmax) {
+        int p = q[i];
+        float4 a = ps.o[p], b = ps.d[p];
+        o = mk(a.x, a.y, a.z);
+        d = mk(b.x, b.y, b.z);
+        tmax = FLT_MAX;
+    };
+    auto store = [&](unsigned i, const TraceLane& L) {
+        int p = q[i];
+        int id = L.status ? -1 : L.hit_id;  // corrupt tree or stack overflow: a miss
+        ps.hit[p] = make_float4(__int_as_float(id), L.tmax, L.hu, L.hv);
+    };
+    trace_persistent<false, COUNT>(sv.bvh, n, &ps.wcount[depth], load, store, ni, nt, status);
     if (COUNT) add_counts(&ps.stats[2], ni, nt);
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ps.stats[0], (unsigned long long)n);
 }
 
-// ---- any hit for the shadow queue of this depth --------------------------------
+// Any hit for the shadow queue of this depth; unoccluded rays add their
+// contribution to the path's radiance.
 template <bool COUNT>
-__global__ void __launch_bounds__(kThreads) k_shadow(SceneView sv, PathState ps, int depth) {
+__global__ void __launch_bounds__(kThreads, kPersistentBlocksPerSM) k_shadow(SceneView sv, PathState ps, int depth) {
     const unsigned n = ps.scount[depth];
     unsigned long long ni = 0, nt = 0;
-    const unsigned stride = gridDim.x * blockDim.x;
-    const unsigned rounds = (n + stride - 1) / stride;
-    for (unsigned r = 0; r < rounds; r++) {
-        unsigned i = blockIdx.x * blockDim.x + threadIdx.x + r * stride;
-        if (i < n) {
-            float4 a = ps.sh_o[i], b = ps.sh_d[i];
-            int id, st;
-            float t, u, v;
-            bool occluded =
-                bvh_trace<true, COUNT>(sv.bvh, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, id, t, u, v, st, ni, nt);
-            if (!occluded && !st) {
-                int p = ps.sh_path[i];
-                float4 c = ps.sh_c[i];
-                float4 l = ps.L[p];
-                ps.L[p] = make_float4(l.x + c.x, l.y + c.y, l.z + c.z, 0.f);
-            }
+    unsigned status = 0;
+    auto load = [&](unsigned i, xv3& o, xv3& d, float& tmax) {
+        float4 a = ps.sh_o[i], b = ps.sh_d[i];
+        o = mk(a.x, a.y, a.z);
+        d = mk(b.x, b.y, b.z);
+        tmax = a.w;
+    };
+    auto store = [&](unsigned i, const TraceLane& L) {
+        if (L.hit_id < 0 && !L.status) {
+            int p = ps.sh_path[i];
+            float4 c = ps.sh_c[i];
+            float4 l = ps.L[p];
+            ps.L[p] = make_float4(l.x + c.x, l.y + c.y, l.z + c.z, 0.f);
         }
-    }
+    };
+    trace_persistent<true, COUNT>(sv.bvh, n, &ps.wcount[kMaxDepthCap + 2 + depth], load, store, ni, nt, status);
     if (COUNT) add_counts(&ps.stats[4], ni, nt);
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ps.stats[1], (unsigned long long)n);
+}
+
+inline unsigned persistent_grid(int64_t n) {
+    int64_t b = (n + kThreads - 1) / kThreads;
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(b, 152 * kPersistentBlocksPerSM));
 }
 
 // Scene::calculateShadingData (Scene.h:152-176).
@@ -244,7 +254,7 @@ __device__ __forceinline__ void shading_data(const SceneView& sv, const float4& 
 // RayTracer::computeDirect (Renderer.h:269-354).  Draws the light and the
 // light sample; returns true with the shadow ray and the contribution it
 // carries when the contribution can be non-zero.
-__device__ bool next_event(const SceneView& sv, const DevMaterial& m, const Shading& sd, uint64_t& rng, float4& so,
+__device__ __noinline__ bool next_event(const SceneView& sv, const DevMaterial& m, const Shading& sd, uint64_t& rng, float4& so,
                            float4& sdir, F3& contrib, const GuideView& gv, int qroot, float frac) {
     if (bsdf_pure_specular(m)) return false;
     if (sv.nlights == 0) return false;
@@ -340,7 +350,7 @@ __device__ __forceinline__ void push_shadow(PathState& ps, int depth, int p, flo
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(kThreads) k_shade(SceneView sv, PathState ps, FrameParams fp, int depth,
+__global__ void __launch_bounds__(kThreads, 8) k_shade(SceneView sv, PathState ps, FrameParams fp, int depth,
                                                     GuideView gv) {
     const unsigned n = ps.qcount[depth];
     const int* __restrict__ q = ps.queue[depth & 1];
@@ -357,6 +367,13 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneView sv, PathState ps, 
         float4 so = make_float4(0.f, 0.f, 0.f, 0.f), sdir = so;
         F3 sc = zero3();
         int p = active ? q[i] : 0;
+        // Recording for the cache outside guided-Li: the radiance the path has
+        // gathered up to here (after the previous vertex's NEE) is the
+        // baseline from which k_finalize recovers that vertex's incident Li.
+        const int sample_of_p = fp.spp0 + (int)(p / ((int64_t)sv.width * sv.height));
+        const bool rec_on = MODE != PGX_MODE_GUIDED_LI && active && sample_of_p >= fp.collect_lo &&
+                            sample_of_p < fp.collect_hi;
+        if (rec_on && depth > 0) ps.rec_e[(size_t)(depth - 1) * cap + p] = ps.L[p];
         if (active) {
             float4 o = ps.o[p], d = ps.d[p], h = ps.hit[p], Tw = ps.T[p];
             uint64_t rng = ps.rng[p];
@@ -453,6 +470,11 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneView sv, PathState ps, 
                             }
                         }
                         if (alive) {
+                            if (rec_on) {
+                                r_store = !bsdf_pure_specular(m);
+                                r_wi = wi;
+                                r_w = T;  // throughput after this vertex
+                            }
                             float sgn = (dot(wi, sd.gn) >= 0.f) ? 1.f : -1.f;
                             F3 org = sd.x + sd.gn * (PGX_EPSILON * sgn);
                             ps.o[p] = make_float4(org.x, org.y, org.z, 0.f);
@@ -488,9 +510,21 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneView sv, PathState ps, 
                 ps.rec_w[ri] = make_float4(r_w.x, r_w.y, r_w.z, 0.f);
                 ps.rec_e[ri] = make_float4(r_e.x, r_e.y, r_e.z, 0.f);
                 ps.nrec[p] = depth + 1;
-            } else if (add.x != 0.f || add.y != 0.f || add.z != 0.f || !valid(add)) {
-                float4 l = ps.L[p];
-                ps.L[p] = make_float4(l.x + add.x, l.y + add.y, l.z + add.z, 0.f);
+            } else {
+                if (add.x != 0.f || add.y != 0.f || add.z != 0.f || !valid(add)) {
+                    float4 l = ps.L[p];
+                    ps.L[p] = make_float4(l.x + add.x, l.y + add.y, l.z + add.z, 0.f);
+                }
+                if (rec_on) {
+                    size_t ri = (size_t)depth * cap + p;
+                    ps.rec_pos[ri] = make_float4(r_pos.x, r_pos.y, r_pos.z, (cont && r_store) ? 1.f : 0.f);
+                    if (cont && r_store) {
+                        ps.rec_nrm[ri] = make_float4(r_nrm.x, r_nrm.y, r_nrm.z, 0.f);
+                        ps.rec_wi[ri] = make_float4(r_wi.x, r_wi.y, r_wi.z, 0.f);
+                        ps.rec_w[ri] = make_float4(r_w.x, r_w.y, r_w.z, 0.f);
+                    }
+                    ps.nrec[p] = depth + 1;
+                }
             }
             ps.rng[p] = rng;
         }
@@ -542,9 +576,10 @@ __global__ void __launch_bounds__(kThreads) k_finalize(SceneView sv, PathState p
     const int64_t n = npix * fp.batch;
     for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
         F3 col;
+        const int sample_of_p = fp.spp0 + (int)(p / npix);
+        const bool collect = sample_of_p >= fp.collect_lo && sample_of_p < fp.collect_hi;
         if (MODE == PGX_MODE_GUIDED_LI) {
             int nr = ps.nrec[p];
-            bool collect = fp.collect >= 0 && (fp.spp0 + (int)(p / npix)) == fp.collect;
             F3 li = zero3();
             for (int i = nr - 1; i >= 0; i--) {
                 size_t ri = (size_t)i * ps.capacity + p;
@@ -574,6 +609,38 @@ __global__ void __launch_bounds__(kThreads) k_finalize(SceneView sv, PathState p
             col = li;
         } else {
             col = f3(ps.L[p]);
+            if (collect && valid(col)) {
+                // Incident radiance along each recorded wi: what the path gathered
+                // after that vertex, divided by the throughput it carried.
+                int nr = ps.nrec[p];
+                for (int i = 0; i < nr; i++) {
+                    size_t ri = (size_t)i * ps.capacity + p;
+                    float4 pos = ps.rec_pos[ri];
+                    if (pos.w == 0.f) continue;
+                    F3 tn = f3(ps.rec_w[ri]);
+                    F3 dl = col - f3(ps.rec_e[ri]);
+                    F3 li = f3(tn.x > 0.f ? dl.x / tn.x : 0.f, tn.y > 0.f ? dl.y / tn.y : 0.f,
+                               tn.z > 0.f ? dl.z / tn.z : 0.f);
+                    if (!(valid(li) && lum(li) > 0.f)) continue;
+                    unsigned slot = atomicAdd(ps.nvertices, 1u);
+                    if (slot >= (unsigned)ps.vcapacity) continue;
+                    float4 nr4 = ps.rec_nrm[ri], wi = ps.rec_wi[ri];
+                    pgx_path_vertex v;
+                    v.position[0] = pos.x;
+                    v.position[1] = pos.y;
+                    v.position[2] = pos.z;
+                    v.normal[0] = nr4.x;
+                    v.normal[1] = nr4.y;
+                    v.normal[2] = nr4.z;
+                    v.wi[0] = wi.x;
+                    v.wi[1] = wi.y;
+                    v.wi[2] = wi.z;
+                    v.Li[0] = li.x;
+                    v.Li[1] = li.y;
+                    v.Li[2] = li.z;
+                    ps.vertices[slot] = v;
+                }
+            }
         }
         if (!valid(col)) continue;
         float2 xy = ps.pix[p];
@@ -624,7 +691,7 @@ int ensure_state(pgx_ctx* ctx, RenderState* rs, int64_t cap, int rec_depth, int6
         PGX_CUDA_TRY(ctx, rs->vertices.reserve(sizeof(pgx_path_vertex) * vcap));
         rs->vcapacity = vcap;
     }
-    PGX_CUDA_TRY(ctx, rs->counters.reserve(sizeof(unsigned) * 2 * (kMaxDepthCap + 2) + sizeof(unsigned long long) * kStats +
+    PGX_CUDA_TRY(ctx, rs->counters.reserve(sizeof(unsigned) * 4 * (kMaxDepthCap + 2) + sizeof(unsigned long long) * kStats +
                                            sizeof(unsigned) * 4));
     if (!rs->ev0) {
         PGX_CUDA_TRY(ctx, cudaEventCreate(&rs->ev0));
@@ -659,8 +726,9 @@ PathState path_view(RenderState* rs) {
     unsigned* c = rs->counters.as<unsigned>();
     ps.qcount = c;
     ps.scount = c + (kMaxDepthCap + 2);
-    ps.stats = reinterpret_cast<unsigned long long*>(c + 2 * (kMaxDepthCap + 2));
-    ps.nvertices = c + 2 * (kMaxDepthCap + 2) + 2 * kStats;
+    ps.wcount = c + 2 * (kMaxDepthCap + 2);
+    ps.stats = reinterpret_cast<unsigned long long*>(c + 4 * (kMaxDepthCap + 2));
+    ps.nvertices = c + 4 * (kMaxDepthCap + 2) + 2 * kStats;
     ps.vertices = rs->vertices.as<pgx_path_vertex>();
     ps.capacity = rs->capacity;
     ps.vcapacity = rs->vcapacity;
@@ -702,15 +770,16 @@ int enqueue_frame(pgx_ctx* ctx, RenderState* rs, const FrameParams& fp, cudaStre
     const unsigned g = grid_for(n);
     const bool prof = fp.profile != 0;
     int launches = 0;
-    cudaMemsetAsync(ps.qcount, 0, sizeof(unsigned) * 2 * (kMaxDepthCap + 2), s);
+    cudaMemsetAsync(ps.qcount, 0, sizeof(unsigned) * 4 * (kMaxDepthCap + 2), s);
     k_camgen<<<g, kThreads, 0, s>>>(sv, ps, fp);
     launches++;
     for (int depth = 0; depth <= fp.max_depth; depth++) {
         if (prof) cudaEventRecord(rs->prof[4 * depth + 0], s);
+        const unsigned pg = persistent_grid(n);
         if (prof)
-            k_extend<true><<<g, kThreads, 0, s>>>(sv, ps, depth);
+            k_extend<true><<<pg, kThreads, 0, s>>>(sv, ps, depth);
         else
-            k_extend<false><<<g, kThreads, 0, s>>>(sv, ps, depth);
+            k_extend<false><<<pg, kThreads, 0, s>>>(sv, ps, depth);
         if (prof) cudaEventRecord(rs->prof[4 * depth + 1], s);
         switch (fp.mode) {
             case PGX_MODE_GUIDED_LI:
@@ -727,9 +796,9 @@ int enqueue_frame(pgx_ctx* ctx, RenderState* rs, const FrameParams& fp, cudaStre
         if (prof) cudaEventRecord(rs->prof[4 * depth + 2], s);
         if (fp.mode != PGX_MODE_GUIDED_LI) {
             if (prof)
-                k_shadow<true><<<g, kThreads, 0, s>>>(sv, ps, depth);
+                k_shadow<true><<<pg, kThreads, 0, s>>>(sv, ps, depth);
             else
-                k_shadow<false><<<g, kThreads, 0, s>>>(sv, ps, depth);
+                k_shadow<false><<<pg, kThreads, 0, s>>>(sv, ps, depth);
             launches++;
         }
         if (prof) cudaEventRecord(rs->prof[4 * depth + 3], s);
@@ -809,17 +878,28 @@ extern "C" int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t fr
     RenderState* rs = state_of(ctx);
     const int64_t npix = (int64_t)ctx->width * ctx->height;
     // Samples per wavefront: enough paths to fill the GPU, bounded memory.
-    const int64_t target_paths = 1 << 22;
-    int batch = (int)std::max<int64_t>(1, std::min<int64_t>(frames, target_paths / std::max<int64_t>(npix, 1)));
     const bool guided_li = cfg->mode == PGX_MODE_GUIDED_LI;
-    const int rec_depth = guided_li ? cfg->max_depth + 1 : 0;
-    // Path vertices of the last frame with SPP < 16 are kept (Renderer.h:720-746).
-    int collect = -1;
+    // Recorded samples [collect_lo, collect_hi).  Guided-Li keeps the vertices
+    // of the last frame with SPP < 16 (Renderer.h:720-746); the other modes
+    // record the last `record_paths` frames of this call.
+    int collect_lo = 0, collect_hi = 0;
     if (guided_li && cfg->record_paths) {
         int last = std::min(ctx->spp + frames, kCollectionSPP - 1);
-        if (last > ctx->spp) collect = last - 1;
+        if (last > ctx->spp) {
+            collect_lo = last - 1;
+            collect_hi = last;
+        }
+    } else if (!guided_li && cfg->record_paths > 0) {
+        collect_hi = ctx->spp + frames;
+        collect_lo = collect_hi - std::min(cfg->record_paths, frames);
     }
-    const int64_t vcap = collect >= 0 ? npix * (cfg->max_depth + 1) : 0;
+    const bool recording = collect_hi > collect_lo;
+    const int rec_depth = (guided_li || recording) ? cfg->max_depth + 1 : 0;
+    // Samples per wavefront: enough paths to fill the GPU, bounded memory
+    // (per-depth vertex records cost 80 bytes per path and depth).
+    const int64_t target_paths = rec_depth ? (int64_t)(1 << 21) : (int64_t)(1 << 22);
+    int batch = (int)std::max<int64_t>(1, std::min<int64_t>(frames, target_paths / std::max<int64_t>(npix, 1)));
+    const int64_t vcap = recording ? npix * (cfg->max_depth + 1) * (collect_hi - collect_lo) : 0;
     PGX_TRY(ensure_state(ctx, rs, npix * batch, rec_depth, vcap));
     cudaStream_t s = ctx->stream;
     PathState ps = path_view(rs);
@@ -836,7 +916,8 @@ extern "C" int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t fr
         fp.seed = cfg->seed;
         fp.spp0 = ctx->spp + done;
         fp.batch = std::min(batch, frames - done);
-        fp.collect = (collect >= fp.spp0 && collect < fp.spp0 + fp.batch) ? collect : -1;
+        fp.collect_lo = collect_lo;
+        fp.collect_hi = collect_hi;
         fp.guide_fraction = cfg->guide_fraction;
         fp.profile = prof ? 1 : 0;
         launches += enqueue_frame(ctx, rs, fp, s);
@@ -872,7 +953,7 @@ extern "C" int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t fr
     rst.ms_extend = times.extend;
     rst.ms_shade = times.shade;
     rst.ms_shadow = times.shadow;
-    if (collect >= 0) {
+    if (recording) {
         rs->nvertices_last = std::min<int64_t>(nv, rs->vcapacity);
         rst.path_vertices = rs->nvertices_last;
         PGX_TRY(cache_build_device(ctx, rs->vertices.as<pgx_path_vertex>(), rs->nvertices_last));

@@ -11,26 +11,30 @@ namespace {
 
 constexpr int kTraceThreads = 128;
 
+constexpr int kPersistentBlocksPerSM = 8;
+
+// Persistent traversal of a ray batch: whole warps loop, refilling lanes
+// from counters->next (see trace_persistent).
 template <bool ANY, bool COUNT>
-__global__ void __launch_bounds__(kTraceThreads) k_trace(BvhView bvh, const pgx_ray* __restrict__ rays, int64_t n,
-                                                         pgx_hit* __restrict__ hits, uint8_t* __restrict__ visible,
-                                                         TraceCounters* __restrict__ counters) {
+__global__ void __launch_bounds__(kTraceThreads, kPersistentBlocksPerSM)
+    k_trace(BvhView bvh, const pgx_ray* __restrict__ rays, int64_t n, pgx_hit* __restrict__ hits,
+            uint8_t* __restrict__ visible, TraceCounters* __restrict__ counters) {
     unsigned long long ni = 0, nt = 0;
-    unsigned overflow = 0;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    unsigned status = 0;
+    auto load = [&](unsigned i, xv3& o, xv3& d, float& tmax) {
         const float4* rp = reinterpret_cast<const float4*>(rays + i);
         float4 a = __ldg(rp), b = __ldg(rp + 1);
-        xv3 o = mk(a.x, a.y, a.z), d = mk(b.x, b.y, b.z);
-        int id, status;
-        float t, u = 0.f, v = 0.f;
-        bool occluded = bvh_trace<ANY, COUNT>(bvh, o, d, a.w, id, t, u, v, status, ni, nt);
-        overflow |= (unsigned)status;
-        if (ANY) {
-            visible[i] = occluded ? 0 : 1;
-        } else {
-            reinterpret_cast<float4*>(hits)[i] = make_float4(__int_as_float(id), t, u, v);
-        }
-    }
+        o = mk(a.x, a.y, a.z);
+        d = mk(b.x, b.y, b.z);
+        tmax = a.w;
+    };
+    auto store = [&](unsigned i, const TraceLane& L) {
+        if (ANY)
+            visible[i] = (L.hit_id >= 0) ? 0 : 1;
+        else
+            reinterpret_cast<float4*>(hits)[i] = make_float4(__int_as_float(L.hit_id), L.tmax, L.hu, L.hv);
+    };
+    trace_persistent<ANY, COUNT>(bvh, (unsigned)n, &counters->next, load, store, ni, nt, status);
     if (COUNT) {
         for (int o = 16; o > 0; o >>= 1) {
             ni += __shfl_xor_sync(0xFFFFFFFFu, ni, o);
@@ -41,7 +45,12 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(BvhView bvh, const pgx_
             atomicAdd(&counters->tri_tests, nt);
         }
     }
-    if (overflow) atomicOr(&counters->overflow, overflow);
+    if (status) atomicOr(&counters->overflow, status);
+}
+
+unsigned persistent_grid(int64_t n) {
+    int64_t blocks = (n + kTraceThreads - 1) / kTraceThreads;
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(blocks, 152 * kPersistentBlocksPerSM));
 }
 
 // Camera::generateRay with exact arithmetic.
@@ -83,8 +92,8 @@ int launch_trace(pgx_ctx* ctx, const pgx_ray* d_rays, int64_t n, pgx_hit* d_hits
     PGX_CUDA_TRY(ctx, ctx->counters.reserve(sizeof(TraceCounters)));
     PGX_CUDA_TRY(ctx, cudaMemsetAsync(ctx->counters.p, 0, sizeof(TraceCounters), s));
     if (n > 0) {
-        int64_t blocks = (n + kTraceThreads - 1) / kTraceThreads;
-        unsigned grid = (unsigned)std::min<int64_t>(blocks, 152 * 64);
+        if (n > (int64_t)UINT32_MAX) return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "too many rays in one call");
+        unsigned grid = persistent_grid(n);
         BvhView v = bvh_view(ctx);
         TraceCounters* c = ctx->counters.as<TraceCounters>();
         if (any)
@@ -184,9 +193,8 @@ extern "C" int pgx_trace_closest_noalloc(pgx_ctx* ctx, const pgx_ray* rays, int6
     PGX_CUDA_TRY(ctx, cudaMemsetAsync(counters, 0, sizeof(TraceCounters), s));
     if (n > 0) {
         PGX_CUDA_TRY(ctx, cudaMemcpyAsync(d_rays, rays, sizeof(pgx_ray) * n, cudaMemcpyHostToDevice, s));
-        int64_t blocks = (n + kTraceThreads - 1) / kTraceThreads;
-        unsigned grid = (unsigned)std::min<int64_t>(blocks, 152 * 64);
-        k_trace<false, true><<<grid, kTraceThreads, 0, s>>>(bvh_view(ctx), d_rays, n, d_hits, nullptr, counters);
+        k_trace<false, true><<<persistent_grid(n), kTraceThreads, 0, s>>>(bvh_view(ctx), d_rays, n, d_hits, nullptr,
+                                                                          counters);
         PGX_CUDA_TRY(ctx, cudaGetLastError());
     }
     TraceCounters hc{};
