@@ -286,12 +286,20 @@ def run_relmse_study(args) -> dict:
     plain_img = rgb / spp
     plain_err = relmse(plain_img, ref)
 
-    # Guided: train the cache from `train_spp` plain frames (timed), then
-    # render guided frames until the plain error is reached.
-    ctx.clear()
-    train_ms = render_ms(args.train_spp, abi.MODE_PLAIN, 11, record_paths=args.train_spp)
+    # Guided: train the cache over `train_iters` iterations of 1, 2, 4, ...
+    # frames (the first plain, the rest guided by the previous cache; every
+    # iteration's records rebuild the cache), all timed; then render guided
+    # frames until the plain error is reached.
+    train_ms = 0.0
+    train_spp = 0
+    for it in range(args.train_iters):
+        ctx.clear()
+        n = 1 << it
+        mode = abi.MODE_PLAIN if it == 0 else abi.MODE_GUIDED_QUADTREE
+        train_ms += render_ms(n, mode, 11 + it, record_paths=n, guide_fraction=args.guide_fraction)
+        train_ms += ctx.cache_stats().build_ms
+        train_spp += n
     cst = ctx.cache_stats()
-    train_ms += cst.build_ms
     ctx.clear()
     guided_ms = 0.0
     curve = []
@@ -323,7 +331,8 @@ def run_relmse_study(args) -> dict:
         "reference": {"spp": args.ref_spp, "ms": ref_ms},
         "plain": {"spp": args.plain_spp, "ms": plain_ms, "relmse": plain_err,
                   "rrmse_metrics_h": rrmse_reference_metric(plain_img, ref)},
-        "guided": {"train_spp": args.train_spp, "cache_records": cst.records, "train_ms": train_ms,
+        "guided": {"train_spp": train_spp, "train_iters": args.train_iters, "cache_records": cst.records,
+                   "train_ms": train_ms,
                    "guide_fraction": args.guide_fraction, "spp_rendered": total,
                    "ms_to_plain_error": reached_ms, "relmse_at_plain_time": eq_err,
                    "rrmse_metrics_h_final": rrmse_reference_metric(guided_img, ref),
@@ -385,8 +394,8 @@ def main() -> None:
     ap.add_argument("--study-res", default="640x360")
     ap.add_argument("--ref-spp", type=int, default=16384)
     ap.add_argument("--plain-spp", type=int, default=1024)
-    ap.add_argument("--train-spp", type=int, default=4)
-    ap.add_argument("--guide-fraction", type=float, default=0.5)
+    ap.add_argument("--train-iters", type=int, default=6)
+    ap.add_argument("--guide-fraction", type=float, default=0.25)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     if args.gpus != 1 or int(os.environ.get("WORLD_SIZE", "1")) != 1:

@@ -344,11 +344,13 @@ int pgx_cache_knn(pgx_ctx* ctx, const float* queries, int64_t nq, int32_t k,
                   int32_t* idx, float* d2);
 
 /* Guide queries (extension; the reference has no guiding distribution).
- * For each position, the QuadTree of the cache region nearest to it:
- * pgx_guide_pdf gives the solid-angle pdf of direction dirs[i] (0 where the
- * region has no recorded flux); pgx_guide_sample maps two uniforms u2[2i],
- * u2[2i+1] to a direction and its pdf (pdf 0 and direction (0,0,1) when the
- * region has no flux).  positions, dirs: n*3 floats. */
+ * For each position, the QuadTree of its cache region (found by descending
+ * the point BVH towards the position): pgx_guide_pdf gives the solid-angle
+ * pdf of direction dirs[i] under the QuadTree alone (0 where the region has
+ * no recorded flux); pgx_guide_sample maps two uniforms u2[2i], u2[2i+1] to a
+ * QuadTree direction and its pdf (pdf 0 and direction (0,0,1) when the
+ * region has no flux).  The renderer mixes this distribution with a 20 %
+ * uniform share.  positions, dirs: n*3 floats. */
 int pgx_guide_pdf(pgx_ctx* ctx, const float* positions, const float* dirs, int64_t n, float* pdf);
 int pgx_guide_sample(pgx_ctx* ctx, const float* positions, const float* u2, int64_t n, float* dirs, float* pdf);
 

@@ -26,7 +26,7 @@ constexpr int kSmall = 256;      // one-thread subtrees at or below this size
 constexpr int kChunk = 2048;
 constexpr int kThreads = 256;
 constexpr int kPer = kChunk / kThreads;
-constexpr int kRegionMax = 512;  // guide region size bound
+constexpr int kRegionMax = 1024;  // guide region size bound
 constexpr int kStack = 128;
 
 struct PItem {
@@ -36,7 +36,6 @@ struct PItem {
     unsigned prefix;
     int k;
     int lcur, rcur, tie;
-    int region_parent;  // parent count > kRegionMax
     int acc[2][6];      // child bounds: min xyz, max xyz (ordered ints)
 };
 
@@ -51,7 +50,7 @@ struct PMisc {
 
 struct CacheState {
     DevBuf recs_in, recs, pos, idx, idx2, nodes, trav, items, items2, hist, chunks, small, misc, regions, region_of;
-    DevBuf qroot, qnodes, knn_q, knn_i, knn_d;
+    DevBuf qroot, qnodes, knn_q, knn_i, knn_d, node_region;
     int64_t n_records = 0;
     int64_t n_nodes = 0;
     int n_regions = 0;
@@ -107,7 +106,6 @@ __global__ void k_root(const float4* __restrict__ pos, int64_t n, PMisc* misc, p
     it.node = 0;
     it.offset = 0;
     it.used = (int)n;
-    it.region_parent = 0;
     misc->nitems_next = 1;
 }
 
@@ -319,7 +317,7 @@ __global__ void k_pcopy(const PItem* __restrict__ items, const int2* __restrict_
 }
 
 __global__ void k_pcommit(PItem* items, int nitems, PItem* next, int next_cap, int* small, int small_cap,
-                          pgx_cache_node* nodes, int2* regions, PMisc* misc) {
+                          pgx_cache_node* nodes, int2* regions, int* node_region, PMisc* misc) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nitems) return;
     PItem& it = items[i];
@@ -344,6 +342,7 @@ __global__ void k_pcommit(PItem* items, int nitems, PItem* next, int next_cap, i
         if (cn <= kRegionMax && it.used > kRegionMax) {
             int r = atomicAdd(&misc->nregions, 1);
             regions[r] = make_int2(cs, cn);
+            node_region[c + side] = r;
         }
         if (cn <= kLeafMax) continue;
         if (cn <= kSmall) {
@@ -472,64 +471,132 @@ __global__ void k_regions(const int2* __restrict__ regions, int nreg, const pgx_
     }
 }
 
-// One thread builds one region's quadtree (pgx_guide.cuh).
-__global__ void k_quadtree(const int2* __restrict__ regions, int nreg, const pgx_path_vertex* __restrict__ recs,
-                           int* __restrict__ qroot, QuadNode* __restrict__ qnodes) {
-    int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= nreg) return;
+// Record weight for the guide: luminance of Li, clamped at kClampMedian x the
+// region's median luminance so that a few very bright records (the sun seen
+// through a specular chain) do not take the whole distribution.
+constexpr float kClampMedian = 10.f;
+
+__device__ __forceinline__ float record_lum(const pgx_path_vertex& v) {
+    float w = ((0.2126f * v.Li[0]) + (0.7152f * v.Li[1])) + (0.0722f * v.Li[2]);
+    return (isfinite(w) && w > 0.f) ? w : 0.f;
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    return v;
+}
+__device__ __forceinline__ int warp_sum_i(int v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    return v;
+}
+
+// One warp builds one region's quadtree (pgx_guide.cuh): the lanes stride
+// over the region's records and reduce with shuffles; lane 0 keeps the BFS
+// queue of cells in shared memory.
+constexpr int kQtWarps = 4;
+
+__global__ void __launch_bounds__(32 * kQtWarps) k_quadtree(const int2* __restrict__ regions, int nreg,
+                                                            const pgx_path_vertex* __restrict__ recs,
+                                                            int* __restrict__ qroot, QuadNode* __restrict__ qnodes) {
+    __shared__ float s_u[kQtWarps][PGX_QT_MAX_NODES], s_v[kQtWarps][PGX_QT_MAX_NODES],
+        s_s[kQtWarps][PGX_QT_MAX_NODES];
+    __shared__ unsigned char s_d[kQtWarps][PGX_QT_MAX_NODES];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r = blockIdx.x * kQtWarps + warp;
+    if (r >= nreg) return;  // uniform per warp
     int2 g = regions[r];
-    float total = 0.f;
-    for (int i = 0; i < g.y; i++) {
-        const pgx_path_vertex& v = recs[g.x + i];
-        float w = ((0.2126f * v.Li[0]) + (0.7152f * v.Li[1])) + (0.0722f * v.Li[2]);
-        if (isfinite(w) && w > 0.f) total += w;
+    const pgx_path_vertex* rr = recs + g.x;
+    // Median of the positive luminances by bisection on the value.
+    float lo = FLT_MAX, hi = 0.f;
+    int pos = 0;
+    for (int i = lane; i < g.y; i += 32) {
+        float w = record_lum(rr[i]);
+        if (w > 0.f) {
+            lo = fminf(lo, w);
+            hi = fmaxf(hi, w);
+            pos++;
+        }
     }
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = fminf(lo, __shfl_xor_sync(0xFFFFFFFFu, lo, o));
+        hi = fmaxf(hi, __shfl_xor_sync(0xFFFFFFFFu, hi, o));
+    }
+    pos = warp_sum_i(pos);
+    if (pos == 0) {
+        if (lane == 0) qroot[r] = -1;
+        return;
+    }
+    const int half_count = (pos + 1) / 2;
+    for (int it = 0; it < 24; it++) {
+        float mid = 0.5f * (lo + hi);
+        int below = 0;
+        for (int i = lane; i < g.y; i += 32) {
+            float w = record_lum(rr[i]);
+            if (w > 0.f && w <= mid) below++;
+        }
+        below = warp_sum_i(below);
+        if (below >= half_count)
+            hi = mid;
+        else
+            lo = mid;
+    }
+    const float clamp = kClampMedian * hi;
+    float total = 0.f;
+    for (int i = lane; i < g.y; i += 32) total += fminf(record_lum(rr[i]), clamp);
+    total = warp_sum(total);
     if (!(total > 0.f) || !isfinite(total)) {
-        qroot[r] = -1;
+        if (lane == 0) qroot[r] = -1;
         return;
     }
     QuadNode* out = qnodes + (size_t)r * PGX_QT_MAX_NODES;
-    // BFS over cells: (u0, v0, size, depth) per node index.
-    float cu[PGX_QT_MAX_NODES], cv[PGX_QT_MAX_NODES], cs[PGX_QT_MAX_NODES];
-    int cd[PGX_QT_MAX_NODES];
+    float* cu = s_u[warp];
+    float* cv = s_v[warp];
+    float* cs = s_s[warp];
+    unsigned char* cd = s_d[warp];
+    if (lane == 0) {
+        cu[0] = 0.f;
+        cv[0] = 0.f;
+        cs[0] = 1.f;
+        cd[0] = 0;
+    }
+    __syncwarp();
     int nn = 1, head = 0;
-    cu[0] = 0.f;
-    cv[0] = 0.f;
-    cs[0] = 1.f;
-    cd[0] = 0;
     const float thresh = 0.01f * total;
     while (head < nn) {
         int node = head++;
-        float u0 = cu[node], v0 = cv[node], s = cs[node], half = s * 0.5f;
+        float u0 = cu[node], v0 = cv[node], sz = cs[node], half = sz * 0.5f;
         float flux[4] = {0.f, 0.f, 0.f, 0.f};
         int cnt[4] = {0, 0, 0, 0};
-        for (int i = 0; i < g.y; i++) {
-            const pgx_path_vertex& v = recs[g.x + i];
-            float w = ((0.2126f * v.Li[0]) + (0.7152f * v.Li[1])) + (0.0722f * v.Li[2]);
-            if (!(isfinite(w) && w > 0.f)) continue;
+        for (int i = lane; i < g.y; i += 32) {
+            float w = fminf(record_lum(rr[i]), clamp);
+            if (!(w > 0.f)) continue;
             float u, vv;
-            dir_to_uv(f3(v.wi[0], v.wi[1], v.wi[2]), u, vv);
-            if (u < u0 || u >= u0 + s || vv < v0 || vv >= v0 + s) continue;
+            dir_to_uv(f3(rr[i].wi[0], rr[i].wi[1], rr[i].wi[2]), u, vv);
+            if (u < u0 || u >= u0 + sz || vv < v0 || vv >= v0 + sz) continue;
             int c = 2 * (vv >= v0 + half ? 1 : 0) + (u >= u0 + half ? 1 : 0);
             flux[c] += w;
             cnt[c]++;
         }
         QuadNode q;
         for (int c = 0; c < 4; c++) {
-            q.flux[c] = flux[c];
+            q.flux[c] = warp_sum(flux[c]);
+            int cc = warp_sum_i(cnt[c]);
             q.child[c] = -1;
-            if (flux[c] > thresh && cnt[c] >= 2 && cd[node] + 1 < PGX_QT_MAX_DEPTH && nn < PGX_QT_MAX_NODES) {
+            if (q.flux[c] > thresh && cc >= 2 && cd[node] + 1 < PGX_QT_MAX_DEPTH && nn < PGX_QT_MAX_NODES) {
                 int k = nn++;
-                cu[k] = u0 + half * (float)(c & 1);
-                cv[k] = v0 + half * (float)(c >> 1);
-                cs[k] = half;
-                cd[k] = cd[node] + 1;
+                if (lane == 0) {
+                    cu[k] = u0 + half * (float)(c & 1);
+                    cv[k] = v0 + half * (float)(c >> 1);
+                    cs[k] = half;
+                    cd[k] = (unsigned char)(cd[node] + 1);
+                }
                 q.child[c] = k;
             }
         }
-        out[node] = q;
+        __syncwarp();
+        if (lane == 0) out[node] = q;
     }
-    qroot[r] = 0;  // region-relative; guide_view rebases
+    if (lane == 0) qroot[r] = 0;  // region-relative; k_rebase makes it absolute
 }
 
 __global__ void k_rebase(int* qroot, int nreg) {
@@ -632,7 +699,7 @@ __global__ void k_guide_query(GuideView g, const float* __restrict__ pos, const 
             w = uv_to_dir(u, v);
             float pu, pv;
             dir_to_uv(w, pu, pv);
-            p = quad_pdf(g.qnodes, root, pu, pv) * inv4pi;
+            p = quad_pdf(g.qnodes, root, pu, pv) * inv4pi;  // the quadtree alone
         }
         dirs[3 * i] = w.x;
         dirs[3 * i + 1] = w.y;
@@ -674,6 +741,7 @@ GuideView guide_view(const pgx_ctx* ctx) {
     g.rec_pos = cs->pos.as<float4>();
     g.region_qroot = cs->qroot.as<int>();
     g.qnodes = cs->qnodes.as<QuadNode>();
+    g.node_region = cs->node_region.as<int>();
     return g;
 }
 
@@ -715,6 +783,11 @@ int cache_build_device(pgx_ctx* ctx, const pgx_path_vertex* d_records, int64_t n
     PGX_CUDA_TRY(ctx, cs->small.reserve(sizeof(int) * small_cap));
     PGX_CUDA_TRY(ctx, cs->misc.reserve(sizeof(PMisc) + sizeof(int) * 8));
     PGX_CUDA_TRY(ctx, cs->regions.reserve(sizeof(int2) * reg_cap));
+    PGX_CUDA_TRY(ctx, cs->node_region.reserve(sizeof(int) * max_nodes));
+    // -1 everywhere; region roots get their region index (the root: region 0
+    // when the whole cache is one region).
+    PGX_CUDA_TRY(ctx, cudaMemsetAsync(cs->node_region.p, 0xFF, sizeof(int) * max_nodes, s));
+    if (n <= kRegionMax) PGX_CUDA_TRY(ctx, cudaMemsetAsync(cs->node_region.p, 0, sizeof(int), s));
     if (d_records != cs->recs_in.as<pgx_path_vertex>())
         PGX_CUDA_TRY(ctx, cudaMemcpyAsync(cs->recs_in.p, d_records, sizeof(pgx_path_vertex) * n,
                                           cudaMemcpyDeviceToDevice, s));
@@ -755,7 +828,8 @@ int cache_build_device(pgx_ctx* ctx, const pgx_path_vertex* d_records, int64_t n
         k_ppart<<<grid, kThreads, 0, s>>>(items, chunks, misc, idx, idx2, pos);
         k_pcopy<<<grid, kThreads, 0, s>>>(items, chunks, misc, idx, idx2);
         k_pcommit<<<blocks_for(nitems, 128), 128, 0, s>>>(items, nitems, items2, (int)item_cap, small,
-                                                          (int)small_cap, nodes, regions, misc);
+                                                          (int)small_cap, nodes, regions, cs->node_region.as<int>(),
+                                                          misc);
         PGX_CUDA_TRY(ctx, cudaGetLastError());
         PGX_CUDA_TRY(ctx, cudaMemcpyAsync(&nitems, &misc->nitems_next, sizeof(int), cudaMemcpyDeviceToHost, s));
         PGX_CUDA_TRY(ctx, cudaStreamSynchronize(s));
@@ -783,8 +857,8 @@ int cache_build_device(pgx_ctx* ctx, const pgx_path_vertex* d_records, int64_t n
     k_regions<<<std::max(1, cs->n_regions), 128, 0, s>>>(regions, cs->n_regions, recs, pos);
     PGX_CUDA_TRY(ctx, cs->qroot.reserve(sizeof(int) * std::max(1, cs->n_regions)));
     PGX_CUDA_TRY(ctx, cs->qnodes.reserve(sizeof(QuadNode) * PGX_QT_MAX_NODES * (size_t)std::max(1, cs->n_regions)));
-    k_quadtree<<<blocks_for(cs->n_regions, 64), 64, 0, s>>>(regions, cs->n_regions, recs, cs->qroot.as<int>(),
-                                                              cs->qnodes.as<QuadNode>());
+    k_quadtree<<<blocks_for(cs->n_regions, kQtWarps), 32 * kQtWarps, 0, s>>>(
+        regions, cs->n_regions, recs, cs->qroot.as<int>(), cs->qnodes.as<QuadNode>());
     k_rebase_children<<<std::max(1, cs->n_regions), 128, 0, s>>>(cs->qnodes.as<QuadNode>(), cs->qroot.as<int>(),
                                                                    cs->n_regions);
     k_rebase<<<blocks_for(cs->n_regions, 128), 128, 0, s>>>(cs->qroot.as<int>(), cs->n_regions);

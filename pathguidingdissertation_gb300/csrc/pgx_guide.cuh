@@ -10,7 +10,9 @@
 // while they hold more than 1 % of the region's flux, where a record's flux
 // is the luminance of its Li (Mueller et al. 2017, "Practical Path Guiding").
 //
-// At a shading point the region of the nearest cached record is used; the
+// At a shading point the region is found by descending the point BVH; the
+// guide is the region's quadtree mixed with a 20 % uniform share, records are
+// weighted by their luminance clamped at 10x the region's median, and the
 // continuation direction is drawn by one-sample MIS between the guide and
 // the BSDF (probability `guide_fraction` for the guide), and the combined
 // pdf is used both for the throughput and for the MIS weights of NEE and of
@@ -22,7 +24,9 @@
 #include "pgx_shade.cuh"
 
 #define PGX_QT_MAX_DEPTH 10
-#define PGX_QT_MAX_NODES 96
+#define PGX_QT_MAX_NODES 256
+// Share of the guide's samples drawn uniformly over the sphere (defensive).
+#define PGX_GUIDE_UNIFORM 0.2f
 
 // Interior quadtree cell: flux of its four children (index = 2*yhalf + xhalf
 // in (u, v)) and their node indices within the region (-1 = leaf).
@@ -46,6 +50,7 @@ struct GuideView {
     const float4* __restrict__ rec_pos;   // xyz, w = region id bits
     const int* __restrict__ region_qroot; // first QuadNode of each region (-1: no flux)
     const QuadNode* __restrict__ qnodes;
+    const int* __restrict__ node_region;  // region index of region-root nodes, else -1
 };
 
 GuideView guide_view(const pgx_ctx* ctx);
@@ -189,22 +194,41 @@ static __device__ void quad_sample(const QuadNode* qn, int root, float r1, float
     v = v0 + size * r2;
 }
 
-// Region quadtree of the nearest record (-1 when unusable).
+// Region of x: descend the point BVH from the root, entering the child whose
+// box is nearer to x (0 when inside; ties to the left), until a region root.
 __device__ __forceinline__ int guide_region_root(const GuideView& g, F3 x) {
-    if (!g.valid) return -1;
-    int rec = guide_nearest(g, x);
-    if (rec < 0) return -1;
-    int region = __float_as_int(g.rec_pos[rec].w);
-    return g.region_qroot[region];
+    if (!g.valid || g.n_nodes <= 0) return -1;
+    int node = 0;
+    for (int d = 0; d < 64; d++) {
+        int r = g.node_region[node];
+        if (r >= 0) return g.region_qroot[r];
+        CacheTravNode n = g.nodes[node];
+        int l = __float_as_int(n.bmin.w), rt = __float_as_int(n.bmax.w);
+        if (l < 0) return -1;
+        CacheTravNode a = g.nodes[l], b = g.nodes[rt];
+        auto box_d = [&](const CacheTravNode& c) {
+            float dx = fmaxf(fmaxf(c.bmin.x - x.x, x.x - c.bmax.x), 0.f);
+            float dy = fmaxf(fmaxf(c.bmin.y - x.y, x.y - c.bmax.y), 0.f);
+            float dz = fmaxf(fmaxf(c.bmin.z - x.z, x.z - c.bmax.z), 0.f);
+            return dx * dx + dy * dy + dz * dz;
+        };
+        node = (box_d(b) < box_d(a)) ? rt : l;
+    }
+    return -1;
+}
+
+// Solid-angle pdf of the guide (quadtree mixed with a uniform share).
+__device__ __forceinline__ float guide_pdf_dir(const GuideView& g, int qroot, F3 wi) {
+    float u, v;
+    dir_to_uv(wi, u, v);
+    return ((1.f - PGX_GUIDE_UNIFORM) * quad_pdf(g.qnodes, qroot, u, v) + PGX_GUIDE_UNIFORM) *
+           (1.f / (4.f * 3.14159265f));
 }
 
 // Solid-angle pdf of the one-sample mixture at wi.
 __device__ __forceinline__ float mixture_pdf(const GuideView& g, int qroot, float frac, float bsdf_p, F3 wi) {
     if (qroot < 0) return bsdf_p;
-    float u, v;
-    dir_to_uv(wi, u, v);
-    float gp = quad_pdf(g.qnodes, qroot, u, v) * (1.f / (4.f * 3.14159265f));
-    return frac * gp + (1.f - frac) * bsdf_p;
+    return frac * guide_pdf_dir(g, qroot, wi) + (1.f - frac) * bsdf_p;
 }
 
 // Continuation direction for the guided estimator: pdf is the mixture pdf.
@@ -218,7 +242,13 @@ static __device__ F3 guided_sample(const GuideView& g, float frac, const DevMate
     if (sel < frac) {
         float r1 = pgx_rng_next(rng), r2 = pgx_rng_next(rng);
         float u, v;
-        quad_sample(g.qnodes, qroot, r1, r2, u, v);
+        float pick = sel / frac;  // reuse the selection number for the uniform share
+        if (pick < PGX_GUIDE_UNIFORM) {
+            u = r1;
+            v = r2;
+        } else {
+            quad_sample(g.qnodes, qroot, r1, r2, u, v);
+        }
         wi = uv_to_dir(u, v);
         f = bsdf_eval(m, tv, sd, wi);
     } else {
