@@ -341,6 +341,114 @@ def run_relmse_study(args) -> dict:
     }
 
 
+def run_traversal_study(args) -> dict:
+    """Incoherent secondary-ray closest-hit traversal on the ~2M-triangle
+    interior: 10^7 rays whose origins are 1-spp first hits and whose
+    directions are cosine-distributed about the geometric normal (seed 7)."""
+    import torch
+
+    from pathguidingdissertation_gb300 import abi, scenes
+    from pathguidingdissertation_gb300 import build as pkg_build
+    from pathguidingdissertation_gb300.api import Context
+
+    pkg_build.build()
+    desc = scenes.interior(seed=2, target_tris=2_000_000, env_width=64, env_height=32)
+    ctx = Context(0)
+    ctx.upload(desc)
+    t0 = time.perf_counter()
+    ctx.bvh_build()
+    build_s = time.perf_counter() - t0
+    bst = ctx.bvh_stats()
+    rng = np.random.default_rng(7)
+    n = args.trav_rays
+    W, H = desc.camera["width"], desc.camera["height"]
+    px = (rng.random(n) * W).astype(np.float32)
+    py = (rng.random(n) * H).astype(np.float32)
+    cam = ctx.camera_rays(px, py)
+    first = ctx.trace_closest(cam)
+    hit = first["id"] >= 0
+    tris = desc.triangles["v"]["p"].astype(np.float64)
+    ids = first["id"][hit]
+    p = cam["o"][hit] + cam["d"][hit] * first["t"][hit][:, None]
+    e1 = tris[ids, 2] - tris[ids, 1]
+    e2 = tris[ids, 0] - tris[ids, 2]
+    ng = np.cross(e1, e2)
+    ng /= np.linalg.norm(ng, axis=1, keepdims=True)
+    ng = np.where((np.einsum("ij,ij->i", ng, cam["d"][hit]) > 0)[:, None], -ng, ng)
+    # cosine-weighted directions about ng
+    r1, r2 = rng.random(len(ng)), rng.random(len(ng))
+    t = np.where(np.abs(ng[:, 0:1]) > 0.9, [[0.0, 1.0, 0.0]], [[1.0, 0.0, 0.0]])
+    u = np.cross(t, ng)
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    v = np.cross(ng, u)
+    sr = np.sqrt(r1)
+    d = (u * (sr * np.cos(2 * np.pi * r2))[:, None] + v * (sr * np.sin(2 * np.pi * r2))[:, None]
+         + ng * np.sqrt(1 - r1)[:, None])
+    rays = np.zeros(len(d), abi.RAY)
+    rays["o"] = (p + ng * 1e-4).astype(np.float32)
+    rays["d"] = d.astype(np.float32)
+    rays["tmax"] = np.finfo(np.float32).max
+    rays = np.resize(rays, n)  # reuse origins to reach exactly n rays
+    drays = torch.from_numpy(rays.view(np.uint8)).cuda()
+    dhits = torch.empty(n * 16, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    times = []
+    for it in range(args.warmup + args.steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1_ = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.check(ctx.lib.pgx_trace_closest_device(ctx.h, drays.data_ptr(), n, dhits.data_ptr(), stream.cuda_stream))
+        e1_.record(stream)
+        torch.cuda.synchronize()
+        if it >= args.warmup:
+            times.append(e0.elapsed_time(e1_))
+    iv, tt = ctx.trace_counters()
+    hits = dhits.cpu().numpy().view(abi.HIT)
+    ms = float(np.median(times))
+    alg_bytes = iv * 64 + tt * 48
+    peaks = measured_peaks()
+    out = {
+        "study": "incoherent secondary-ray closest-hit traversal",
+        "scene": f"interior, {desc.ntris} triangles, GPU binned-SAH BVH ({bst.nodes} nodes, depth {bst.max_depth}, "
+                 f"SAH {bst.sah_cost:.2f}, build {bst.build_ms:.1f} ms)",
+        "rays": n,
+        "ms": ms,
+        "mrays_per_s": n / ms / 1e3,
+        "interior_nodes_per_ray": iv / n,
+        "triangles_per_ray": tt / n,
+        "alg_gbs": alg_bytes / (ms * 1e-3) / 1e9,
+        "hbm_frac": alg_bytes / (ms * 1e-3) / 1e9 / peaks["hbm_gbs"],
+        "hit_fraction": float(np.mean(hits["id"] >= 0)),
+        "bvh_build_s_host_clock": build_s,
+    }
+    if not args.no_cpu_baseline:
+        from oracle.ffi import Oracle
+        oracle = Oracle()
+        nodes, idx = ctx.bvh_export()
+        sub = min(n, 200_000)
+        ref, _, _ = oracle.trace_closest(desc.triangles, nodes, idx, rays[:sub])
+        out["parity_subset"] = {"rays": sub, "identical": bool(ref.tobytes() == hits[:sub].tobytes())}
+        cores = os.cpu_count() or 1
+        csub = min(n, 2_000_000)
+        try:
+            from oracle.ffi import Reference, reference_available
+            if not reference_available():
+                raise RuntimeError("reference sources not staged")
+            world = Reference(variant="fast").world(desc.triangles)  # BVHNode::build on the host
+            _, cs = world.trace_closest(rays[:csub], threads=cores)
+            world.close()
+            kind, what = "reference", "BVHNode::traverse of the reference (-O3) on its own BVH"
+        except Exception:  # noqa: BLE001
+            t1 = time.perf_counter()
+            oracle.trace_closest_mt(desc.triangles, nodes, idx, rays[:csub], cores)
+            cs = time.perf_counter() - t1
+            kind, what = "port", "the oracle's restatement of BVHNode::traverse on the same tree"
+        out["cpu_baseline"] = {"value": csub / cs / 1e6, "unit": "Mrays/s", "cores": cores, "kind": kind,
+                               "sample": f"{csub} of the rays through {what}"}
+    ctx.close()
+    return out
+
+
 def run_reference(args) -> dict:
     from oracle.ffi import Reference, reference_available
     desc, _, wl = make_workload(args.workload)
@@ -389,13 +497,14 @@ def main() -> None:
     ap.add_argument("--mode", choices=["plain", "guided_quadtree"], default="plain")
     ap.add_argument("--workload", choices=["interior", "cornell"], default="interior")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--study", choices=["relmse"], default=None,
+    ap.add_argument("--study", choices=["relmse", "traversal"], default=None,
                     help="instead of the throughput line, run the equal-time relMSE study")
     ap.add_argument("--study-res", default="640x360")
     ap.add_argument("--ref-spp", type=int, default=16384)
     ap.add_argument("--plain-spp", type=int, default=1024)
     ap.add_argument("--train-iters", type=int, default=6)
     ap.add_argument("--guide-fraction", type=float, default=0.25)
+    ap.add_argument("--trav-rays", type=int, default=10_000_000)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     if args.gpus != 1 or int(os.environ.get("WORLD_SIZE", "1")) != 1:
@@ -407,6 +516,9 @@ def main() -> None:
         raise SystemExit("--steps must be >= 1 and --warmup >= 0")
     if args.study == "relmse":
         print(json.dumps(run_relmse_study(args)))
+        return
+    if args.study == "traversal":
+        print(json.dumps(run_traversal_study(args)))
         return
     out = run_reference(args) if args.impl == "reference" else run_pgx(args)
     print(json.dumps(out))

@@ -326,6 +326,21 @@ int pgx_get_spp(pgx_ctx* ctx, int32_t* spp);
 int pgx_film_read(pgx_ctx* ctx, float* rgb, float* rgb2, int32_t* spp);
 int pgx_render_get_stats(pgx_ctx* ctx, pgx_render_stats* out);
 
+/* ---- BSDF queries -------------------------------------------------------- */
+
+/* `BSDF::sample` (Materials.h:124) for `count` shading points with normal
+ * normals[i] (shading = geometric normal, frame from Frame::fromVector) and
+ * outgoing direction wo[i], driven by the reference's TestSampler
+ * (Sampling.h:26-48): the first two draws are uv[2i], uv[2i+1], later draws
+ * 0.5.  Writes the sampled direction, the BSDF value (may be NULL) and the
+ * pdf (may be NULL).  The material must have a constant albedo. */
+int pgx_bsdf_sample_batch(pgx_ctx* ctx, const pgx_material* mat, const float* normals, const float* wo,
+                          const float* uv, int64_t count, float* wi, float* f, float* pdf);
+/* `BSDF::invert` (Materials.h:125,163-171,287-306,673-681): the primary
+ * sample (u, v) that maps to wi[i]. */
+int pgx_bsdf_invert_batch(pgx_ctx* ctx, const pgx_material* mat, const float* normals, const float* wo,
+                          const float* wi, int64_t count, float* uv);
+
 /* ---- radiance cache ------------------------------------------------------ */
 
 /* `PointBVHNode::buildPointBVHNode` (Renderer.h:189-211) over host records. */

@@ -191,6 +191,8 @@ class Reference:
         L.orcref_clear.argtypes = [_P]
         L.orcref_pointbvh.restype = _I64
         L.orcref_pointbvh.argtypes = [_P, _I64, _P, _P]
+        L.orcref_bsdf_roundtrip.restype = None
+        L.orcref_bsdf_roundtrip.argtypes = [_P, _P, _P, _P, _I64, _P, _P, _P, _P]
 
     def bvh_build(self, tris: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
         tris = np.ascontiguousarray(tris, TRIANGLE)
@@ -199,6 +201,21 @@ class Reference:
         idx = np.zeros(max(1, n), np.int32)
         cnt = self.lib.orcref_bvh_build(_p(tris), n, _p(nodes), _p(idx))
         return nodes[:cnt].copy(), idx[:n].copy()
+
+    def bsdf_roundtrip(self, material, normals, wo, uv):
+        """Reference BSDF::sample (TestSampler) and BSDF::invert per row."""
+        mat = np.ascontiguousarray(material, MATERIAL).reshape(())
+        n = np.ascontiguousarray(normals, np.float32).reshape(-1, 3)
+        o = np.ascontiguousarray(wo, np.float32).reshape(-1, 3)
+        u = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+        cnt = len(u)
+        wi = np.zeros((cnt, 3), np.float32)
+        f = np.zeros((cnt, 3), np.float32)
+        pdf = np.zeros(cnt, np.float32)
+        uv_out = np.zeros((cnt, 2), np.float32)
+        self.lib.orcref_bsdf_roundtrip(mat.ctypes.data, _p(n), _p(o), _p(u), cnt, _p(wi), _p(f), _p(pdf),
+                                       _p(uv_out))
+        return wi, f, pdf, uv_out
 
     def world(self, tris: np.ndarray) -> "RefWorld":
         return RefWorld(self, tris)

@@ -406,6 +406,42 @@ int64_t orcref_pointbvh(const pgx_path_vertex* recs, int64_t n, pgx_cache_node* 
     return count;
 }
 
+// BSDF::sample driven by TestSampler (Sampling.h:26-48) and BSDF::invert
+// for shading points with normal n[i] and outgoing direction wo[i], as
+// runTest sets them up (main.cpp:301-306).
+void orcref_bsdf_roundtrip(const pgx_material* mat, const float* n, const float* wo, const float* uv, int64_t count,
+                           float* wi_out, float* f_out, float* pdf_out, float* uv_out) {
+    std::vector<Texture*> none;
+    BSDF* bsdf = make_bsdf(*mat, none);
+    TestSampler ts;
+    for (int64_t i = 0; i < count; i++) {
+        ShadingData sd;
+        sd.sNormal = Vec4(n[3 * i], n[3 * i + 1], n[3 * i + 2]);
+        sd.gNormal = sd.sNormal;
+        sd.wo = Vec4(wo[3 * i], wo[3 * i + 1], wo[3 * i + 2]);
+        sd.x = Vec4(0.f, 0.f, 0.f);
+        sd.tu = 0.f;
+        sd.tv = 0.f;
+        sd.bsdf = bsdf;
+        sd.frame.fromVector(sd.sNormal);
+        ts.set(uv[2 * i], uv[2 * i + 1]);
+        Colour col(0.f, 0.f, 0.f);
+        float pdf = 0.f;
+        Vec4 wi = bsdf->sample(sd, &ts, col, pdf);
+        float uo = 0.f, vo = 0.f;
+        bsdf->invert(sd, wi, uo, vo);
+        wi_out[3 * i] = wi.x;
+        wi_out[3 * i + 1] = wi.y;
+        wi_out[3 * i + 2] = wi.z;
+        f_out[3 * i] = col.r;
+        f_out[3 * i + 1] = col.g;
+        f_out[3 * i + 2] = col.b;
+        pdf_out[i] = pdf;
+        uv_out[2 * i] = uo;
+        uv_out[2 * i + 1] = vo;
+    }
+}
+
 void orcref_rng_floats(uint64_t seed, uint64_t pixel, uint64_t sample, int32_t count, float* out) {
     PcgSampler s;
     s.reset(seed, pixel, sample);

@@ -115,6 +115,8 @@ SIGNATURES = {
     "pgx_get_spp": (C.c_int, [_P, C.POINTER(_I32)]),
     "pgx_film_read": (C.c_int, [_P, _P, _P, C.POINTER(_I32)]),
     "pgx_render_get_stats": (C.c_int, [_P, C.POINTER(RenderStats)]),
+    "pgx_bsdf_sample_batch": (C.c_int, [_P, _P, _P, _P, _P, _I64, _P, _P, _P]),
+    "pgx_bsdf_invert_batch": (C.c_int, [_P, _P, _P, _P, _P, _I64, _P]),
     "pgx_cache_build": (C.c_int, [_P, _P, _I64]),
     "pgx_cache_build_from_render": (C.c_int, [_P]),
     "pgx_cache_get_stats": (C.c_int, [_P, C.POINTER(CacheStats)]),

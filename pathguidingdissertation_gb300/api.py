@@ -153,6 +153,29 @@ class Context:
         self.check(self.lib.pgx_render_get_stats(self.h, C.byref(s)))
         return s
 
+    # ---- BSDF queries ---------------------------------------------------------
+    def bsdf_sample(self, material: np.ndarray, normals: np.ndarray, wo: np.ndarray, uv: np.ndarray):
+        """BSDF::sample with TestSampler semantics: (wi, f, pdf) per row."""
+        mat = np.ascontiguousarray(material, abi.MATERIAL).reshape(())
+        n = np.ascontiguousarray(normals, np.float32).reshape(-1, 3)
+        o = np.ascontiguousarray(wo, np.float32).reshape(-1, 3)
+        u = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+        wi = np.zeros((len(u), 3), np.float32)
+        f = np.zeros((len(u), 3), np.float32)
+        pdf = np.zeros(len(u), np.float32)
+        self.check(self.lib.pgx_bsdf_sample_batch(self.h, mat.ctypes.data, ptr(n), ptr(o), ptr(u), len(u), ptr(wi),
+                                                  ptr(f), ptr(pdf)))
+        return wi, f, pdf
+
+    def bsdf_invert(self, material: np.ndarray, normals: np.ndarray, wo: np.ndarray, wi: np.ndarray) -> np.ndarray:
+        mat = np.ascontiguousarray(material, abi.MATERIAL).reshape(())
+        n = np.ascontiguousarray(normals, np.float32).reshape(-1, 3)
+        o = np.ascontiguousarray(wo, np.float32).reshape(-1, 3)
+        w = np.ascontiguousarray(wi, np.float32).reshape(-1, 3)
+        uv = np.zeros((len(w), 2), np.float32)
+        self.check(self.lib.pgx_bsdf_invert_batch(self.h, mat.ctypes.data, ptr(n), ptr(o), ptr(w), len(w), ptr(uv)))
+        return uv
+
     # ---- radiance cache -------------------------------------------------------
     def cache_build(self, records: np.ndarray) -> None:
         records = np.ascontiguousarray(records, abi.PATH_VERTEX)

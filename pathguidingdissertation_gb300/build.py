@@ -47,7 +47,7 @@ def _deps() -> list[Path]:
 # Per-file flags: the integrator and the cache round every product and sum
 # separately, like the reference's scalar code and the float32 checks
 # (traversal uses explicit _rn intrinsics and is exact regardless).
-FILE_FLAGS = {"render.cu": ["-fmad=false"], "cache.cu": ["-fmad=false"]}
+FILE_FLAGS = {"render.cu": ["-fmad=false"], "cache.cu": ["-fmad=false"], "bsdf.cu": ["-fmad=false"]}
 
 
 def _compile(src: Path, extra: list[str]) -> Path:

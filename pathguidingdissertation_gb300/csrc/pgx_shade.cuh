@@ -375,14 +375,31 @@ static __device__ __noinline__ float bsdf_pdf(const DevMaterial& m, const TexVie
     (void)tv;
 }
 
-// BSDF::sample for all kinds; consumes random numbers like the reference.
-static __device__ __noinline__ F3 bsdf_sample(const DevMaterial& m, const TexView& tv, const Shading& sd, uint64_t& rng, F3& f,
-                          float& pdf) {
+// Samplers: the path's PCG32 stream, or the reference's TestSampler
+// (Sampling.h:26-48: the first two draws are u and v, every later one 0.5).
+struct PcgSampler {
+    uint64_t& state;
+    __device__ float next() { return pgx_rng_next(state); }
+};
+struct FixedSampler {
+    float u, v;
+    int called;
+    __device__ float next() {
+        float r = called == 0 ? u : (called == 1 ? v : 0.5f);
+        called++;
+        return r;
+    }
+};
+
+// BSDF::sample for all kinds; draws from the sampler exactly like the reference.
+template <class Smp>
+static __device__ __noinline__ F3 bsdf_sample_s(const DevMaterial& m, const TexView& tv, const Shading& sd, Smp& rng,
+                                                F3& f, float& pdf) {
     switch (m.kind) {
         case PGX_BSDF_DIFFUSE:
         case PGX_BSDF_ORENNAYAR: {
-            float r1 = pgx_rng_next(rng);
-            float r2 = pgx_rng_next(rng);
+            float r1 = rng.next();
+            float r2 = rng.next();
             F3 wi = to_world(sd.frame, cosine_sample(r1, r2));
             f = bsdf_eval(m, tv, sd, wi);
             pdf = bsdf_pdf(m, tv, sd, wi);
@@ -414,8 +431,8 @@ static __device__ __noinline__ F3 bsdf_sample(const DevMaterial& m, const TexVie
                 pdf = 1.f;
                 return to_world(sd.frame, wr);
             }
-            float r1 = pgx_rng_next(rng);
-            float r2 = pgx_rng_next(rng);
+            float r1 = rng.next();
+            float r2 = rng.next();
             F3 h = ggx_sample_h(m.alpha, r1, r2);
             F3 wil = -wol + (h * 2.f) * dot(h, wol);
             F3 wi = to_world(sd.frame, wil);
@@ -435,7 +452,7 @@ static __device__ __noinline__ F3 bsdf_sample(const DevMaterial& m, const TexVie
             float eta = (ci < 0.f) ? (m.int_ior / m.ext_ior) : (m.ext_ior / m.int_ior);
             if (ci < 0.f) ci = fabsf(ci);
             F3 alb = albedo_of(tv, m, sd);
-            if (pgx_rng_next(rng) < F) {
+            if (rng.next() < F) {
                 F3 wr = f3(-wol.x, -wol.y, wol.z);
                 pdf = F;
                 f = divs(alb, fabsf(wr.z)) * F;
@@ -463,7 +480,7 @@ static __device__ __noinline__ F3 bsdf_sample(const DevMaterial& m, const TexVie
             F3 alb = albedo_of(tv, m, sd);
             if (m.alpha < PGX_EPSILON) {
                 float F = fresnel_dielectric(wol.z, m.int_ior, m.ext_ior);
-                if (pgx_rng_next(rng) < F) {
+                if (rng.next() < F) {
                     F3 w = f3(-wol.x, -wol.y, wol.z);
                     pdf = F;
                     f = divs(alb, fabsf(w.z)) * F;
@@ -487,11 +504,11 @@ static __device__ __noinline__ F3 bsdf_sample(const DevMaterial& m, const TexVie
                 f = divs(alb, fabsf(w.z)) * (1.f - F);
                 return to_world(sd.frame, w);
             }
-            float r1 = pgx_rng_next(rng), r2 = pgx_rng_next(rng);
+            float r1 = rng.next(), r2 = rng.next();
             F3 h = ggx_sample_h(m.alpha, r1, r2);
             float F = fresnel_dielectric(dot(wol, h), m.int_ior, m.ext_ior);
             F3 wi;
-            if (pgx_rng_next(rng) < F) {
+            if (rng.next() < F) {
                 wi = to_world(sd.frame, -wol + (h * 2.f) * dot(h, wol));
             } else {
                 Frame hf = frame_from(h);
@@ -512,11 +529,11 @@ static __device__ __noinline__ F3 bsdf_sample(const DevMaterial& m, const TexVie
         }
         case PGX_BSDF_PLASTIC: {
             F3 wol = to_local(sd.frame, sd.wo);
-            float r1 = pgx_rng_next(rng);
-            float r2 = pgx_rng_next(rng);
+            float r1 = rng.next();
+            float r2 = rng.next();
             float F = fresnel_dielectric(fabsf(wol.z), m.int_ior, m.ext_ior);
             F3 wil;
-            if (pgx_rng_next(rng) < F) {
+            if (rng.next() < F) {
                 float e = plastic_exponent(m.alpha);
                 float th = acosf(powf(1.f - r1, 1.f / (e + 1.f)));
                 float ph = (float)(2.0 * PGX_PI_D * (double)r2);
@@ -534,6 +551,55 @@ static __device__ __noinline__ F3 bsdf_sample(const DevMaterial& m, const TexVie
             pdf = 0.f;
             f = zero3();
             return f3(0.f, 0.f, 1.f);
+    }
+}
+
+__device__ __forceinline__ F3 bsdf_sample(const DevMaterial& m, const TexView& tv, const Shading& sd, uint64_t& rng,
+                                          F3& f, float& pdf) {
+    PcgSampler smp{rng};
+    return bsdf_sample_s(m, tv, sd, smp, f, pdf);
+}
+
+// BSDF::invert (Materials.h:163-171, 287-306, 673-681): the primary sample
+// (u, v) that BSDF::sample would map to wi.  Delta lobes give (0, 0); the
+// reference leaves the rough dielectric and plastic unimplemented
+// (Materials.h:541-543, 782-784), so their (u, v) stay unchanged.
+static __device__ __noinline__ void bsdf_invert(const DevMaterial& m, const Shading& sd, F3 wi, float& u, float& v) {
+    switch (m.kind) {
+        case PGX_BSDF_DIFFUSE:
+        case PGX_BSDF_ORENNAYAR: {
+            F3 wl = to_local(sd.frame, wi);
+            float theta = acosf(wl.z);
+            float phi = spherical_phi(wl);
+            float c = cosf(theta);
+            u = c * c;
+            v = (float)((double)phi / (2.0 * PGX_PI_D));
+            break;
+        }
+        case PGX_BSDF_CONDUCTOR: {
+            if (m.alpha < PGX_EPSILON) {
+                u = 0.f;
+                v = 0.f;
+                break;
+            }
+            F3 wil = to_local(sd.frame, wi), wol = to_local(sd.frame, sd.wo);
+            F3 h = normalize(wil + wol);
+            float theta = acosf(h.z);
+            float phi = spherical_phi(h);
+            float a2 = m.alpha * m.alpha;
+            float a1 = a2 - 1.f;
+            float c = cosf(theta);
+            u = (a2 / ((c * c) * (a1 * a1) + a1)) - (1.f / a1);
+            v = (float)((double)phi / (2.0 * PGX_PI_D));
+            break;
+        }
+        case PGX_BSDF_MIRROR:
+        case PGX_BSDF_GLASS:
+            u = 0.f;
+            v = 0.f;
+            break;
+        default:
+            break;
     }
 }
 

@@ -11,6 +11,9 @@ numpy on another machine.
 * render_<scene>.npz — scene inputs and the films of the reference's own
   integrators (`pathTrace`, `guidedPath`) driven by the PCG32 stream of
   (seed, pixel, sample) through oracle/ref_harness.cpp.
+* bsdf_roundtrip.npz — per material: `BSDF::sample` driven by TestSampler and
+  `BSDF::invert` (Materials.h:121-897) on random normals / outgoing
+  directions.
 * traversal_<scene>.npz — triangles; the reference's BVH (`BVHNode::build`,
   Geometry.h:419-446) as nodes + triangle indexes; rays; closest hits from
   `BVHNode::traverse` (Geometry.h:455-512); any-hit visibility from
@@ -71,8 +74,46 @@ def render_fixture(ref: Reference, name: str, desc, spp: int, seed: int) -> None
           f"plain mean {plain.mean() / spp:.4f}, guided mean {guided.mean() / spp:.4f}")
 
 
+BSDF_CASES = {
+    # name: material keyword arguments (scenes.material)
+    "conductor_runtest": dict(kind=2, albedo=(1, 1, 1), eta=(1.0, 0.6, 1.5), k=(0.65, 0.85, 1.0), roughness=0.5),
+    "conductor_smooth": dict(kind=2, albedo=(0.9, 0.8, 0.7), eta=(0.2, 0.9, 1.1), k=(3.9, 2.4, 2.2), roughness=0.0),
+    "diffuse": dict(kind=0, albedo=(0.6, 0.5, 0.4)),
+    "mirror": dict(kind=1, albedo=(0.9, 0.9, 0.9)),
+    "glass": dict(kind=3, albedo=(1, 1, 1), int_ior=1.5, ext_ior=1.0),
+    "dielectric_rough": dict(kind=4, albedo=(1, 1, 1), int_ior=1.5, ext_ior=1.0, roughness=0.3),
+    "orennayar": dict(kind=5, albedo=(0.7, 0.6, 0.5), sigma=0.5),
+    "plastic": dict(kind=6, albedo=(0.3, 0.5, 0.7), int_ior=1.5, ext_ior=1.0, roughness=0.2),
+}
+
+
+def bsdf_fixture(ref: Reference, count: int = 800, seed: int = 21) -> None:
+    """BSDF::sample with TestSampler and BSDF::invert (Materials.h) per
+    material, for random normals and outgoing directions (some below the
+    surface, to exercise the two-sided and transmission branches)."""
+    rng = np.random.default_rng(seed)
+    out = {}
+    for name, kw in BSDF_CASES.items():
+        n = rng.normal(size=(count, 3))
+        n /= np.linalg.norm(n, axis=1, keepdims=True)
+        wo = rng.normal(size=(count, 3))
+        wo /= np.linalg.norm(wo, axis=1, keepdims=True)
+        flip = np.einsum("ij,ij->i", n, wo) < 0
+        flip[: count // 5] = False  # keep a fifth below the surface
+        wo[flip] = -wo[flip]
+        uv = rng.random((count, 2))
+        n, wo, uv = n.astype(np.float32), wo.astype(np.float32), uv.astype(np.float32)
+        mat = scenes.material(**kw)
+        wi, f, pdf, uv_out = ref.bsdf_roundtrip(mat, n, wo, uv)
+        for k, v in dict(material=mat, n=n, wo=wo, uv=uv, wi=wi, f=f, pdf=pdf, uv_out=uv_out).items():
+            out[f"{name}__{k}"] = v
+    np.savez_compressed(HERE / "bsdf_roundtrip.npz", **out)
+    print(f"bsdf_roundtrip: {len(BSDF_CASES)} materials x {count} samples")
+
+
 def main() -> None:
     ref = Reference()
+    bsdf_fixture(ref)
     render_fixture(ref, "cornell", scenes.cornell_box(seed=1, width=32, height=32), 4, seed=11)
     render_fixture(ref, "interior", scenes.interior(seed=5, target_tris=3000, n_objects=24, width=48, height=27,
                                                     env_width=64, env_height=32), 4, seed=12)

@@ -103,3 +103,24 @@ def test_reference_reproduces_render_fixture(reference, path):
     guided, _, _ = rs.render_pcg(True, int(g["seed"]), 0, int(g["spp"]), threads=4)
     assert np.array_equal(plain, g["plain"])
     assert np.array_equal(guided, g["guided"])
+
+
+def test_reference_runtest_passes(reference):
+    """The reference's own inversion test (main.cpp:13-72) through the harness."""
+    n = 100000
+    rng = np.random.default_rng(1)
+    uv = rng.random((n, 2)).astype(np.float32)
+    normal = np.tile(np.array([0, 1, 0], np.float32), (n, 1))
+    mat = scenes.material(kind=2, albedo=(1, 1, 1), eta=(1.0, 0.6, 1.5), k=(0.65, 0.85, 1.0), roughness=0.5)
+    _, _, _, uv_out = reference.bsdf_roundtrip(mat, normal, normal, uv)
+    d = np.abs(uv.astype(np.float64) - uv_out)
+    d[:, 1] = np.minimum(d[:, 1], np.abs(d[:, 1] - 1.0))
+    assert np.all(d < 1e-4)
+
+
+def test_reference_reproduces_bsdf_fixture(reference):
+    g = np.load(GOLDEN / "bsdf_roundtrip.npz")
+    for case in sorted({k.split("__")[0] for k in g.files}):
+        wi, f, pdf, uv_out = reference.bsdf_roundtrip(g[f"{case}__material"], g[f"{case}__n"], g[f"{case}__wo"],
+                                                      g[f"{case}__uv"])
+        assert np.array_equal(wi, g[f"{case}__wi"]) and np.array_equal(uv_out, g[f"{case}__uv_out"]), case
