@@ -184,6 +184,10 @@ typedef struct pgx_render_config {
 
 /* pgx_render_config.flags */
 #define PGX_RENDER_PROFILE 1
+/* Splat with the Mitchell-Netravali filter, B = C = 1/3, radius 2
+ * (MitchellNetravaliFilter, Imaging.h:153-176) instead of the box filter
+ * RayTracer::init installs (Renderer.h:255). */
+#define PGX_RENDER_FILTER_MITCHELL 2
 
 /* Statistics of the last pgx_render call.  The per-stage times and the
  * node/triangle fetch counts are filled only with PGX_RENDER_PROFILE. */
@@ -325,6 +329,10 @@ int pgx_get_spp(pgx_ctx* ctx, int32_t* spp);
  * NULL).  Both width*height*3 floats. */
 int pgx_film_read(pgx_ctx* ctx, float* rgb, float* rgb2, int32_t* spp);
 int pgx_render_get_stats(pgx_ctx* ctx, pgx_render_stats* out);
+/* Film::tonemap for every pixel (Imaging.h:220-244): film / SPP * exposure,
+ * extended Reinhard with white point lmax_white, gamma 1/2.2, clamped to
+ * 8 bits.  rgb8: width*height*3 bytes (the reference's window back buffer). */
+int pgx_film_tonemap(pgx_ctx* ctx, float exposure, float lmax_white, uint8_t* rgb8);
 
 /* ---- BSDF queries -------------------------------------------------------- */
 

@@ -104,6 +104,12 @@ def build_reference(force: bool = False) -> Path | None:
     new_text = text.replace("#define GUIDED_PATH true", "#define GUIDED_PATH false", 1)
     if not plain_h.exists() or plain_h.read_text() != new_text:
         plain_h.write_text(new_text)
+    # SceneLoader.h includes "Renderer.h" from its own directory first, so the
+    # plain variant needs its own copy beside the edited Renderer.h.
+    loader_text = (REF_SRC / "SceneLoader.h").read_text()
+    plain_loader = plain_dir / "SceneLoader.h"
+    if not plain_loader.exists() or plain_loader.read_text() != loader_text:
+        plain_loader.write_text(loader_text)
     outs = {
         "liborcref.so": ["-O2", "-ffp-contract=off", "-fno-fast-math"],
         "liborcref_fast.so": ["-O3"],

@@ -191,8 +191,30 @@ class Reference:
         L.orcref_clear.argtypes = [_P]
         L.orcref_pointbvh.restype = _I64
         L.orcref_pointbvh.argtypes = [_P, _I64, _P, _P]
+        L.orcref_set_filter.restype = None
+        L.orcref_set_filter.argtypes = [_I32]
+        L.orcref_tonemap.restype = None
+        L.orcref_tonemap.argtypes = [_P, _I32, _I32, _I32, C.c_float, C.c_float, _P]
+        L.orcref_metrics.restype = None
+        L.orcref_metrics.argtypes = [_P, _P, _I32, _I32, _P]
         L.orcref_bsdf_roundtrip.restype = None
         L.orcref_bsdf_roundtrip.argtypes = [_P, _P, _P, _P, _I64, _P, _P, _P, _P]
+        L.orcref_load_scene.restype = _P
+        L.orcref_load_scene.argtypes = [C.c_char_p, _P]
+        L.orcref_loaded_from_arrays.restype = _P
+        L.orcref_loaded_from_arrays.argtypes = [_P, _I64, _P, _I32, _P, _I32, _P, _P, _P]
+        L.orcref_loaded_destroy.restype = None
+        L.orcref_loaded_destroy.argtypes = [_P]
+        for f in (L.orcref_loaded_triangles, L.orcref_loaded_materials, L.orcref_loaded_camera):
+            f.restype = None
+            f.argtypes = [_P, _P]
+        L.orcref_texture_load.restype = _P
+        L.orcref_texture_load.argtypes = [C.c_char_p, _P]
+        L.orcref_texture_read.restype = None
+        L.orcref_texture_read.argtypes = [_P, _P]
+        for f in (L.orcref_loaded_texture_size, L.orcref_loaded_texture):
+            f.restype = None
+            f.argtypes = [_P, _I32, _P]
 
     def bvh_build(self, tris: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
         tris = np.ascontiguousarray(tris, TRIANGLE)
@@ -201,6 +223,24 @@ class Reference:
         idx = np.zeros(max(1, n), np.int32)
         cnt = self.lib.orcref_bvh_build(_p(tris), n, _p(nodes), _p(idx))
         return nodes[:cnt].copy(), idx[:n].copy()
+
+    def set_filter(self, mitchell: bool) -> None:
+        self.lib.orcref_set_filter(int(mitchell))
+
+    def tonemap(self, film: np.ndarray, spp: int, exposure: float = 1.0, lmax_white: float = 10.0) -> np.ndarray:
+        f = np.ascontiguousarray(film, np.float32).copy()
+        h, w = f.shape[:2]
+        out = np.zeros((h, w, 3), np.uint8)
+        self.lib.orcref_tonemap(_p(f), w, h, spp, exposure, lmax_white, _p(out))
+        return out
+
+    def metrics(self, test: np.ndarray, gt: np.ndarray) -> tuple[float, float, float]:
+        t = np.ascontiguousarray(test, np.float32)
+        g = np.ascontiguousarray(gt, np.float32)
+        h, w = t.shape[:2]
+        out = np.zeros(3, np.float32)
+        self.lib.orcref_metrics(_p(t), _p(g), w, h, _p(out))
+        return float(out[0]), float(out[1]), float(out[2])
 
     def bsdf_roundtrip(self, material, normals, wo, uv):
         """Reference BSDF::sample (TestSampler) and BSDF::invert per row."""
@@ -216,6 +256,54 @@ class Reference:
         self.lib.orcref_bsdf_roundtrip(mat.ctypes.data, _p(n), _p(o), _p(u), cnt, _p(wi), _p(f), _p(pdf),
                                        _p(uv_out))
         return wi, f, pdf, uv_out
+
+    def _export_loaded(self, h, counts: np.ndarray) -> dict:
+        L = self.lib
+        try:
+            tris = np.zeros(int(counts[0]), TRIANGLE)
+            L.orcref_loaded_triangles(h, _p(tris))
+            mats = np.zeros((int(counts[1]), 20), np.float32)
+            L.orcref_loaded_materials(h, _p(mats))
+            texs = []
+            for i in list(range(int(counts[2]))) + [-1]:
+                wh = np.zeros(2, np.int32)
+                L.orcref_loaded_texture_size(h, i, _p(wh))
+                if wh[0] == 0:
+                    texs.append(None)
+                    continue
+                img = np.zeros((int(wh[1]), int(wh[0]), 3), np.float32)
+                L.orcref_loaded_texture(h, i, _p(img))
+                texs.append(img)
+            cam = np.zeros(32, np.float32)
+            L.orcref_loaded_camera(h, _p(cam))
+        finally:
+            L.orcref_loaded_destroy(h)
+        return dict(triangles=tris, materials=mats, textures=texs[:-1], env=texs[-1],
+                    projection=cam[:16].reshape(4, 4), camera=cam[16:].reshape(4, 4),
+                    width=int(counts[3]), height=int(counts[4]))
+
+    def load_texture(self, filename: str) -> np.ndarray:
+        """Texture::load of one image file: (H, W, 3) float32 texels."""
+        wh = np.zeros(2, np.int32)
+        h = self.lib.orcref_texture_load(str(filename).encode(), _p(wh))
+        img = np.zeros((int(wh[1]), int(wh[0]), 3), np.float32)
+        self.lib.orcref_texture_read(h, _p(img))
+        return img
+
+    def load_scene(self, scene_dir: str) -> dict:
+        """The reference's loadScene on a scene directory, exported: triangles,
+        per-material parameters (20 floats, see orcref_loaded_materials),
+        distinct albedo textures, environment texels and camera matrices."""
+        counts = np.zeros(5, np.int64)
+        h = self.lib.orcref_load_scene(str(scene_dir).encode(), _p(counts))
+        return self._export_loaded(h, counts)
+
+    def loaded_from_desc(self, desc) -> dict:
+        """The same export for a scene assembled from pgx upload arrays."""
+        sa = SceneArgs(desc)
+        counts = np.zeros(5, np.int64)
+        h = self.lib.orcref_loaded_from_arrays(*sa.args(), _p(counts))
+        return self._export_loaded(h, counts)
 
     def world(self, tris: np.ndarray) -> "RefWorld":
         return RefWorld(self, tris)

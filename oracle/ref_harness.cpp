@@ -37,6 +37,7 @@
 
 #include "Lights.h"
 #include "Materials.h"
+#include "Metrics.h"
 #include "Scene.h"
 
 // Count every ray the integrators trace: `Scene::traverse` and
@@ -63,6 +64,7 @@ static inline int pgx_count_ray() {
 #undef private
 #undef traverse
 #undef visible
+#include "SceneLoader.h"
 
 #include "../include/pgx.h"
 #include "pgx_oracle_rng.h"
@@ -273,6 +275,11 @@ void orcref_scene_destroy(void* h) { delete static_cast<RefScene*>(h); }
 // caller-zeroed); rows are split over `threads` threads with private films.
 // Path vertices of sample `collect` (guided only) go to verts (capacity
 // vcap); returns the number written.  rays_out gets the rays traced.
+static int g_mitchell = 0;
+// Selects the film filter of orcref_render_pcg: 0 box (Renderer.h:255),
+// 1 MitchellNetravaliFilter (Imaging.h:153-176).
+void orcref_set_filter(int32_t mitchell) { g_mitchell = mitchell; }
+
 int64_t orcref_render_pcg(void* h, int32_t guided, uint64_t seed, int32_t spp0, int32_t nspp, float* film_rgb,
                           int32_t threads, int32_t collect, pgx_path_vertex* verts, int64_t vcap,
                           int64_t* rays_out) {
@@ -288,7 +295,8 @@ int64_t orcref_render_pcg(void* h, int32_t guided, uint64_t seed, int32_t spp0, 
         film.height = H;
         film.film = reinterpret_cast<Colour*>(films[(size_t)tid].data());
         BoxFilter box;
-        film.filter = &box;
+        MitchellNetravaliFilter mitchell;
+        film.filter = g_mitchell ? static_cast<ImageFilter*>(&mitchell) : static_cast<ImageFilter*>(&box);
         film.SPP = 0;
         PcgSampler sampler;
         std::vector<PathVertex> scratch;
@@ -440,6 +448,235 @@ void orcref_bsdf_roundtrip(const pgx_material* mat, const float* n, const float*
         uv_out[2 * i] = uo;
         uv_out[2 * i + 1] = vo;
     }
+}
+
+// Film::tonemap (Imaging.h:220-244) of a film buffer for every pixel.
+void orcref_tonemap(float* film_rgb, int32_t w, int32_t h, int32_t spp, float exposure, float lmax_white,
+                    uint8_t* out) {
+    Film film;
+    film.width = w;
+    film.height = h;
+    film.film = reinterpret_cast<Colour*>(film_rgb);
+    film.SPP = spp;
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) {
+            unsigned char r, g, b;
+            film.tonemap(x, y, r, g, b, exposure, lmax_white);
+            size_t i = ((size_t)y * w + x) * 3;
+            out[i] = r;
+            out[i + 1] = g;
+            out[i + 2] = b;
+        }
+}
+
+// Metrics::calculateMSE / RMSE / RRMSE (Metrics.h:8-68).
+void orcref_metrics(const float* test, const float* gt, int32_t w, int32_t h, float* out3) {
+    std::vector<float> t(test, test + (size_t)w * h * 3), g(gt, gt + (size_t)w * h * 3);
+    Metrics m;
+    out3[0] = m.calculateMSE(t, g, w, h);
+    out3[1] = m.calculateRMSE(t, g, w, h);
+    out3[2] = m.calculateRRMSE(t, g, w, h);
+}
+
+// ---- scene ingestion ------------------------------------------------------
+// A scene as the reference holds it after loading: its triangles, BSDF
+// objects, background and camera.  Built either by the reference's own
+// loadScene (SceneLoader.h:222-269) from a scene directory, or from pgx's
+// upload arrays with the harness's make_bsdf, so both sides export through
+// the same code.
+struct RefLoaded {
+    Scene* scene = nullptr;
+    std::vector<Texture*> textures;  // distinct albedo textures, first-use order
+};
+
+static void collect_textures(RefLoaded* rl) {
+    for (BSDF* b : rl->scene->materials) {
+        BSDF* base = b;
+        if (auto* l = dynamic_cast<LayeredBSDF*>(b)) base = l->base;
+        Texture* t = nullptr;
+        if (auto* m = dynamic_cast<DiffuseBSDF*>(base)) t = m->albedo;
+        else if (auto* m = dynamic_cast<MirrorBSDF*>(base)) t = m->albedo;
+        else if (auto* m = dynamic_cast<ConductorBSDF*>(base)) t = m->albedo;
+        else if (auto* m = dynamic_cast<GlassBSDF*>(base)) t = m->albedo;
+        else if (auto* m = dynamic_cast<DielectricBSDF*>(base)) t = m->albedo;
+        else if (auto* m = dynamic_cast<OrenNayarBSDF*>(base)) t = m->albedo;
+        else if (auto* m = dynamic_cast<PlasticBSDF*>(base)) t = m->albedo;
+        if (t && std::find(rl->textures.begin(), rl->textures.end(), t) == rl->textures.end()) rl->textures.push_back(t);
+    }
+}
+
+// loadScene on `dir`; counts go to counts[0..3] = triangles, materials,
+// textures, width, height (counts has 5 entries).
+void* orcref_load_scene(const char* dir, int64_t* counts) {
+    RefLoaded* rl = new RefLoaded();
+    std::streambuf* old = std::cout.rdbuf(nullptr);
+    rl->scene = loadScene(dir);
+    std::cout.rdbuf(old);
+    collect_textures(rl);
+    counts[0] = (int64_t)rl->scene->triangles.size();
+    counts[1] = (int64_t)rl->scene->materials.size();
+    counts[2] = (int64_t)rl->textures.size();
+    counts[3] = (int64_t)rl->scene->camera.width;
+    counts[4] = (int64_t)rl->scene->camera.height;
+    return rl;
+}
+
+// The same assembly from pgx arrays (orcref_scene_create's path).
+void* orcref_loaded_from_arrays(const pgx_triangle* tris, int64_t n, const pgx_material* mats, int32_t nm,
+                                const pgx_texture* textures, int32_t ntex, const pgx_texture* env,
+                                const pgx_camera* cam, int64_t* counts) {
+    RefLoaded* rl = new RefLoaded();
+    rl->scene = new Scene();
+    std::vector<Texture*> texs;
+    for (int32_t i = 0; i < ntex; i++) texs.push_back(make_texture(textures[i].width, textures[i].height, textures[i].rgb));
+    std::vector<BSDF*> bsdfs;
+    for (int32_t i = 0; i < nm; i++) bsdfs.push_back(make_bsdf(mats[i], texs));
+    Light* background;
+    if (env) background = new EnvironmentMap(make_texture(env->width, env->height, env->rgb));
+    else background = new BackgroundColour(Colour(0.0f, 0.0f, 0.0f));
+    Matrix P = Matrix::perspective(0.001f, 10000.0f, (float)cam->width / (float)cam->height, cam->fov_degrees);
+    Matrix V = Matrix::lookAt(Vec4(cam->from[0], cam->from[1], cam->from[2]), Vec4(cam->to[0], cam->to[1], cam->to[2]),
+                              Vec4(cam->up[0], cam->up[1], cam->up[2]));
+    V = V.invert();
+    if (cam->flip_x == 1) P.a[0][0] = -P.a[0][0];
+    rl->scene->camera.init(P, cam->width, cam->height);
+    rl->scene->camera.updateView(V);
+    rl->scene->init(to_triangles(tris, n), bsdfs, background);
+    collect_textures(rl);
+    counts[0] = (int64_t)rl->scene->triangles.size();
+    counts[1] = (int64_t)rl->scene->materials.size();
+    counts[2] = (int64_t)rl->textures.size();
+    counts[3] = (int64_t)rl->scene->camera.width;
+    counts[4] = (int64_t)rl->scene->camera.height;
+    return rl;
+}
+
+void orcref_loaded_destroy(void* h) { delete static_cast<RefLoaded*>(h); }
+
+// Triangles as pgx_triangle (vertex position, normal, uv; material index).
+void orcref_loaded_triangles(void* h, pgx_triangle* out) {
+    RefLoaded* rl = static_cast<RefLoaded*>(h);
+    for (size_t i = 0; i < rl->scene->triangles.size(); i++) {
+        const Triangle& t = rl->scene->triangles[i];
+        for (int k = 0; k < 3; k++) {
+            const Vertex& v = t.vertices[k];
+            out[i].v[k].p[0] = v.p.x;
+            out[i].v[k].p[1] = v.p.y;
+            out[i].v[k].p[2] = v.p.z;
+            out[i].v[k].n[0] = v.normal.x;
+            out[i].v[k].n[1] = v.normal.y;
+            out[i].v[k].n[2] = v.normal.z;
+            out[i].v[k].u = v.u;
+            out[i].v[k].v = v.v;
+        }
+        out[i].material = t.materialIndex;
+    }
+}
+
+// Per material 20 floats: kind (pgx numbering), layered, emission rgb,
+// intIOR, extIOR, alpha (the constructor's value, not the roughness),
+// sigma, eta rgb, k rgb, albedo texture index, coating sigmaA rgb,
+// coating thickness.
+void orcref_loaded_materials(void* h, float* out) {
+    RefLoaded* rl = static_cast<RefLoaded*>(h);
+    for (size_t i = 0; i < rl->scene->materials.size(); i++) {
+        float* p = out + 20 * i;
+        for (int j = 0; j < 20; j++) p[j] = 0.f;
+        BSDF* b = rl->scene->materials[i];
+        BSDF* base = b;
+        if (auto* l = dynamic_cast<LayeredBSDF*>(b)) {
+            base = l->base;
+            p[1] = 1.f;
+            p[16] = l->sigmaa.r;
+            p[17] = l->sigmaa.g;
+            p[18] = l->sigmaa.b;
+            p[19] = l->thickness;
+        }
+        p[2] = b->emission.r;
+        p[3] = b->emission.g;
+        p[4] = b->emission.b;
+        Texture* t = nullptr;
+        if (auto* m = dynamic_cast<DiffuseBSDF*>(base)) {
+            p[0] = PGX_BSDF_DIFFUSE;
+            t = m->albedo;
+        } else if (auto* m = dynamic_cast<MirrorBSDF*>(base)) {
+            p[0] = PGX_BSDF_MIRROR;
+            t = m->albedo;
+        } else if (auto* m = dynamic_cast<ConductorBSDF*>(base)) {
+            p[0] = PGX_BSDF_CONDUCTOR;
+            t = m->albedo;
+            p[7] = m->alpha;
+            p[9] = m->eta.r, p[10] = m->eta.g, p[11] = m->eta.b;
+            p[12] = m->k.r, p[13] = m->k.g, p[14] = m->k.b;
+        } else if (auto* m = dynamic_cast<GlassBSDF*>(base)) {
+            p[0] = PGX_BSDF_GLASS;
+            t = m->albedo;
+            p[5] = m->intIOR, p[6] = m->extIOR;
+        } else if (auto* m = dynamic_cast<DielectricBSDF*>(base)) {
+            p[0] = PGX_BSDF_DIELECTRIC;
+            t = m->albedo;
+            p[5] = m->intIOR, p[6] = m->extIOR, p[7] = m->alpha;
+        } else if (auto* m = dynamic_cast<OrenNayarBSDF*>(base)) {
+            p[0] = PGX_BSDF_ORENNAYAR;
+            t = m->albedo;
+            p[8] = m->sigma;
+        } else if (auto* m = dynamic_cast<PlasticBSDF*>(base)) {
+            p[0] = PGX_BSDF_PLASTIC;
+            t = m->albedo;
+            p[5] = m->intIOR, p[6] = m->extIOR, p[7] = m->alpha;
+        }
+        p[15] = (float)(std::find(rl->textures.begin(), rl->textures.end(), t) - rl->textures.begin());
+    }
+}
+
+// Size of texture i (i = -1: the environment map; 0 x 0 when there is none).
+void orcref_loaded_texture_size(void* h, int32_t i, int32_t* wh) {
+    RefLoaded* rl = static_cast<RefLoaded*>(h);
+    Texture* t = nullptr;
+    if (i < 0) {
+        if (auto* e = dynamic_cast<EnvironmentMap*>(rl->scene->background)) t = e->env;
+    } else {
+        t = rl->textures[(size_t)i];
+    }
+    wh[0] = t ? t->width : 0;
+    wh[1] = t ? t->height : 0;
+}
+
+void orcref_loaded_texture(void* h, int32_t i, float* rgb) {
+    RefLoaded* rl = static_cast<RefLoaded*>(h);
+    Texture* t = i < 0 ? dynamic_cast<EnvironmentMap*>(rl->scene->background)->env : rl->textures[(size_t)i];
+    for (size_t k = 0; k < (size_t)t->width * t->height; k++) {
+        rgb[3 * k] = t->texels[k].r;
+        rgb[3 * k + 1] = t->texels[k].g;
+        rgb[3 * k + 2] = t->texels[k].b;
+    }
+}
+
+// Texture::load (Imaging.h:44-79) of one file; the texture is kept until
+// orcref_texture_free.  wh gets width, height.
+void* orcref_texture_load(const char* filename, int32_t* wh) {
+    Texture* t = new Texture();
+    t->load(filename);
+    wh[0] = t->width;
+    wh[1] = t->height;
+    return t;
+}
+
+void orcref_texture_read(void* h, float* rgb) {
+    Texture* t = static_cast<Texture*>(h);
+    for (size_t k = 0; k < (size_t)t->width * t->height; k++) {
+        rgb[3 * k] = t->texels[k].r;
+        rgb[3 * k + 1] = t->texels[k].g;
+        rgb[3 * k + 2] = t->texels[k].b;
+    }
+    delete t;
+}
+
+// Camera matrices: projection (16), camera-to-world (16).
+void orcref_loaded_camera(void* h, float* out32) {
+    RefLoaded* rl = static_cast<RefLoaded*>(h);
+    memcpy(out32, rl->scene->camera.projectionMatrix.m, 16 * sizeof(float));
+    memcpy(out32 + 16, rl->scene->camera.camera.m, 16 * sizeof(float));
 }
 
 void orcref_rng_floats(uint64_t seed, uint64_t pixel, uint64_t sample, int32_t count, float* out) {

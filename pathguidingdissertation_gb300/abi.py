@@ -65,6 +65,7 @@ class BvhStats(C.Structure):
 
 
 RENDER_PROFILE = 1
+RENDER_FILTER_MITCHELL = 2
 
 
 class RenderConfig(C.Structure):
@@ -115,6 +116,7 @@ SIGNATURES = {
     "pgx_get_spp": (C.c_int, [_P, C.POINTER(_I32)]),
     "pgx_film_read": (C.c_int, [_P, _P, _P, C.POINTER(_I32)]),
     "pgx_render_get_stats": (C.c_int, [_P, C.POINTER(RenderStats)]),
+    "pgx_film_tonemap": (C.c_int, [_P, C.c_float, C.c_float, _P]),
     "pgx_bsdf_sample_batch": (C.c_int, [_P, _P, _P, _P, _P, _I64, _P, _P, _P]),
     "pgx_bsdf_invert_batch": (C.c_int, [_P, _P, _P, _P, _P, _I64, _P]),
     "pgx_cache_build": (C.c_int, [_P, _P, _I64]),

@@ -127,9 +127,10 @@ class Context:
         self.check(self.lib.pgx_set_camera(self.h, C.byref(camera_struct(camera))))
 
     def render(self, frames: int = 1, mode: int = abi.MODE_PLAIN, seed: int = 1, max_depth: int = 8,
-               guide_fraction: float = 0.5, record_paths: int | bool = 0, profile: bool = False) -> None:
-        cfg = abi.RenderConfig(mode, max_depth, seed, guide_fraction, int(record_paths),
-                               abi.RENDER_PROFILE if profile else 0)
+               guide_fraction: float = 0.5, record_paths: int | bool = 0, profile: bool = False,
+               mitchell: bool = False) -> None:
+        flags = (abi.RENDER_PROFILE if profile else 0) | (abi.RENDER_FILTER_MITCHELL if mitchell else 0)
+        cfg = abi.RenderConfig(mode, max_depth, seed, guide_fraction, int(record_paths), flags)
         self.check(self.lib.pgx_render(self.h, C.byref(cfg), frames))
 
     def clear(self) -> None:
@@ -147,6 +148,13 @@ class Context:
         s = C.c_int32()
         self.check(self.lib.pgx_film_read(self.h, ptr(rgb), ptr(rgb2), C.byref(s)))
         return rgb, rgb2, s.value
+
+    def tonemap(self, exposure: float = 1.0, lmax_white: float = 10.0) -> np.ndarray:
+        """Film::tonemap of every pixel: (H, W, 3) uint8."""
+        w, h = self.scene.camera["width"], self.scene.camera["height"]
+        out = np.zeros((h, w, 3), np.uint8)
+        self.check(self.lib.pgx_film_tonemap(self.h, exposure, lmax_white, ptr(out)))
+        return out
 
     def render_stats(self) -> abi.RenderStats:
         s = abi.RenderStats()
@@ -282,6 +290,10 @@ class RayTracer:
     def getSPP(self) -> int:  # noqa: N802 - reference name
         return self.scene.ctx.spp()
 
+    def savePNG(self, filename: str) -> None:  # noqa: N802 - reference name
+        """RayTracer::savePNG (Renderer.h:751): the tonemapped film as PNG."""
+        write_png(filename, self.scene.ctx.tonemap())
+
     def saveHDR(self, filename: str) -> None:  # noqa: N802 - reference name
         """Film::save (Imaging.h:263-272): film / SPP as Radiance HDR."""
         rgb, _, spp = self.scene.ctx.film()
@@ -290,7 +302,9 @@ class RayTracer:
 
 
 def write_hdr(filename: str, img: np.ndarray) -> None:
-    """Minimal Radiance RGBE writer (uncompressed scanlines)."""
+    """Radiance RGBE writer.  Scanlines 8..32767 pixels wide are written in
+    the run-length layout (one literal run per 128 bytes of each channel),
+    which no reader can mistake for a flat scanline; other widths flat."""
     h, w, _ = img.shape
     rgb = np.asarray(img, np.float64)
     mx = rgb.max(axis=2)
@@ -305,4 +319,32 @@ def write_hdr(filename: str, img: np.ndarray) -> None:
     with open(filename, "wb") as f:
         f.write(b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n")
         f.write(f"-Y {h} +X {w}\n".encode())
-        f.write(out.tobytes())
+        if not 8 <= w < 32768:
+            f.write(out.tobytes())
+            return
+        head = bytes([2, 2, w >> 8, w & 255])
+        runs = [(x, min(128, w - x)) for x in range(0, w, 128)]
+        for y in range(h):
+            parts = [head]
+            for c in range(4):
+                row = out[y, :, c].tobytes()
+                for x, n in runs:
+                    parts.append(bytes([n]) + row[x:x + n])
+            f.write(b"".join(parts))
+
+
+def write_png(filename: str, rgb8: np.ndarray) -> None:
+    """8-bit RGB PNG (filter 0 on every row, zlib stream)."""
+    import struct
+    import zlib
+    h, w, _ = rgb8.shape
+    raw = b"".join(b"\x00" + np.ascontiguousarray(rgb8[y]).tobytes() for y in range(h))
+
+    def chunk(tag: bytes, data: bytes) -> bytes:
+        return struct.pack(">I", len(data)) + tag + data + struct.pack(">I", zlib.crc32(tag + data) & 0xFFFFFFFF)
+
+    with open(filename, "wb") as f:
+        f.write(b"\x89PNG\r\n\x1a\n")
+        f.write(chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 2, 0, 0, 0)))
+        f.write(chunk(b"IDAT", zlib.compress(raw, 6)))
+        f.write(chunk(b"IEND", b""))

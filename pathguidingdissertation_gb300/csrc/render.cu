@@ -111,6 +111,7 @@ struct FrameParams {
     int collect_hi;
     float guide_fraction;
     int profile;     // count node/triangle fetches
+    int mitchell;    // Mitchell-Netravali splat instead of the box filter
 };
 
 // ---- camera rays (Camera::generateRay, Scene.h:253-265; jitter Renderer.h:679-681)
@@ -534,19 +535,39 @@ __global__ void __launch_bounds__(kThreads, 8) k_shade(SceneView sv, PathState p
     }
 }
 
-// Film::splat with the box filter (Imaging.h:186-217).
-__device__ __forceinline__ void splat(float* film, float* film2, int W, int H, float x, float y, F3 c) {
+// MitchellNetravaliFilter::separable with B = C = 1/3 (Imaging.h:160-175).
+__device__ __forceinline__ float mitchell_1d(float val) {
+    const float B = 1.f / 3.f, C = 1.f / 3.f;
+    float x = fabsf(val);
+    float x2 = x * x;
+    float x3 = x * x * x;
+    if (x < 1.f)
+        return (1.f / 6.f) * ((12.f - 9.f * B - 6.f * C) * x3 + (-18.f + 12.f * B + 6.f * C) * x2 + (6.f - 2.f * B));
+    if (x < 2.f)
+        return (1.f / 6.f) * ((-B - 6.f * C) * x3 + (6.f * B + 30.f * C) * x2 + (-12.f * B - 48.f * C) * x +
+                              (8.f * B + 24.f * C));
+    return 0.f;
+}
+
+// Film::splat (Imaging.h:186-217) with the box filter (radius 1) or the
+// Mitchell-Netravali filter (radius 2): weights of the in-image pixels around
+// round(x, y), normalised by their sum.
+template <int R>
+__device__ __forceinline__ void splat_r(float* film, float* film2, int W, int H, float x, float y, F3 c) {
+    constexpr int K = (2 * R + 1) * (2 * R + 1);
     int bx = (int)floorf(x + 0.5f), by = (int)floorf(y + 0.5f);
-    int idx[9];
-    float wts[9];
+    int idx[K];
+    float wts[K];
     int used = 0;
     float total = 0.f;
-    for (int i = -1; i <= 1; i++)
-        for (int j = -1; j <= 1; j++) {
+    for (int i = -R; i <= R; i++)
+        for (int j = -R; j <= R; j++) {
             int px = bx + j, py = by + i;
             if (px >= 0 && px < W && py >= 0 && py < H) {
                 idx[used] = py * W + px;
-                wts[used] = (fabsf((float)px - x) < 0.5f && fabsf((float)py - y) < 0.5f) ? 1.f : 0.f;
+                float dx = (float)px - x, dy = (float)py - y;
+                wts[used] = (R == 1) ? ((fabsf(dx) < 0.5f && fabsf(dy) < 0.5f) ? 1.f : 0.f)
+                                     : mitchell_1d(dx) * mitchell_1d(dy);
                 total += wts[used];
                 used++;
             }
@@ -565,6 +586,37 @@ __device__ __forceinline__ void splat(float* film, float* film2, int W, int H, f
             }
         }
     }
+}
+
+__device__ __forceinline__ void splat(float* film, float* film2, int W, int H, float x, float y, F3 c, bool mitchell) {
+    if (mitchell)
+        splat_r<2>(film, film2, W, H, x, y, c);
+    else
+        splat_r<1>(film, film2, W, H, x, y, c);
+}
+
+// Film::tonemap (Imaging.h:220-244) for every pixel.
+__global__ void k_tonemap(const float* __restrict__ film, int64_t npix, int spp, float exposure, float lmax_white,
+                          uint8_t* __restrict__ out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npix) return;
+    float inv_spp = (spp > 0) ? 1.f / (float)spp : 1.f;
+    F3 col = (f3(film[3 * i], film[3 * i + 1], film[3 * i + 2]) * inv_spp) * exposure;
+    float lin = lum(col);
+    uint8_t r = 0, g = 0, b = 0;
+    if (!(lin < 1e-4f)) {
+        float lw2 = lmax_white * lmax_white;
+        float lout = lin * (1.f + (lin / lw2)) / (1.f + lin);
+        float coef = lout / lin;
+        float ge = 1.f / 2.2f;
+        float cr = powf(col.x * coef, ge), cg = powf(col.y * coef, ge), cb = powf(col.z * coef, ge);
+        r = (uint8_t)(s_max(0.f, s_min(cr, 1.f)) * 255.f);
+        g = (uint8_t)(s_max(0.f, s_min(cg, 1.f)) * 255.f);
+        b = (uint8_t)(s_max(0.f, s_min(cb, 1.f)) * 255.f);
+    }
+    out[3 * i] = r;
+    out[3 * i + 1] = g;
+    out[3 * i + 2] = b;
 }
 
 // End of frame: guided-Li back-propagation (Renderer.h:376-393), NaN/Inf
@@ -644,7 +696,7 @@ __global__ void __launch_bounds__(kThreads) k_finalize(SceneView sv, PathState p
         }
         if (!valid(col)) continue;
         float2 xy = ps.pix[p];
-        splat(film, film2, sv.width, sv.height, xy.x, xy.y, col);
+        splat(film, film2, sv.width, sv.height, xy.x, xy.y, col, fp.mitchell != 0);
     }
 }
 
@@ -920,6 +972,7 @@ extern "C" int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t fr
         fp.collect_hi = collect_hi;
         fp.guide_fraction = cfg->guide_fraction;
         fp.profile = prof ? 1 : 0;
+        fp.mitchell = (cfg->flags & PGX_RENDER_FILTER_MITCHELL) ? 1 : 0;
         launches += enqueue_frame(ctx, rs, fp, s);
         batches++;
         PGX_CUDA_TRY(ctx, cudaGetLastError());
@@ -1002,6 +1055,23 @@ extern "C" int pgx_film_read(pgx_ctx* ctx, float* rgb, float* rgb2, int32_t* spp
     if (rgb2) PGX_CUDA_TRY(ctx, cudaMemcpyAsync(rgb2, ctx->film2.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
     PGX_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     if (spp) *spp = ctx->spp;
+    return PGX_OK;
+}
+
+extern "C" int pgx_film_tonemap(pgx_ctx* ctx, float exposure, float lmax_white, uint8_t* rgb8) {
+    if (!ctx) return PGX_ERR_INVALID_ARG;
+    ctx->err.clear();
+    if (!rgb8) return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_film_tonemap: null output");
+    if (!ctx->has_scene) return pgx_fail(ctx, PGX_ERR_STATE, "pgx_film_tonemap: no scene");
+    PGX_TRY(ensure_film(ctx));
+    const int64_t npix = (int64_t)ctx->width * ctx->height;
+    DevBuf out;
+    PGX_CUDA_TRY(ctx, out.reserve((size_t)npix * 3));
+    k_tonemap<<<(unsigned)((npix + 255) / 256), 256, 0, ctx->stream>>>(ctx->film.as<float>(), npix, ctx->spp, exposure,
+                                                                       lmax_white, out.as<uint8_t>());
+    PGX_CUDA_TRY(ctx, cudaGetLastError());
+    PGX_CUDA_TRY(ctx, cudaMemcpyAsync(rgb8, out.p, (size_t)npix * 3, cudaMemcpyDeviceToHost, ctx->stream));
+    PGX_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     return PGX_OK;
 }
 

@@ -134,3 +134,49 @@ def test_render_matches_golden(ctx, oracle, path, mode):
     ctx.render(int(g["spp"]), mode=mode, seed=int(g["seed"]), max_depth=8)
     film, _, _ = ctx.film()
     _compare(film, g["plain"] if mode == abi.MODE_PLAIN else g["guided"])
+
+
+def test_mitchell_filter_vs_reference(ctx, reference):
+    desc = scenes.cornell_box(seed=1, width=40, height=32)
+    ctx.upload(desc)
+    nodes, idx = reference.bvh_build(desc.triangles)
+    ctx.bvh_import(nodes, idx)
+    ctx.clear()
+    ctx.render(4, mode=abi.MODE_PLAIN, seed=21, max_depth=8, mitchell=True)
+    film, _, _ = ctx.film()
+    reference.set_filter(True)
+    try:
+        ref_film, _, _ = reference.scene(desc).render_pcg(False, 21, 0, 4, threads=4)
+    finally:
+        reference.set_filter(False)
+    _compare(film, ref_film)
+
+
+def test_tonemap_matches_reference(ctx, reference):
+    desc = scenes.cornell_box(seed=1, width=48, height=40)
+    ctx.upload(desc)
+    ctx.bvh_build()
+    ctx.clear()
+    ctx.render(8, mode=abi.MODE_PLAIN, seed=2, max_depth=8)
+    film, _, spp = ctx.film()
+    for exposure, white in ((1.0, 10.0), (4.0, 2.0)):
+        got = ctx.tonemap(exposure, white)
+        ref = reference.tonemap(film, spp, exposure, white)
+        diff = np.abs(got.astype(int) - ref.astype(int))
+        assert diff.max() <= 1 and np.mean(diff > 0) < 0.01
+
+
+def test_save_png_and_hdr(ctx, tmp_path):
+    from pathguidingdissertation_gb300.api import RayTracer, Scene
+    scene = Scene(ctx)
+    scene.init(scenes.cornell_box(seed=1, width=24, height=24))
+    scene.build()
+    rt = RayTracer()
+    rt.init(scene)
+    rt.render()
+    rt.render()
+    assert rt.getSPP() == 2
+    rt.savePNG(str(tmp_path / "a.png"))
+    rt.saveHDR(str(tmp_path / "a.hdr"))
+    assert (tmp_path / "a.png").read_bytes()[:8] == b"\x89PNG\r\n\x1a\n"
+    assert (tmp_path / "a.hdr").stat().st_size > 24 * 24 * 4

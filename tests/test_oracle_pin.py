@@ -124,3 +124,15 @@ def test_reference_reproduces_bsdf_fixture(reference):
         wi, f, pdf, uv_out = reference.bsdf_roundtrip(g[f"{case}__material"], g[f"{case}__n"], g[f"{case}__wo"],
                                                       g[f"{case}__uv"])
         assert np.array_equal(wi, g[f"{case}__wi"]) and np.array_equal(uv_out, g[f"{case}__uv_out"]), case
+
+
+def test_metrics_match_reference(reference):
+    """pathguidingdissertation_gb300.metrics against Metrics.h."""
+    from pathguidingdissertation_gb300 import metrics
+    rng = np.random.default_rng(4)
+    gt = rng.random((24, 32, 3)).astype(np.float32)
+    test = (gt + rng.normal(0, 0.05, gt.shape)).astype(np.float32)
+    m, r, rr = reference.metrics(test, gt)
+    assert metrics.mse(test, gt) == pytest.approx(m, rel=1e-4)
+    assert metrics.rmse(test, gt) == pytest.approx(r, rel=1e-4)
+    assert metrics.rrmse(test, gt) == pytest.approx(rr, rel=1e-4)
