@@ -165,7 +165,12 @@ enum pgx_render_mode {
     /* Extension: plain estimator whose continuation directions are drawn
      * by one-sample MIS between the BSDF and the radiance-cache QuadTree
      * guide (the design sketched in Renderer.h:398-414). */
-    PGX_MODE_GUIDED_QUADTREE = 2
+    PGX_MODE_GUIDED_QUADTREE = 2,
+    /* Extension: the same estimator with the learned guide (pgx_mlp_*): at
+     * every non-specular vertex the network's vMF mixture for (position,
+     * shading normal, wo) is evaluated on the tensor cores and mixed with
+     * the BSDF by one-sample MIS; needs pgx_mlp_init. */
+    PGX_MODE_GUIDED_MLP = 3
 };
 
 typedef struct pgx_render_config {
@@ -188,6 +193,9 @@ typedef struct pgx_render_config {
  * (MitchellNetravaliFilter, Imaging.h:153-176) instead of the box filter
  * RayTracer::init installs (Renderer.h:255). */
 #define PGX_RENDER_FILTER_MITCHELL 2
+/* PGX_MODE_GUIDED_MLP: after every frame, one Adam step of the learned guide
+ * on the radiance samples that frame's paths produced (pgx_mlp_configure). */
+#define PGX_RENDER_TRAIN_GUIDE 4
 
 /* Statistics of the last pgx_render call.  The per-stage times and the
  * node/triangle fetch counts are filled only with PGX_RENDER_PROFILE. */
@@ -376,6 +384,56 @@ int pgx_cache_knn(pgx_ctx* ctx, const float* queries, int64_t nq, int32_t k,
  * uniform share.  positions, dirs: n*3 floats. */
 int pgx_guide_pdf(pgx_ctx* ctx, const float* positions, const float* dirs, int64_t n, float* pdf);
 int pgx_guide_sample(pgx_ctx* ctx, const float* positions, const float* u2, int64_t n, float* dirs, float* pdf);
+
+/* ---- learned guide (extension; the reference has no learned component) ----
+ * A 6-layer MLP (inputs: position encoded with 12 sin/cos frequencies per
+ * axis after normalising to the scene bounds, shading normal, wo — 78
+ * values padded to 80; 5 hidden layers of 64 with ReLU; 40 outputs) with
+ * BF16 weights and activations and FP32 accumulation on the tensor cores.
+ * Outputs: 8 lobe logits (softmax weights), 8 unnormalised mean directions
+ * (3 each), 8 concentrations kappa = softplus(r) + 0.01; the guide is the
+ * mixture of the 8 von Mises-Fisher lobes.
+ *
+ * Parameters (FP32 master copy, PGX_MLP_PARAMS floats) are, per layer l,
+ * W_l[n][k] row-major followed by b_l[n], with (k, n) = (80, 64), (64, 64)
+ * x 4, (64, 40).  Queries are 9 floats each: position, normal, wo. */
+#define PGX_MLP_PARAMS 24424
+#define PGX_MLP_OUTPUTS 40
+
+/* One training sample: the direction wi continued from (position, normal,
+ * wo) and its weight, e.g. Lum(incident radiance along wi) / pdf(wi). */
+typedef struct pgx_radiance_sample {
+    float position[3];
+    float normal[3];
+    float wo[3];
+    float wi[3];
+    float weight;
+} pgx_radiance_sample;
+
+/* Creates (or re-initialises) the network with He-uniform weights from
+ * `seed`; positions are normalised to [bmin, bmax] (both NULL: the uploaded
+ * scene's bounds).  Resets the optimiser. */
+int pgx_mlp_init(pgx_ctx* ctx, uint64_t seed, const float* bmin, const float* bmax);
+int pgx_mlp_get_params(pgx_ctx* ctx, float* params);
+/* Replaces the parameters and resets the optimiser moments. */
+int pgx_mlp_set_params(pgx_ctx* ctx, const float* params);
+/* Raw outputs (n x 40) of n queries. */
+int pgx_mlp_forward(pgx_ctx* ctx, const float* queries, int64_t n, float* raw);
+/* Mixture pdf (solid angle) of dirs[i] for query i. */
+int pgx_mlp_pdf(pgx_ctx* ctx, const float* queries, const float* dirs, int64_t n, float* pdf);
+/* Samples the mixture with three uniforms per query (lobe, cos, azimuth);
+ * dirs: n x 3, pdf: n. */
+int pgx_mlp_sample(pgx_ctx* ctx, const float* queries, const float* u3, int64_t n, float* dirs, float* pdf);
+/* Gradient of the loss sum_i w_i (-log q(wi_i | query_i)) / sum_i w_i with
+ * respect to the parameters (PGX_MLP_PARAMS floats), without an update. */
+int pgx_mlp_gradient(pgx_ctx* ctx, const pgx_radiance_sample* samples, int64_t n, float* grad, double* loss);
+/* One Adam step (beta1 0.9, beta2 0.99, eps 1e-8) with learning rate lr on
+ * the same loss; loss (may be NULL) gets its value before the step. */
+int pgx_mlp_train_step(pgx_ctx* ctx, const pgx_radiance_sample* samples, int64_t n, float lr, double* loss);
+/* Online training inside pgx_render (PGX_RENDER_TRAIN_GUIDE): learning rate
+ * lr * decay^step and at most `batch` samples per step (default 1e-2,
+ * 0.998, 262144). */
+int pgx_mlp_configure(pgx_ctx* ctx, float lr, float decay, int64_t batch);
 
 #ifdef __cplusplus
 }

@@ -25,10 +25,17 @@ PGX_ERR_TIMEOUT = 5
 PGX_ERR_STATE = 6
 NOALLOC_MAX_RAYS = 65536  # PGX_NOALLOC_MAX_RAYS
 
+MLP_PARAMS = 24424   # PGX_MLP_PARAMS
+MLP_OUTPUTS = 40     # PGX_MLP_OUTPUTS
+RENDER_TRAIN_GUIDE = 4
+# pgx_radiance_sample: position, normal, wo, wi, weight
+RADIANCE_SAMPLE = np.dtype([("position", "<f4", 3), ("normal", "<f4", 3), ("wo", "<f4", 3), ("wi", "<f4", 3),
+                            ("weight", "<f4")])
+
 # BSDF kinds
 BSDF_DIFFUSE, BSDF_MIRROR, BSDF_CONDUCTOR, BSDF_GLASS, BSDF_DIELECTRIC, BSDF_ORENNAYAR, BSDF_PLASTIC = range(7)
 # render modes
-MODE_PLAIN, MODE_GUIDED_LI, MODE_GUIDED_QUADTREE = 0, 1, 2
+MODE_PLAIN, MODE_GUIDED_LI, MODE_GUIDED_QUADTREE, MODE_GUIDED_MLP = 0, 1, 2, 3
 
 # ---- numpy layouts of the C structs ---------------------------------------------
 VERTEX = np.dtype([("p", "<f4", 3), ("n", "<f4", 3), ("u", "<f4"), ("v", "<f4")])
@@ -126,6 +133,15 @@ SIGNATURES = {
     "pgx_cache_knn": (C.c_int, [_P, _P, _I64, _I32, _P, _P]),
     "pgx_guide_pdf": (C.c_int, [_P, _P, _P, _I64, _P]),
     "pgx_guide_sample": (C.c_int, [_P, _P, _P, _I64, _P, _P]),
+    "pgx_mlp_init": (C.c_int, [_P, C.c_uint64, _P, _P]),
+    "pgx_mlp_get_params": (C.c_int, [_P, _P]),
+    "pgx_mlp_set_params": (C.c_int, [_P, _P]),
+    "pgx_mlp_forward": (C.c_int, [_P, _P, _I64, _P]),
+    "pgx_mlp_pdf": (C.c_int, [_P, _P, _P, _I64, _P]),
+    "pgx_mlp_sample": (C.c_int, [_P, _P, _P, _I64, _P, _P]),
+    "pgx_mlp_gradient": (C.c_int, [_P, _P, _I64, _P, C.POINTER(C.c_double)]),
+    "pgx_mlp_train_step": (C.c_int, [_P, _P, _I64, C.c_float, C.POINTER(C.c_double)]),
+    "pgx_mlp_configure": (C.c_int, [_P, C.c_float, C.c_float, _I64]),
 }
 
 _lib: C.CDLL | None = None

@@ -220,6 +220,63 @@ class Context:
         self.check(self.lib.pgx_guide_sample(self.h, ptr(p), ptr(u), len(p), ptr(dirs), ptr(pdf)))
         return dirs, pdf
 
+    # ---- learned guide ----
+    def mlp_init(self, seed: int = 1, bmin=None, bmax=None) -> None:
+        lo = None if bmin is None else np.ascontiguousarray(bmin, np.float32)
+        hi = None if bmax is None else np.ascontiguousarray(bmax, np.float32)
+        self.check(self.lib.pgx_mlp_init(self.h, seed, ptr(lo), ptr(hi)))
+
+    def mlp_params(self) -> np.ndarray:
+        out = np.zeros(abi.MLP_PARAMS, np.float32)
+        self.check(self.lib.pgx_mlp_get_params(self.h, ptr(out)))
+        return out
+
+    def mlp_set_params(self, params: np.ndarray) -> None:
+        p = np.ascontiguousarray(params, np.float32)
+        assert p.size == abi.MLP_PARAMS
+        self.check(self.lib.pgx_mlp_set_params(self.h, ptr(p)))
+
+    @staticmethod
+    def _queries(queries) -> np.ndarray:
+        return np.ascontiguousarray(queries, np.float32).reshape(-1, 9)
+
+    def mlp_forward(self, queries: np.ndarray) -> np.ndarray:
+        q = self._queries(queries)
+        out = np.zeros((len(q), abi.MLP_OUTPUTS), np.float32)
+        self.check(self.lib.pgx_mlp_forward(self.h, ptr(q), len(q), ptr(out)))
+        return out
+
+    def mlp_pdf(self, queries: np.ndarray, dirs: np.ndarray) -> np.ndarray:
+        q = self._queries(queries)
+        d = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+        out = np.zeros(len(q), np.float32)
+        self.check(self.lib.pgx_mlp_pdf(self.h, ptr(q), ptr(d), len(q), ptr(out)))
+        return out
+
+    def mlp_sample(self, queries: np.ndarray, u3: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+        q = self._queries(queries)
+        u = np.ascontiguousarray(u3, np.float32).reshape(-1, 3)
+        dirs = np.zeros((len(q), 3), np.float32)
+        pdf = np.zeros(len(q), np.float32)
+        self.check(self.lib.pgx_mlp_sample(self.h, ptr(q), ptr(u), len(q), ptr(dirs), ptr(pdf)))
+        return dirs, pdf
+
+    def mlp_gradient(self, samples: np.ndarray) -> tuple[np.ndarray, float]:
+        s = np.ascontiguousarray(samples, abi.RADIANCE_SAMPLE)
+        g = np.zeros(abi.MLP_PARAMS, np.float32)
+        loss = C.c_double(0.0)
+        self.check(self.lib.pgx_mlp_gradient(self.h, ptr(s), len(s), ptr(g), C.byref(loss)))
+        return g, loss.value
+
+    def mlp_train_step(self, samples: np.ndarray, lr: float = 1e-2) -> float:
+        s = np.ascontiguousarray(samples, abi.RADIANCE_SAMPLE)
+        loss = C.c_double(0.0)
+        self.check(self.lib.pgx_mlp_train_step(self.h, ptr(s), len(s), lr, C.byref(loss)))
+        return loss.value
+
+    def mlp_configure(self, lr: float = 1e-2, decay: float = 0.998, batch: int = 262144) -> None:
+        self.check(self.lib.pgx_mlp_configure(self.h, lr, decay, batch))
+
     def cache_knn(self, queries: np.ndarray, k: int) -> tuple[np.ndarray, np.ndarray]:
         q = np.ascontiguousarray(queries, np.float32).reshape(-1, 3)
         idx = np.zeros((len(q), k), np.int32)

@@ -63,6 +63,7 @@ extern "C" int pgx_destroy(pgx_ctx* ctx) {
     cudaStreamSynchronize(ctx->stream);
     render_state_free(ctx);
     cache_state_free(ctx);
+    mlp_state_free(ctx);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
     return PGX_OK;

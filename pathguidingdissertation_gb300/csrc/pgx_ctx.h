@@ -159,6 +159,7 @@ struct pgx_ctx {
     pgx_render_stats rstats{};
     void* render_state = nullptr;  // owned by render.cu
     void* cache_state = nullptr;   // owned by cache.cu
+    void* mlp_state = nullptr;     // owned by mlp.cu
 
     pgx_ctx() = default;
     pgx_ctx(const pgx_ctx&) = delete;
@@ -187,3 +188,4 @@ int bvh_layout_from_ref(pgx_ctx* ctx, const int32_t* node_rec_host);
 BvhView bvh_view(const pgx_ctx* ctx);
 void render_state_free(pgx_ctx* ctx);
 void cache_state_free(pgx_ctx* ctx);
+void mlp_state_free(pgx_ctx* ctx);

@@ -1,0 +1,154 @@
+"""The learned guide on the GPU: tensor-core forward and backward against
+the CPU restatement (oracle/mlp_oracle.py), the mixture's pdf and sampler,
+and training on radiance samples."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle import mlp_oracle as mo
+from pathguidingdissertation_gb300 import abi
+
+pytestmark = pytest.mark.gpu
+
+BMIN, BMAX = np.array([-1.0, 0.0, -2.0], np.float32), np.array([3.0, 2.0, 1.0], np.float32)
+
+
+def _unit(rng, n):
+    v = rng.standard_normal((n, 3))
+    return (v / np.linalg.norm(v, axis=1, keepdims=True)).astype(np.float32)
+
+
+def _queries(rng, n):
+    return np.concatenate([rng.uniform(BMIN, BMAX, (n, 3)).astype(np.float32), _unit(rng, n), _unit(rng, n)], 1)
+
+
+def _samples(rng, n):
+    s = np.zeros(n, abi.RADIANCE_SAMPLE)
+    q = _queries(rng, n)
+    s["position"], s["normal"], s["wo"] = q[:, 0:3], q[:, 3:6], q[:, 6:9]
+    s["wi"] = _unit(rng, n)
+    s["weight"] = rng.uniform(0.1, 2.0, n)
+    return s
+
+
+@pytest.fixture()
+def net(ctx):
+    ctx.mlp_init(1, BMIN, BMAX)
+    params = mo.init_params(2)
+    ctx.mlp_set_params(params)
+    return ctx, params
+
+
+def test_params_round_trip(net):
+    ctx, params = net
+    assert np.array_equal(ctx.mlp_params(), params)
+
+
+def test_forward_matches_oracle(net):
+    ctx, params = net
+    rng = np.random.default_rng(3)
+    q = _queries(rng, 1000)          # 7 full tiles and a partial one
+    gpu = ctx.mlp_forward(q).astype(np.float64)
+    cpu, _ = mo.forward(params, q, BMIN, BMAX)
+    # FP32 tensor-core sums vs float64 sums: the bf16 rounding of a hidden
+    # activation can land on different sides, so compare in norm
+    err = np.linalg.norm(gpu - cpu) / np.linalg.norm(cpu)
+    assert err < 5e-3, err
+    assert np.max(np.abs(gpu - cpu)) < 0.05 * np.abs(cpu).max()
+
+
+def test_gradient_matches_oracle(net):
+    ctx, params = net
+    rng = np.random.default_rng(4)
+    s = _samples(rng, 3000)
+    g_gpu, loss_gpu = ctx.mlp_gradient(s)
+    loss_cpu, g_cpu = mo.loss_and_grad(params, s, BMIN, BMAX)
+    assert abs(loss_gpu - loss_cpu) < 5e-3 * abs(loss_cpu)
+    err = np.linalg.norm(g_gpu - g_cpu) / np.linalg.norm(g_cpu)
+    assert err < 2e-2, err
+    # per layer, weights and biases separately
+    for (k, n), (ow, ob) in zip(mo.DIMS, mo.OFFSETS):
+        for a, b in ((ow, ob), (ob, ob + n)):
+            e = np.linalg.norm(g_gpu[a:b] - g_cpu[a:b]) / max(np.linalg.norm(g_cpu[a:b]), 1e-12)
+            assert e < 5e-2, (a, b, e)
+
+
+def _sphere_grid(n):
+    c = (np.arange(n) + 0.5) / n * 2.0 - 1.0
+    phi = (np.arange(n) + 0.5) / n * 2.0 * np.pi
+    cc, pp = np.meshgrid(c, phi, indexing="ij")
+    s = np.sqrt(1.0 - cc ** 2)
+    return np.stack([s * np.cos(pp), s * np.sin(pp), cc], -1).reshape(-1, 3).astype(np.float32), 4 * np.pi / n ** 2
+
+
+def test_pdf_is_normalised_and_matches_oracle(net):
+    ctx, params = net
+    rng = np.random.default_rng(5)
+    d, da = _sphere_grid(500)
+    for q in _queries(rng, 3):
+        qq = np.repeat(q[None], len(d), 0)
+        p = ctx.mlp_pdf(qq, d).astype(np.float64)
+        assert abs(p.sum() * da - 1.0) < 5e-3
+        raw = ctx.mlp_forward(q[None]).astype(np.float64)
+        ref = mo.mixture_pdf(np.repeat(raw, len(d), 0), d)
+        np.testing.assert_allclose(p, ref, rtol=2e-3, atol=1e-6)
+
+
+def test_sample_matches_pdf_and_oracle(net):
+    ctx, params = net
+    rng = np.random.default_rng(6)
+    n = 20000
+    q = np.repeat(_queries(rng, 1), n, 0)
+    u = rng.random((n, 3)).astype(np.float32)
+    d, pdf = ctx.mlp_sample(q, u)
+    np.testing.assert_allclose(np.linalg.norm(d, axis=1), 1.0, atol=1e-5)
+    np.testing.assert_allclose(pdf, ctx.mlp_pdf(q, d), rtol=1e-5)
+    raw = ctx.mlp_forward(q[:1]).astype(np.float64)
+    ref = mo.sample(np.repeat(raw, n, 0), u)
+    close = np.sum(d * ref, axis=1) > 1.0 - 1e-4
+    assert close.mean() > 0.999     # lobe picks at cdf boundaries may differ
+
+
+def test_training_learns_a_directional_field(ctx):
+    """Samples whose directions follow vMF(mu(x), 20) with mu pointing from a
+    light position: after training, the guide's log-likelihood of fresh
+    samples is far above that of the uniform density it starts near."""
+    ctx.mlp_init(7, BMIN, BMAX)
+    rng = np.random.default_rng(8)
+    light = np.array([1.0, 3.0, -0.5])
+
+    def batch(n):
+        s = _samples(rng, n)
+        mu = light - s["position"]
+        mu /= np.linalg.norm(mu, axis=1, keepdims=True)
+        raw = np.zeros((n, 40))
+        raw[:, 8:11] = mu
+        raw[:, 11:32] = np.tile(mu, 7)
+        raw[:, 32:40] = np.log(np.expm1(20.0))
+        s["wi"] = mo.sample(raw, rng.random((n, 3)))
+        s["weight"] = 1.0
+        return s
+
+    test = batch(20000)
+    q = np.concatenate([test["position"], test["normal"], test["wo"]], 1)
+    ll0 = np.mean(np.log(ctx.mlp_pdf(q, test["wi"])))
+    losses = [ctx.mlp_train_step(batch(1 << 14), lr=1e-2) for _ in range(300)]
+    ll1 = np.mean(np.log(ctx.mlp_pdf(q, test["wi"])))
+    assert np.all(np.isfinite(losses))
+    assert losses[-1] < losses[0] - 1.0
+    # uniform: log(1/4pi) = -2.53; the target's own mean log-density is
+    # log(20 / 2pi) - 20 (1 - coth 20 + 1/20) = +0.16
+    assert ll0 < -1.5 and ll1 > -1.0, (ll0, ll1)
+
+
+def test_api_errors(ctx, pgx_lib):
+    from pathguidingdissertation_gb300.abi import PgxError
+    with pytest.raises(PgxError):
+        ctx.mlp_forward(np.zeros((4, 9), np.float32))      # not initialised
+    ctx.mlp_init(1, BMIN, BMAX)
+    assert ctx.mlp_forward(np.zeros((0, 9), np.float32)).shape == (0, 40)
+    with pytest.raises(PgxError):
+        ctx.mlp_init(1, BMIN, BMIN)                        # empty bounds
+    with pytest.raises(PgxError):
+        ctx.mlp_configure(lr=-1.0)
