@@ -243,6 +243,15 @@ def relmse(img: np.ndarray, ref: np.ndarray, eps: float = 1e-2) -> float:
     return float(np.mean(d * d / (ref * ref + eps)))
 
 
+def relmse_robust(img: np.ndarray, ref: np.ndarray, eps: float = 1e-2, drop: float = 1e-3) -> float:
+    """relMSE with the largest 0.1 % of per-pixel errors left out (a few
+    fireflies from the sun lobe otherwise decide the mean)."""
+    d = img.astype(np.float64) - ref
+    e = np.sort((d * d / (ref * ref + eps)).mean(axis=2).ravel())
+    k = max(1, int(len(e) * drop))
+    return float(e[:-k].mean())
+
+
 def rrmse_reference_metric(img: np.ndarray, ref: np.ndarray) -> float:
     """Metrics::calculateRRMSE (Metrics.h:48-68): RMSE / (sqrt(sum ref^2) + 1e-2)."""
     d = img.astype(np.float64) - ref
@@ -250,8 +259,10 @@ def rrmse_reference_metric(img: np.ndarray, ref: np.ndarray) -> float:
 
 
 def run_relmse_study(args) -> dict:
-    """Equal-time relMSE of QuadTree-guided vs plain path tracing against a
-    converged plain render of the same view."""
+    """Equal-time relMSE of guided (learned or QuadTree) vs plain path tracing
+    against a converged plain render of the same view.  All times are device
+    times of pgx_render (and of the cache build); training frames are part of
+    the guided image and of its time."""
     from pathguidingdissertation_gb300 import abi
     from pathguidingdissertation_gb300 import build as pkg_build
     from pathguidingdissertation_gb300.api import Context
@@ -274,43 +285,58 @@ def run_relmse_study(args) -> dict:
             left -= n
         return ms
 
+    def image():
+        rgb, _, spp = ctx.film()
+        return rgb.astype(np.float64) / spp
+
     ctx.clear()
     ref_ms = render_ms(args.ref_spp, abi.MODE_PLAIN, 1000)
-    rgb, _, spp = ctx.film()
-    ref = rgb.astype(np.float64) / spp
+    ref = image()
+    metric = relmse_robust if args.metric == "robust" else relmse
 
     # Plain: its error at plain_spp and the time it takes.
     ctx.clear()
     plain_ms = render_ms(args.plain_spp, abi.MODE_PLAIN, 7)
-    rgb, _, spp = ctx.film()
-    plain_img = rgb / spp
-    plain_err = relmse(plain_img, ref)
+    plain_img = image()
+    plain_err = metric(plain_img, ref)
 
-    # Guided: train the cache over `train_iters` iterations of 1, 2, 4, ...
-    # frames (the first plain, the rest guided by the previous cache; every
-    # iteration's records rebuild the cache), all timed; then render guided
-    # frames until the plain error is reached.
+    ctx.clear()
     train_ms = 0.0
     train_spp = 0
-    for it in range(args.train_iters):
+    extra = {}
+    if args.guide == "mlp":
+        # Learned guide: online training on the first `train_frames` frames
+        # (one Adam step per frame, batch 2^18), which stay in the image.
+        ctx.mlp_init(3)
+        ctx.mlp_configure(lr=args.mlp_lr, decay=args.mlp_decay, batch=1 << 18, steps=args.mlp_steps)
+        mode = abi.MODE_GUIDED_MLP
+        train_ms = render_ms(args.train_frames, mode, 13, guide_fraction=args.guide_fraction, train_guide=True)
+        train_spp = args.train_frames
+        extra = {"train_frames": args.train_frames, "lr": args.mlp_lr, "lr_decay": args.mlp_decay,
+                 "adam_steps_per_frame": args.mlp_steps}
+    else:
+        # QuadTree: train the cache over `train_iters` iterations of 1, 2, 4,
+        # ... frames (the first plain, the rest guided by the previous cache;
+        # every iteration's records rebuild the cache), all timed.
+        mode = abi.MODE_GUIDED_QUADTREE
+        for it in range(args.train_iters):
+            ctx.clear()
+            n = 1 << it
+            m = abi.MODE_PLAIN if it == 0 else abi.MODE_GUIDED_QUADTREE
+            train_ms += render_ms(n, m, 11 + it, record_paths=n, guide_fraction=args.guide_fraction)
+            train_ms += ctx.cache_stats().build_ms
+            train_spp += n
+        extra = {"train_iters": args.train_iters, "cache_records": ctx.cache_stats().records}
         ctx.clear()
-        n = 1 << it
-        mode = abi.MODE_PLAIN if it == 0 else abi.MODE_GUIDED_QUADTREE
-        train_ms += render_ms(n, mode, 11 + it, record_paths=n, guide_fraction=args.guide_fraction)
-        train_ms += ctx.cache_stats().build_ms
-        train_spp += n
-    cst = ctx.cache_stats()
-    ctx.clear()
     guided_ms = 0.0
     curve = []
     reached_ms = None
     chunk = max(1, args.plain_spp // 32)
-    total = 0
+    total = train_spp if args.guide == "mlp" else 0
     while total < 4 * args.plain_spp:
-        guided_ms += render_ms(chunk, abi.MODE_GUIDED_QUADTREE, 13, guide_fraction=args.guide_fraction)
+        guided_ms += render_ms(chunk, mode, 17 + total, guide_fraction=args.guide_fraction)
         total += chunk
-        rgb, _, spp = ctx.film()
-        err = relmse(rgb / spp, ref)
+        err = metric(image(), ref)
         curve.append((total, train_ms + guided_ms, err))
         if reached_ms is None and err <= plain_err:
             reached_ms = train_ms + guided_ms
@@ -318,25 +344,26 @@ def run_relmse_study(args) -> dict:
             break
         if train_ms + guided_ms >= 4.0 * plain_ms:
             break
-    # Guided error at the plain render's wall time (linear in 1/time between points).
+    # Guided error at the plain render's wall time (linear between points).
     eq_err = None
     for (s0, t0, e0), (s1, t1, e1) in zip(curve, curve[1:]):
         if t0 <= plain_ms <= t1:
             eq_err = e0 + (e1 - e0) * (plain_ms - t0) / max(t1 - t0, 1e-9)
-    guided_img = rgb / spp
+    guided_img = image()
     ctx.close()
     return {
-        "study": "equal-time relMSE, QuadTree-guided vs plain GPU path tracing",
+        "study": f"equal-time relMSE, {args.guide}-guided vs plain GPU path tracing",
+        "metric": "relMSE (x-r)^2/(r^2+0.01)" + (", largest 0.1% pixel errors left out" if args.metric == "robust"
+                                                else ""),
         "workload": f"{args.workload} {w}x{h}, depth {depth}",
         "reference": {"spp": args.ref_spp, "ms": ref_ms},
         "plain": {"spp": args.plain_spp, "ms": plain_ms, "relmse": plain_err,
                   "rrmse_metrics_h": rrmse_reference_metric(plain_img, ref)},
-        "guided": {"train_spp": train_spp, "train_iters": args.train_iters, "cache_records": cst.records,
-                   "train_ms": train_ms,
-                   "guide_fraction": args.guide_fraction, "spp_rendered": total,
-                   "ms_to_plain_error": reached_ms, "relmse_at_plain_time": eq_err,
-                   "rrmse_metrics_h_final": rrmse_reference_metric(guided_img, ref),
-                   "curve": [{"spp": a, "ms": b, "relmse": c} for a, b, c in curve]},
+        "guided": dict(extra, guide=args.guide, train_spp=train_spp, train_ms=train_ms,
+                       guide_fraction=args.guide_fraction, spp_rendered=total,
+                       ms_to_plain_error=reached_ms, relmse_at_plain_time=eq_err,
+                       rrmse_metrics_h_final=rrmse_reference_metric(guided_img, ref),
+                       curve=[{"spp": a, "ms": b, "relmse": c} for a, b, c in curve]),
         "time_ratio_guided_over_plain": (reached_ms / plain_ms) if reached_ms else None,
     }
 
@@ -503,7 +530,13 @@ def main() -> None:
     ap.add_argument("--ref-spp", type=int, default=16384)
     ap.add_argument("--plain-spp", type=int, default=1024)
     ap.add_argument("--train-iters", type=int, default=6)
-    ap.add_argument("--guide-fraction", type=float, default=0.25)
+    ap.add_argument("--guide-fraction", type=float, default=0.5)
+    ap.add_argument("--guide", choices=["mlp", "quadtree"], default="mlp")
+    ap.add_argument("--metric", choices=["robust", "plain"], default="robust")
+    ap.add_argument("--train-frames", type=int, default=64)
+    ap.add_argument("--mlp-lr", type=float, default=5e-3)
+    ap.add_argument("--mlp-decay", type=float, default=0.998)
+    ap.add_argument("--mlp-steps", type=int, default=4)
     ap.add_argument("--trav-rays", type=int, default=10_000_000)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))

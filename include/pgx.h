@@ -430,10 +430,11 @@ int pgx_mlp_gradient(pgx_ctx* ctx, const pgx_radiance_sample* samples, int64_t n
 /* One Adam step (beta1 0.9, beta2 0.99, eps 1e-8) with learning rate lr on
  * the same loss; loss (may be NULL) gets its value before the step. */
 int pgx_mlp_train_step(pgx_ctx* ctx, const pgx_radiance_sample* samples, int64_t n, float lr, double* loss);
-/* Online training inside pgx_render (PGX_RENDER_TRAIN_GUIDE): learning rate
- * lr * decay^step and at most `batch` samples per step (default 1e-2,
- * 0.998, 262144). */
-int pgx_mlp_configure(pgx_ctx* ctx, float lr, float decay, int64_t batch);
+/* Online training inside pgx_render (PGX_RENDER_TRAIN_GUIDE): after every
+ * frame, `steps` Adam steps on disjoint batches of at most `batch` of that
+ * frame's radiance samples, learning rate lr * decay^step (defaults 5e-3,
+ * 0.998, 262144, 4). */
+int pgx_mlp_configure(pgx_ctx* ctx, float lr, float decay, int64_t batch, int32_t steps);
 
 #ifdef __cplusplus
 }

@@ -141,7 +141,7 @@ SIGNATURES = {
     "pgx_mlp_sample": (C.c_int, [_P, _P, _P, _I64, _P, _P]),
     "pgx_mlp_gradient": (C.c_int, [_P, _P, _I64, _P, C.POINTER(C.c_double)]),
     "pgx_mlp_train_step": (C.c_int, [_P, _P, _I64, C.c_float, C.POINTER(C.c_double)]),
-    "pgx_mlp_configure": (C.c_int, [_P, C.c_float, C.c_float, _I64]),
+    "pgx_mlp_configure": (C.c_int, [_P, C.c_float, C.c_float, _I64, _I32]),
 }
 
 _lib: C.CDLL | None = None

@@ -128,8 +128,9 @@ class Context:
 
     def render(self, frames: int = 1, mode: int = abi.MODE_PLAIN, seed: int = 1, max_depth: int = 8,
                guide_fraction: float = 0.5, record_paths: int | bool = 0, profile: bool = False,
-               mitchell: bool = False) -> None:
-        flags = (abi.RENDER_PROFILE if profile else 0) | (abi.RENDER_FILTER_MITCHELL if mitchell else 0)
+               mitchell: bool = False, train_guide: bool = False) -> None:
+        flags = (abi.RENDER_PROFILE if profile else 0) | (abi.RENDER_FILTER_MITCHELL if mitchell else 0) | \
+            (abi.RENDER_TRAIN_GUIDE if train_guide else 0)
         cfg = abi.RenderConfig(mode, max_depth, seed, guide_fraction, int(record_paths), flags)
         self.check(self.lib.pgx_render(self.h, C.byref(cfg), frames))
 
@@ -274,8 +275,8 @@ class Context:
         self.check(self.lib.pgx_mlp_train_step(self.h, ptr(s), len(s), lr, C.byref(loss)))
         return loss.value
 
-    def mlp_configure(self, lr: float = 1e-2, decay: float = 0.998, batch: int = 262144) -> None:
-        self.check(self.lib.pgx_mlp_configure(self.h, lr, decay, batch))
+    def mlp_configure(self, lr: float = 5e-3, decay: float = 0.998, batch: int = 262144, steps: int = 4) -> None:
+        self.check(self.lib.pgx_mlp_configure(self.h, lr, decay, batch, steps))
 
     def cache_knn(self, queries: np.ndarray, k: int) -> tuple[np.ndarray, np.ndarray]:
         q = np.ascontiguousarray(queries, np.float32).reshape(-1, 3)

@@ -40,8 +40,9 @@ struct MlpState {
     DevBuf loss;                   // double[2]: loss sum, weight sum
     DevBuf status;                 // int: MMA wait timeouts
     Bounds bounds{};
-    float lr = 1e-2f, decay = 0.998f;
+    float lr = 5e-3f, decay = 0.998f;
     int64_t batch = 262144;
+    int steps = 4;
     int64_t step = 0;
     bool valid = false;
     int sms = 0;
@@ -134,18 +135,19 @@ __global__ void __launch_bounds__(kThreads) k_query(const uint8_t* __restrict__ 
         if (mode == Q_RAW) {
             for (int j = 0; j < kOut; j++) out[r * kOut + j] = raw[j];
         } else {
-            Mixture m;
-            mixture_from_raw(raw, m);
+            // the renderer's packed form, so these queries see its numbers
+            float4 g[kPacked];
+            pack_mixture(raw, g);
             if (mode == Q_PDF) {
                 const float* w = aux + r * 3;
-                out[r] = mixture_pdf(m, f3(w[0], w[1], w[2]));
+                out[r] = packed_pdf(g, f3(w[0], w[1], w[2]));
             } else {
                 const float* u = aux + r * 3;
-                F3 w = mixture_sample(m, u[0], u[1], u[2]);
+                F3 w = packed_sample(g, u[0], u[1], u[2]);
                 out[r * 3] = w.x;
                 out[r * 3 + 1] = w.y;
                 out[r * 3 + 2] = w.z;
-                out2[r] = mixture_pdf(m, w);
+                out2[r] = packed_pdf(g, w);
             }
         }
     }
@@ -567,22 +569,32 @@ extern "C" int pgx_mlp_train_step(pgx_ctx* ctx, const pgx_radiance_sample* sampl
     return train_host(ctx, samples, n, lr, loss, nullptr, true, "pgx_mlp_train_step");
 }
 
-extern "C" int pgx_mlp_configure(pgx_ctx* ctx, float lr, float decay, int64_t batch) {
+extern "C" int pgx_mlp_configure(pgx_ctx* ctx, float lr, float decay, int64_t batch, int32_t steps) {
     PGX_TRY(ensure_ready(ctx, "pgx_mlp_configure"));
-    if (!(lr > 0.f) || !(decay > 0.f) || decay > 1.f || batch <= 0)
+    if (!(lr > 0.f) || !(decay > 0.f) || decay > 1.f || batch <= 0 || steps <= 0 || steps > 64)
         return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_mlp_configure: bad arguments");
     MlpState* st = state(ctx);
     st->lr = lr;
     st->decay = decay;
     st->batch = batch;
+    st->steps = steps;
     return PGX_OK;
 }
 
-// Online step inside pgx_render: learning rate lr * decay^step.
+// Online training inside pgx_render: `steps` Adam steps on consecutive
+// slices of the frame's samples (the last slice only if at least a quarter
+// of a batch), learning rate lr * decay^step.
 int mlp_online_step(pgx_ctx* ctx, const float* samples, int64_t n) {
     MlpState* st = state(ctx);
     if (!st->valid || n <= 0) return PGX_OK;
-    n = std::min(n, st->batch);
-    float lr = st->lr * powf(st->decay, (float)st->step);
-    return mlp_train_device(ctx, samples, n, lr, nullptr, true);
+    for (int k = 0; k < st->steps; k++) {
+        int64_t off = (int64_t)k * st->batch;
+        int64_t nk = std::min(st->batch, n - off);
+        if (nk <= 0 || (k > 0 && nk < st->batch / 4)) break;
+        float lr = st->lr * powf(st->decay, (float)st->step);
+        PGX_TRY(mlp_train_device(ctx, samples + off * kSampleFloats, nk, lr, nullptr, true));
+    }
+    return PGX_OK;
 }
+
+int64_t mlp_train_batch(pgx_ctx* ctx) { return state(ctx)->batch * state(ctx)->steps; }

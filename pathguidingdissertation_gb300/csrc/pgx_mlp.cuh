@@ -182,6 +182,67 @@ __device__ __forceinline__ F3 mixture_sample(const Mixture& m, float u0, float u
     return normalize(t * (sw * c) + bt * (sw * s) + mu * cw);
 }
 
+// ---- packed mixture, as the renderer keeps it per path ------------------------------
+// 12 float4: lobe i = (mu.xyz, kappa) for i < 8; then c_0..c_7 with
+// c_i = w_i kappa_i / (2 pi (1 - e^{-2 kappa_i})), so q(w) = sum_i c_i
+// exp(kappa_i (mu_i.w - 1)); then the running sums of w_i for the lobe choice.
+constexpr int kPacked = 12;
+
+__device__ __forceinline__ void pack_mixture(const float* raw, float4* g) {
+    Mixture m;
+    mixture_from_raw(raw, m);
+    float c[kLobes], cdf[kLobes];
+    float acc = 0.f;
+#pragma unroll
+    for (int i = 0; i < kLobes; i++) {
+        float k = m.lobe[i].w;
+        c[i] = m.w[i] * k / (2.f * 3.14159265f * (-expm1f(-2.f * k)));
+        acc += m.w[i];
+        cdf[i] = acc;
+        g[i] = m.lobe[i];
+    }
+    g[8] = make_float4(c[0], c[1], c[2], c[3]);
+    g[9] = make_float4(c[4], c[5], c[6], c[7]);
+    g[10] = make_float4(cdf[0], cdf[1], cdf[2], cdf[3]);
+    g[11] = make_float4(cdf[4], cdf[5], cdf[6], cdf[7]);
+}
+
+__device__ __forceinline__ float packed_pdf(const float4* __restrict__ g, F3 w) {
+    float4 c0 = g[8], c1 = g[9];
+    float c[kLobes] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+    float p = 0.f;
+#pragma unroll
+    for (int i = 0; i < kLobes; i++) {
+        float4 l = g[i];
+        float cosv = l.x * w.x + l.y * w.y + l.z * w.z;
+        p += c[i] * __expf(l.w * (cosv - 1.f));
+    }
+    return p;
+}
+
+__device__ __forceinline__ F3 packed_sample(const float4* __restrict__ g, float u0, float u1, float u2) {
+    float4 a = g[10], b = g[11];
+    float cdf[kLobes] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    int pick = kLobes - 1;
+#pragma unroll
+    for (int i = kLobes - 2; i >= 0; i--)
+        if (u0 < cdf[i]) pick = i;
+    float4 l = g[pick];
+    float k = l.w;
+    float cw = 1.f + __logf(u1 + (1.f - u1) * __expf(-2.f * k)) / k;
+    cw = fminf(fmaxf(cw, -1.f), 1.f);
+    float sw = sqrtf(fmaxf(0.f, 1.f - cw * cw));
+    float s, c;
+    sincospif(2.f * u2, &s, &c);
+    F3 mu = f3(l.x, l.y, l.z);
+    float sign = copysignf(1.f, mu.z);
+    float aa = -1.f / (sign + mu.z);
+    float bb = mu.x * mu.y * aa;
+    F3 t = f3(1.f + sign * mu.x * mu.x * aa, sign * bb, -sign * mu.x);
+    F3 bt = f3(bb, sign + mu.y * mu.y * aa, -mu.y);
+    return normalize(t * (sw * c) + bt * (sw * s) + mu * cw);
+}
+
 // Loss of one training sample, -weight * log q(wi), and its gradient with
 // respect to the 40 raw outputs (d[40]).
 __device__ __forceinline__ float loss_grad(const float* raw, F3 wi, float weight, float* d) {
@@ -306,3 +367,5 @@ struct MlpView {
 MlpView mlp_view(pgx_ctx* ctx);
 int mlp_train_device(pgx_ctx* ctx, const float* samples, int64_t n, float lr, double* loss, bool update);
 int mlp_query_device(pgx_ctx* ctx, const float* q, const float* aux, int64_t n, int mode, float* out, float* out2);
+int mlp_online_step(pgx_ctx* ctx, const float* samples, int64_t n);
+int64_t mlp_train_batch(pgx_ctx* ctx);

@@ -1,7 +1,10 @@
 // Wavefront path tracer: RayTracer::render (Renderer.h:648-747) with the
 // integrators pathTraceRecursive (Renderer.h:531-613, PGX_MODE_PLAIN) and
 // guidedPath/guidedPathRecursive (Renderer.h:368-528, PGX_MODE_GUIDED_LI),
-// plus the QuadTree-guided estimator (PGX_MODE_GUIDED_QUADTREE, guide.cuh).
+// plus the QuadTree-guided estimator (PGX_MODE_GUIDED_QUADTREE, guide.cuh)
+// and the learned-guide estimator (PGX_MODE_GUIDED_MLP, pgx_mlp.cuh), whose
+// network runs on the tensor cores in k_guide_infer between traversal and
+// shading at every depth.
 //
 // One path per (pixel, sample).  The recursion of the reference becomes a
 // loop over depth with queue-per-stage kernels:
@@ -24,6 +27,7 @@
 
 #include "pgx_ctx.h"
 #include "pgx_guide.cuh"
+#include "pgx_mlp.cuh"
 #include "pgx_shade.cuh"
 #include "pgx_trace.cuh"
 
@@ -67,14 +71,26 @@ struct PathState {
     unsigned* nvertices;
     int64_t capacity;
     int64_t vcapacity;
+    // learned guide: per-path mixture (10 float4), training records
+    float4* guide;
+    float4* rec_wo;   // wo
+    float4* rec_f;    // f |cos| / pdf of the continuation
+    float* train;     // radiance samples, 13 floats each
+    unsigned* ntrain;
+    int64_t tcapacity;
 };
 
 struct RenderState {
     DevBuf o, d, T, L, hit, pix, rng, flags, nrec, q0, q1, sh_path, sh_o, sh_d, sh_c;
     DevBuf rec_pos, rec_nrm, rec_wi, rec_w, rec_e;
     DevBuf counters, vertices;
+    DevBuf guide, rec_wo, rec_f, train;
     int64_t capacity = 0;
     int rec_depth = 0;
+    int64_t guide_capacity = 0;
+    int train_depth = 0;
+    int64_t tcapacity = 0;
+    int64_t train_last = 0;   // samples the previous batch produced
     int64_t vcapacity = 0;
     int64_t nvertices_last = 0;
     // captured frame graph
@@ -112,6 +128,8 @@ struct FrameParams {
     float guide_fraction;
     int profile;     // count node/triangle fetches
     int mitchell;    // Mitchell-Netravali splat instead of the box filter
+    int train;       // learned guide: emit radiance samples of recorded vertices
+    float train_keep;  // probability of keeping one radiance sample
 };
 
 // ---- camera rays (Camera::generateRay, Scene.h:253-265; jitter Renderer.h:679-681)
@@ -256,7 +274,8 @@ __device__ __forceinline__ void shading_data(const SceneView& sv, const float4& 
 // light sample; returns true with the shadow ray and the contribution it
 // carries when the contribution can be non-zero.
 __device__ __noinline__ bool next_event(const SceneView& sv, const DevMaterial& m, const Shading& sd, uint64_t& rng, float4& so,
-                           float4& sdir, F3& contrib, const GuideView& gv, int qroot, float frac) {
+                           float4& sdir, F3& contrib, const GuideView& gv, int qroot, float frac,
+                           const float4* __restrict__ mix) {
     if (bsdf_pure_specular(m)) return false;
     if (sv.nlights == 0) return false;
     float pmf = 1.f / (float)sv.nlights;
@@ -276,6 +295,7 @@ __device__ __noinline__ bool next_event(const SceneView& sv, const DevMaterial& 
         float pal = pdf_light * pmf;
         float pab = bsdf_pdf(m, sv.tex, sd, wi);
         if (qroot >= 0) pab = mixture_pdf(gv, qroot, frac, pab, wi);
+        if (mix) pab = frac * mlp::packed_pdf(mix, wi) + (1.f - frac) * pab;
         float wd = power_heuristic(pal, pab);
         contrib = divs(((emitted * f) * cos_t) * wd, pal);
         target = f3(sv.bounds.centre[0], sv.bounds.centre[1], sv.bounds.centre[2]) + wi * sv.bounds.radius;
@@ -302,6 +322,7 @@ __device__ __noinline__ bool next_event(const SceneView& sv, const DevMaterial& 
         F3 f = bsdf_eval(m, sv.tex, sd, wi);
         float pb = bsdf_pdf(m, sv.tex, sd, wi);
         if (qroot >= 0) pb = mixture_pdf(gv, qroot, frac, pb, wi);
+        if (mix) pb = frac * mlp::packed_pdf(mix, wi) + (1.f - frac) * pb;
         float pal = pdf_light * pmf;
         float pab = (pb * cos_tp) / den;
         float wd = power_heuristic(pal, pab);
@@ -339,6 +360,104 @@ __device__ void next_event_draws(const SceneView& sv, const DevMaterial& m, uint
     }
 }
 
+// Continuation direction of the learned-guide estimator: one-sample MIS
+// between the network's vMF mixture (probability frac; the selection number
+// is reused as the lobe choice) and the BSDF; pdf is the mixture pdf.
+static __device__ __noinline__ F3 mlp_guided_sample(const float4* __restrict__ mix, float frac, const DevMaterial& m,
+                                                    const TexView& tv, const Shading& sd, uint64_t& rng, F3& f,
+                                                    float& pdf) {
+    float sel = pgx_rng_next(rng);
+    F3 wi;
+    if (sel < frac) {
+        float u1 = pgx_rng_next(rng), u2 = pgx_rng_next(rng);
+        wi = mlp::packed_sample(mix, sel / frac, u1, u2);
+        f = bsdf_eval(m, tv, sd, wi);
+    } else {
+        float bp;
+        wi = bsdf_sample(m, tv, sd, rng, f, bp);
+    }
+    float bp = bsdf_pdf(m, tv, sd, wi);
+    pdf = frac * mlp::packed_pdf(mix, wi) + (1.f - frac) * bp;
+    return wi;
+}
+
+__device__ __forceinline__ bool mlp_guided_surface(const DevMaterial& m) {
+    return !m.is_light && !bsdf_pure_specular(m) && m.kind != PGX_BSDF_GLASS;
+}
+
+// Learned guide, one depth: the network evaluated on the tensor cores for
+// every queued path, 128 paths per tile; paths whose hit is a guided
+// surface get their vMF mixture (10 float4) in ps.guide.
+constexpr int kInferSmem = mlp::kImageBytes + mlp::kBiasFloats * 4 + (mlp::kIn / 8) * mlp::kChunk;
+
+__global__ void __launch_bounds__(kThreads) k_guide_infer(SceneView sv, PathState ps, int depth, MlpView mv,
+                                                          int* status) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tslot;
+    mlp::FwdSmem s;
+    s.w = smem;
+    s.bias = reinterpret_cast<float*>(smem + mlp::kImageBytes);
+    s.act = smem + mlp::kImageBytes + mlp::kBiasFloats * 4;
+    s.mbar = &mbar;
+    {
+        const uint4* src = reinterpret_cast<const uint4*>(mv.image);
+        uint4* dst = reinterpret_cast<uint4*>(s.w);
+        for (int i = threadIdx.x; i < mlp::kImageBytes / 16; i += blockDim.x) dst[i] = src[i];
+        const float* b = reinterpret_cast<const float*>(mv.image + mlp::kImageBytes);
+        for (int i = threadIdx.x; i < mlp::kBiasFloats; i += blockDim.x) s.bias[i] = b[i];
+    }
+    if (threadIdx.x == 0) tc::mbar_init(&mbar, 1);
+    if (threadIdx.x < 32) {
+        tc::tmem_alloc(&tslot, 64);
+        tc::tmem_relinquish();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    s.tmem = tslot;
+    uint32_t phase = 0;
+    const unsigned n = ps.qcount[depth];
+    const int* __restrict__ q = ps.queue[depth & 1];
+    for (unsigned tile = blockIdx.x; tile * (unsigned)mlp::kRows < n; tile += gridDim.x) {
+        const unsigned i = tile * mlp::kRows + threadIdx.x;
+        int p = 0;
+        bool need = false;
+        F3 x = zero3(), nn = zero3(), wo = zero3();
+        if (i < n) {
+            p = q[i];
+            float4 h = ps.hit[p];
+            if (__float_as_int(h.x) >= 0) {
+                Shading sd;
+                DevMaterial m;
+                F3 tri_gn;
+                float tri_area;
+                shading_data(sv, ps.o[p], ps.d[p], h, sd, m, tri_gn, tri_area);
+                need = mlp_guided_surface(m);
+                x = sd.x;
+                nn = sd.sn;
+                wo = sd.wo;
+            }
+        }
+        mlp::encode_row(s.act, threadIdx.x, mv.bounds, x, nn, wo);
+        float raw[mlp::kOut];
+        if (!mlp::forward_tile(s, phase, raw)) {
+            if (threadIdx.x == 0) atomicAdd(status, 1);
+            break;
+        }
+        if (need) {
+            float4 g[mlp::kPacked];
+            mlp::pack_mixture(raw, g);
+            float4* dst = ps.guide + (size_t)p * mlp::kPacked;
+#pragma unroll
+            for (int j = 0; j < mlp::kPacked; j++) dst[j] = g[j];
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (threadIdx.x < 32) tc::tmem_dealloc(s.tmem, 64);
+}
+
 __device__ __forceinline__ void push_shadow(PathState& ps, int depth, int p, float4 so, float4 sdir, F3 c,
                                             bool want) {
     unsigned slot = warp_aggregated_add(&ps.scount[depth], want);
@@ -374,7 +493,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_shade(SceneView sv, PathState p
         const int sample_of_p = fp.spp0 + (int)(p / ((int64_t)sv.width * sv.height));
         const bool rec_on = MODE != PGX_MODE_GUIDED_LI && active && sample_of_p >= fp.collect_lo &&
                             sample_of_p < fp.collect_hi;
-        if (rec_on && depth > 0) ps.rec_e[(size_t)(depth - 1) * cap + p] = ps.L[p];
+        // (written below, after this vertex's emission is known)
         if (active) {
             float4 o = ps.o[p], d = ps.d[p], h = ps.hit[p], Tw = ps.T[p];
             uint64_t rng = ps.rng[p];
@@ -387,6 +506,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_shade(SceneView sv, PathState p
             int id = __float_as_int(h.x);
             // guided-Li record of this vertex (Renderer.h:419-427)
             F3 r_pos = zero3(), r_nrm = zero3(), r_wi = zero3(), r_w = zero3(), r_e = zero3();
+            F3 r_wo = zero3(), r_f = zero3();
             bool r_store = false;
             if (id >= 0) {
                 Shading sd;
@@ -396,6 +516,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_shade(SceneView sv, PathState p
                 shading_data(sv, o, d, h, sd, m, tri_gn, tri_area);
                 r_pos = sd.x;
                 r_nrm = sd.sn;
+                r_wo = sd.wo;
                 if (m.is_light) {
                     F3 em = f3(m.emission[0], m.emission[1], m.emission[2]);
                     if (MODE == PGX_MODE_GUIDED_LI) {
@@ -418,11 +539,13 @@ __global__ void __launch_bounds__(kThreads, 8) k_shade(SceneView sv, PathState p
                     int qroot = -1;
                     if (MODE == PGX_MODE_GUIDED_QUADTREE && !bsdf_pure_specular(m))
                         qroot = guide_region_root(gv, sd.x);
+                    const bool use_mix = MODE == PGX_MODE_GUIDED_MLP && mlp_guided_surface(m);
+                    const float4* mix = use_mix ? ps.guide + (size_t)p * mlp::kPacked : nullptr;
                     if (MODE == PGX_MODE_GUIDED_LI) {
                         next_event_draws(sv, m, rng);
                     } else {
                         F3 c;
-                        want_shadow = next_event(sv, m, sd, rng, so, sdir, c, gv, qroot, fp.guide_fraction);
+                        want_shadow = next_event(sv, m, sd, rng, so, sdir, c, gv, qroot, fp.guide_fraction, mix);
                         sc = T * c;
                     }
                     bool alive = true;
@@ -448,6 +571,8 @@ __global__ void __launch_bounds__(kThreads, 8) k_shade(SceneView sv, PathState p
                         F3 wi;
                         if (MODE == PGX_MODE_GUIDED_QUADTREE)
                             wi = guided_sample(gv, fp.guide_fraction, m, sv.tex, sd, rng, f, pdf, qroot);
+                        else if (MODE == PGX_MODE_GUIDED_MLP && use_mix)
+                            wi = mlp_guided_sample(mix, fp.guide_fraction, m, sv.tex, sd, rng, f, pdf);
                         else
                             wi = bsdf_sample(m, sv.tex, sd, rng, f, pdf);
                         float cos_t = fabsf(dot(wi, sd.sn));
@@ -463,6 +588,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_shade(SceneView sv, PathState p
                             if (pdf <= 0.f || cos_t <= 0.f) {
                                 alive = false;
                             } else {
+                                r_f = divs(f * cos_t, pdf);
                                 T = divs(T * f * cos_t, pdf);
                                 if (lum(T) <= 0.f) alive = false;
                                 if (isnan(T.x) || isnan(T.y) || isnan(T.z)) alive = false;
@@ -512,10 +638,16 @@ __global__ void __launch_bounds__(kThreads, 8) k_shade(SceneView sv, PathState p
                 ps.rec_e[ri] = make_float4(r_e.x, r_e.y, r_e.z, 0.f);
                 ps.nrec[p] = depth + 1;
             } else {
-                if (add.x != 0.f || add.y != 0.f || add.z != 0.f || !valid(add)) {
-                    float4 l = ps.L[p];
+                float4 l = ps.L[p];
+                // Baseline of the previous vertex's incident radiance: the
+                // cache records the full Li (snapshot before this vertex's
+                // emission); the learned guide trains on indirect light only
+                // (after it), since next-event estimation covers the direct.
+                if (rec_on && depth > 0)
+                    ps.rec_e[(size_t)(depth - 1) * cap + p] =
+                        fp.train ? make_float4(l.x + add.x, l.y + add.y, l.z + add.z, 0.f) : l;
+                if (add.x != 0.f || add.y != 0.f || add.z != 0.f || !valid(add))
                     ps.L[p] = make_float4(l.x + add.x, l.y + add.y, l.z + add.z, 0.f);
-                }
                 if (rec_on) {
                     size_t ri = (size_t)depth * cap + p;
                     ps.rec_pos[ri] = make_float4(r_pos.x, r_pos.y, r_pos.z, (cont && r_store) ? 1.f : 0.f);
@@ -523,6 +655,10 @@ __global__ void __launch_bounds__(kThreads, 8) k_shade(SceneView sv, PathState p
                         ps.rec_nrm[ri] = make_float4(r_nrm.x, r_nrm.y, r_nrm.z, 0.f);
                         ps.rec_wi[ri] = make_float4(r_wi.x, r_wi.y, r_wi.z, 0.f);
                         ps.rec_w[ri] = make_float4(r_w.x, r_w.y, r_w.z, 0.f);
+                        if (MODE == PGX_MODE_GUIDED_MLP && fp.train) {
+                            ps.rec_wo[ri] = make_float4(r_wo.x, r_wo.y, r_wo.z, 0.f);
+                            ps.rec_f[ri] = make_float4(r_f.x, r_f.y, r_f.z, 0.f);
+                        }
                     }
                     ps.nrec[p] = depth + 1;
                 }
@@ -674,6 +810,26 @@ __global__ void __launch_bounds__(kThreads) k_finalize(SceneView sv, PathState p
                     F3 li = f3(tn.x > 0.f ? dl.x / tn.x : 0.f, tn.y > 0.f ? dl.y / tn.y : 0.f,
                                tn.z > 0.f ? dl.z / tn.z : 0.f);
                     if (!(valid(li) && lum(li) > 0.f)) continue;
+                    if (fp.train) {
+                        // radiance sample for the learned guide, weight
+                        // Lum(Li f |cos| / pdf); a hash of (path, vertex,
+                        // batch) keeps a uniform share fp.train_keep of them
+                        uint64_t hsh = pgx_splitmix64(((uint64_t)p << 5) ^ (uint64_t)i ^ ((uint64_t)fp.spp0 << 40));
+                        float u = (float)(hsh >> 40) * (1.f / 16777216.f);
+                        if (u >= fp.train_keep) continue;
+                        float wgt = lum(li * f3(ps.rec_f[ri]));
+                        if (!(wgt > 0.f) || isinf(wgt)) continue;
+                        unsigned slot = atomicAdd(ps.ntrain, 1u);
+                        if (slot >= (unsigned)ps.tcapacity) continue;
+                        float4 nr4 = ps.rec_nrm[ri], wi = ps.rec_wi[ri], wo = ps.rec_wo[ri];
+                        float* o = ps.train + (size_t)slot * 13;
+                        o[0] = pos.x, o[1] = pos.y, o[2] = pos.z;
+                        o[3] = nr4.x, o[4] = nr4.y, o[5] = nr4.z;
+                        o[6] = wo.x, o[7] = wo.y, o[8] = wo.z;
+                        o[9] = wi.x, o[10] = wi.y, o[11] = wi.z;
+                        o[12] = wgt;
+                        continue;
+                    }
                     unsigned slot = atomicAdd(ps.nvertices, 1u);
                     if (slot >= (unsigned)ps.vcapacity) continue;
                     float4 nr4 = ps.rec_nrm[ri], wi = ps.rec_wi[ri];
@@ -710,7 +866,8 @@ RenderState* state_of(pgx_ctx* ctx) {
     return static_cast<RenderState*>(ctx->render_state);
 }
 
-int ensure_state(pgx_ctx* ctx, RenderState* rs, int64_t cap, int rec_depth, int64_t vcap) {
+int ensure_state(pgx_ctx* ctx, RenderState* rs, int64_t cap, int rec_depth, int64_t vcap, bool guide = false,
+                 int train_depth = 0, int64_t tcap = 0) {
     if (cap > rs->capacity) {
         PGX_CUDA_TRY(ctx, rs->o.reserve(sizeof(float4) * cap));
         PGX_CUDA_TRY(ctx, rs->d.reserve(sizeof(float4) * cap));
@@ -742,6 +899,20 @@ int ensure_state(pgx_ctx* ctx, RenderState* rs, int64_t cap, int rec_depth, int6
     if (vcap > rs->vcapacity) {
         PGX_CUDA_TRY(ctx, rs->vertices.reserve(sizeof(pgx_path_vertex) * vcap));
         rs->vcapacity = vcap;
+    }
+    if (guide && rs->guide_capacity < rs->capacity) {
+        PGX_CUDA_TRY(ctx, rs->guide.reserve(sizeof(float4) * mlp::kPacked * rs->capacity));
+        rs->guide_capacity = rs->capacity;
+    }
+    if (train_depth > 0 && (train_depth > rs->train_depth || rs->rec_wo.bytes < sizeof(float4) * train_depth * rs->capacity)) {
+        size_t nrec = (size_t)train_depth * rs->capacity;
+        PGX_CUDA_TRY(ctx, rs->rec_wo.reserve(sizeof(float4) * nrec));
+        PGX_CUDA_TRY(ctx, rs->rec_f.reserve(sizeof(float4) * nrec));
+        rs->train_depth = train_depth;
+    }
+    if (tcap > rs->tcapacity) {
+        PGX_CUDA_TRY(ctx, rs->train.reserve(sizeof(float) * 13 * tcap));
+        rs->tcapacity = tcap;
     }
     PGX_CUDA_TRY(ctx, rs->counters.reserve(sizeof(unsigned) * 4 * (kMaxDepthCap + 2) + sizeof(unsigned long long) * kStats +
                                            sizeof(unsigned) * 4));
@@ -784,6 +955,12 @@ PathState path_view(RenderState* rs) {
     ps.vertices = rs->vertices.as<pgx_path_vertex>();
     ps.capacity = rs->capacity;
     ps.vcapacity = rs->vcapacity;
+    ps.guide = rs->guide.as<float4>();
+    ps.rec_wo = rs->rec_wo.as<float4>();
+    ps.rec_f = rs->rec_f.as<float4>();
+    ps.train = rs->train.as<float>();
+    ps.ntrain = c + 4 * (kMaxDepthCap + 2) + 2 * kStats + 1;
+    ps.tcapacity = rs->tcapacity;
     return ps;
 }
 
@@ -814,10 +991,11 @@ struct StageTimes {
 // Enqueues one batch (fp.batch samples per pixel) on stream s; returns the
 // number of kernels launched.  With fp.profile, events bracket every stage
 // (read back by stage_times after the stream is synchronised).
-int enqueue_frame(pgx_ctx* ctx, RenderState* rs, const FrameParams& fp, cudaStream_t s) {
+int enqueue_frame(pgx_ctx* ctx, RenderState* rs, const FrameParams& fp, cudaStream_t s, int* mlp_status) {
     SceneView sv = scene_view(ctx);
     PathState ps = path_view(rs);
     GuideView gv = guide_view(ctx);
+    MlpView mv = fp.mode == PGX_MODE_GUIDED_MLP ? mlp_view(ctx) : MlpView{};
     const int64_t n = (int64_t)ctx->width * ctx->height * fp.batch;
     const unsigned g = grid_for(n);
     const bool prof = fp.profile != 0;
@@ -833,12 +1011,21 @@ int enqueue_frame(pgx_ctx* ctx, RenderState* rs, const FrameParams& fp, cudaStre
         else
             k_extend<false><<<pg, kThreads, 0, s>>>(sv, ps, depth);
         if (prof) cudaEventRecord(rs->prof[4 * depth + 1], s);
+        if (fp.mode == PGX_MODE_GUIDED_MLP) {
+            const int64_t tiles = (n + mlp::kRows - 1) / mlp::kRows;
+            const unsigned ig = (unsigned)std::max<int64_t>(1, std::min<int64_t>(tiles, 152 * 3));
+            k_guide_infer<<<ig, kThreads, kInferSmem, s>>>(sv, ps, depth, mv, mlp_status);
+            launches++;
+        }
         switch (fp.mode) {
             case PGX_MODE_GUIDED_LI:
                 k_shade<PGX_MODE_GUIDED_LI><<<g, kThreads, 0, s>>>(sv, ps, fp, depth, gv);
                 break;
             case PGX_MODE_GUIDED_QUADTREE:
                 k_shade<PGX_MODE_GUIDED_QUADTREE><<<g, kThreads, 0, s>>>(sv, ps, fp, depth, gv);
+                break;
+            case PGX_MODE_GUIDED_MLP:
+                k_shade<PGX_MODE_GUIDED_MLP><<<g, kThreads, 0, s>>>(sv, ps, fp, depth, gv);
                 break;
             default:
                 k_shade<PGX_MODE_PLAIN><<<g, kThreads, 0, s>>>(sv, ps, fp, depth, gv);
@@ -916,7 +1103,7 @@ extern "C" int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t fr
     if (!ctx) return PGX_ERR_INVALID_ARG;
     ctx->err.clear();
     if (!cfg || frames < 0) return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_render: bad arguments");
-    if (cfg->mode < PGX_MODE_PLAIN || cfg->mode > PGX_MODE_GUIDED_QUADTREE)
+    if (cfg->mode < PGX_MODE_PLAIN || cfg->mode > PGX_MODE_GUIDED_MLP)
         return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_render: unknown mode %d", cfg->mode);
     if (cfg->max_depth < 0 || cfg->max_depth > kMaxDepthCap)
         return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_render: max_depth must be in [0, %d]", kMaxDepthCap);
@@ -924,6 +1111,10 @@ extern "C" int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t fr
     if (!ctx->has_bvh) return pgx_fail(ctx, PGX_ERR_STATE, "pgx_render: no BVH");
     if (cfg->mode == PGX_MODE_GUIDED_QUADTREE && !guide_ready(ctx))
         return pgx_fail(ctx, PGX_ERR_STATE, "pgx_render: guided mode needs a radiance cache (pgx_cache_build)");
+    if (cfg->mode == PGX_MODE_GUIDED_MLP && !mlp_view(ctx).valid)
+        return pgx_fail(ctx, PGX_ERR_STATE, "pgx_render: learned-guide mode needs pgx_mlp_init");
+    if ((cfg->flags & PGX_RENDER_TRAIN_GUIDE) && cfg->mode != PGX_MODE_GUIDED_MLP)
+        return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_render: PGX_RENDER_TRAIN_GUIDE needs PGX_MODE_GUIDED_MLP");
     PGX_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     PGX_TRY(ensure_film(ctx));
     if (frames == 0) return PGX_OK;
@@ -945,17 +1136,30 @@ extern "C" int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t fr
         collect_hi = ctx->spp + frames;
         collect_lo = collect_hi - std::min(cfg->record_paths, frames);
     }
-    const bool recording = collect_hi > collect_lo;
-    const int rec_depth = (guided_li || recording) ? cfg->max_depth + 1 : 0;
+    // Online training of the learned guide records every frame's vertices
+    // for radiance samples instead of path vertices.
+    const bool train = (cfg->flags & PGX_RENDER_TRAIN_GUIDE) != 0;
+    if (train) {
+        collect_lo = ctx->spp;
+        collect_hi = ctx->spp + frames;
+    }
+    const bool recording = collect_hi > collect_lo && !train;
+    const int rec_depth = (guided_li || recording || train) ? cfg->max_depth + 1 : 0;
     // Samples per wavefront: enough paths to fill the GPU, bounded memory
     // (per-depth vertex records cost 80 bytes per path and depth).
     const int64_t target_paths = rec_depth ? (int64_t)(1 << 21) : (int64_t)(1 << 22);
     int batch = (int)std::max<int64_t>(1, std::min<int64_t>(frames, target_paths / std::max<int64_t>(npix, 1)));
+    if (train) batch = 1;  // one Adam step after every frame
     const int64_t vcap = recording ? npix * (cfg->max_depth + 1) * (collect_hi - collect_lo) : 0;
-    PGX_TRY(ensure_state(ctx, rs, npix * batch, rec_depth, vcap));
+    const bool mlp_mode = cfg->mode == PGX_MODE_GUIDED_MLP;
+    const int64_t tcap = train ? mlp_train_batch(ctx) : 0;
+    PGX_TRY(ensure_state(ctx, rs, npix * batch, rec_depth, vcap, mlp_mode, train ? rec_depth : 0, tcap));
+    if (mlp_mode)
+        PGX_CUDA_TRY(ctx, cudaFuncSetAttribute(k_guide_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, kInferSmem));
     cudaStream_t s = ctx->stream;
     PathState ps = path_view(rs);
     PGX_CUDA_TRY(ctx, cudaMemsetAsync(ps.stats, 0, sizeof(unsigned long long) * kStats + sizeof(unsigned) * 4, s));
+    int* mlp_status = reinterpret_cast<int*>(ps.nvertices + 2);
     const bool prof = (cfg->flags & PGX_RENDER_PROFILE) != 0;
     StageTimes times;
     int64_t launches = 0, batches = 0;
@@ -973,9 +1177,23 @@ extern "C" int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t fr
         fp.guide_fraction = cfg->guide_fraction;
         fp.profile = prof ? 1 : 0;
         fp.mitchell = (cfg->flags & PGX_RENDER_FILTER_MITCHELL) ? 1 : 0;
-        launches += enqueue_frame(ctx, rs, fp, s);
+        fp.train = train ? 1 : 0;
+        fp.train_keep = 1.f;
+        if (train && rs->train_last > 0)
+            fp.train_keep = (float)std::min(1.0, (double)tcap / (1.25 * (double)rs->train_last * fp.batch));
+        if (train) PGX_CUDA_TRY(ctx, cudaMemsetAsync(ps.ntrain, 0, sizeof(unsigned), s));
+        launches += enqueue_frame(ctx, rs, fp, s, mlp_status);
         batches++;
         PGX_CUDA_TRY(ctx, cudaGetLastError());
+        if (train) {
+            // one Adam step on this batch's radiance samples
+            unsigned nt = 0;
+            PGX_CUDA_TRY(ctx, cudaMemcpyAsync(&nt, ps.ntrain, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+            PGX_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+            rs->train_last = (int64_t)((double)nt / std::max(fp.train_keep, 1e-6f) / fp.batch);
+            PGX_TRY(mlp_online_step(ctx, ps.train, std::min<int64_t>(nt, tcap)));
+            launches += 4;
+        }
         if (prof) {
             PGX_CUDA_TRY(ctx, cudaStreamSynchronize(s));
             stage_times(rs, fp.max_depth, times);
@@ -987,7 +1205,10 @@ extern "C" int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t fr
     unsigned nv = 0;
     PGX_CUDA_TRY(ctx, cudaMemcpyAsync(st, ps.stats, sizeof(st), cudaMemcpyDeviceToHost, s));
     PGX_CUDA_TRY(ctx, cudaMemcpyAsync(&nv, ps.nvertices, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    int mst = 0;
+    PGX_CUDA_TRY(ctx, cudaMemcpyAsync(&mst, mlp_status, sizeof(int), cudaMemcpyDeviceToHost, s));
     PGX_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    if (mst != 0) return pgx_fail(ctx, PGX_ERR_TIMEOUT, "pgx_render: tensor-core wait timed out in %d CTA(s)", mst);
     float ms = 0.f;
     PGX_CUDA_TRY(ctx, cudaEventElapsedTime(&ms, rs->ev0, rs->ev1));
     ctx->spp += frames;

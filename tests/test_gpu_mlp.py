@@ -152,3 +152,65 @@ def test_api_errors(ctx, pgx_lib):
         ctx.mlp_init(1, BMIN, BMIN)                        # empty bounds
     with pytest.raises(PgxError):
         ctx.mlp_configure(lr=-1.0)
+
+
+# ---- the learned guide inside the renderer ---------------------------------------------
+from pathguidingdissertation_gb300 import scenes  # noqa: E402
+
+
+def _tile_z(a, a2, b, b2, spp, t=8):
+    H, W = a.shape[:2]
+
+    def tiles(x):
+        return x[: H // t * t, : W // t * t].reshape(H // t, t, W // t, t, 3).sum(axis=(1, 3))
+
+    n = spp * t * t
+    ma, mb = tiles(a) / n, tiles(b) / n
+    va = np.maximum(tiles(a2) / n - ma * ma, 0) / n
+    vb = np.maximum(tiles(b2) / n - mb * mb, 0) / n
+    z = np.abs(ma - mb) / np.sqrt(va + vb + 1e-12)
+    z_total = abs(ma.sum() - mb.sum()) / np.sqrt(va.sum() + vb.sum())
+    return z, z_total
+
+
+@pytest.mark.parametrize("scene,trained", [("cornell", False), ("cornell", True), ("interior", True)])
+def test_mlp_guided_estimator_unbiased(ctx, scene, trained):
+    if scene == "cornell":
+        desc = scenes.cornell_box(seed=1, width=48, height=48)
+    else:
+        desc = scenes.interior(seed=3, target_tris=20000, n_objects=40, width=48, height=27, env_width=256,
+                               env_height=128)
+    ctx.upload(desc)
+    ctx.bvh_build()
+    ctx.mlp_init(3)
+    if trained:
+        ctx.mlp_configure(lr=1e-2, decay=0.99, batch=1 << 14)
+        ctx.render(32, mode=abi.MODE_GUIDED_MLP, seed=99, max_depth=8, train_guide=True)
+        ctx.clear()
+    spp = 1024
+    ctx.render(spp, mode=abi.MODE_PLAIN, seed=5, max_depth=8)
+    a, a2, _ = ctx.film(squares=True)
+    ctx.clear()
+    ctx.render(spp, mode=abi.MODE_GUIDED_MLP, seed=6, max_depth=8, guide_fraction=0.5)
+    b, b2, _ = ctx.film(squares=True)
+    z, z_total = _tile_z(a, a2, b, b2, spp)
+    assert np.mean(z < 4.0) > 0.97, np.sort(z.ravel())[-5:]
+    assert z_total < 4.0, z_total
+
+
+def test_online_training_updates_the_guide(ctx):
+    desc = scenes.cornell_box(seed=2, width=64, height=64)
+    ctx.upload(desc)
+    ctx.bvh_build()
+    ctx.mlp_init(5)
+    p0 = ctx.mlp_params()
+    ctx.mlp_configure(lr=5e-3, decay=0.999, batch=1 << 15)
+    ctx.render(8, mode=abi.MODE_GUIDED_MLP, seed=1, max_depth=8, train_guide=True)
+    p1 = ctx.mlp_params()
+    assert np.all(np.isfinite(p1)) and not np.array_equal(p0, p1)
+    rgb, _, spp = ctx.film()
+    assert spp == 8 and np.all(np.isfinite(rgb)) and rgb.mean() > 0
+    # training needs the learned-guide mode
+    from pathguidingdissertation_gb300.abi import PgxError
+    with pytest.raises(PgxError):
+        ctx.render(1, mode=abi.MODE_PLAIN, train_guide=True)
