@@ -436,6 +436,34 @@ int pgx_mlp_train_step(pgx_ctx* ctx, const pgx_radiance_sample* samples, int64_t
  * 0.998, 262144, 4). */
 int pgx_mlp_configure(pgx_ctx* ctx, float lr, float decay, int64_t batch, int32_t steps);
 
+/* ---- differentiable rendering (extension; the reference renders forward only) ----
+ * Plain path tracing with NEE + MIS (PGX_MODE_PLAIN's estimator, box
+ * filter, one thread per pixel) whose sampling decisions -- directions,
+ * pdfs, MIS weights, Russian roulette and the environment's sampling
+ * tables -- use the uploaded scene, while radiance is evaluated with the
+ * "evaluation parameters": environment texels, a per-material albedo
+ * offset (added to the sampled albedo texture; for constant albedos this is
+ * the albedo itself) and per-material GGX roughness.  The estimator stays
+ * unbiased for every evaluation-parameter value, and its derivative with
+ * the sampling held fixed is an unbiased estimate of the image's gradient. */
+
+/* Sets the evaluation parameters; NULL keeps the uploaded value (env W*H*3,
+ * albedo_offset nmats*3 -- zero is the uploaded albedo -- roughness nmats). */
+int pgx_diff_set_params(pgx_ctx* ctx, const float* env_rgb, const float* albedo_offset, const float* roughness);
+/* Mean of spp samples per pixel (seeds hash(seed, pixel, sample)) in double,
+ * summed in a fixed order, so two calls differ only through the samples a
+ * parameter change touches.  image: W*H*3. */
+int pgx_diff_render(pgx_ctx* ctx, int32_t spp, uint64_t seed, int32_t max_depth, double* image);
+/* Gradient of sum_p dloss_dimage[p] . image[p] (the image of
+ * pgx_diff_render with the same spp, seed and max_depth) with respect to the
+ * environment texels (W*H*3), the albedo offsets (nmats*3) and the
+ * roughness values (nmats), by replaying every sample from its seed (path
+ * replay back-propagation; no path state is stored).  Albedo gradients are
+ * computed for diffuse, Oren-Nayar, mirror and conductor materials, roughness
+ * gradients for rough conductors; outputs may be NULL. */
+int pgx_diff_adjoint(pgx_ctx* ctx, int32_t spp, uint64_t seed, int32_t max_depth, const float* dloss_dimage,
+                     float* grad_env, float* grad_albedo, float* grad_roughness);
+
 #ifdef __cplusplus
 }
 #endif

@@ -278,6 +278,31 @@ class Context:
     def mlp_configure(self, lr: float = 5e-3, decay: float = 0.998, batch: int = 262144, steps: int = 4) -> None:
         self.check(self.lib.pgx_mlp_configure(self.h, lr, decay, batch, steps))
 
+    # ---- differentiable rendering ----
+    def diff_set_params(self, env: np.ndarray | None = None, albedo_offset: np.ndarray | None = None,
+                        roughness: np.ndarray | None = None) -> None:
+        e = None if env is None else np.ascontiguousarray(env, np.float32)
+        a = None if albedo_offset is None else np.ascontiguousarray(albedo_offset, np.float32)
+        r = None if roughness is None else np.ascontiguousarray(roughness, np.float32)
+        self.check(self.lib.pgx_diff_set_params(self.h, ptr(e), ptr(a), ptr(r)))
+
+    def diff_render(self, spp: int, seed: int = 1, max_depth: int = 8) -> np.ndarray:
+        w, h = self.scene.camera["width"], self.scene.camera["height"]
+        img = np.zeros((h, w, 3), np.float64)
+        self.check(self.lib.pgx_diff_render(self.h, spp, seed, max_depth, ptr(img)))
+        return img
+
+    def diff_adjoint(self, dloss_dimage: np.ndarray, spp: int, seed: int = 1, max_depth: int = 8):
+        """(grad_env (H_env, W_env, 3) or None, grad_albedo (nmats, 3), grad_roughness (nmats,))."""
+        d = np.ascontiguousarray(dloss_dimage, np.float32)
+        nm = len(self.scene.materials)
+        env = self.scene.env
+        ge = None if env is None else np.zeros(env.shape, np.float32)
+        ga = np.zeros((nm, 3), np.float32)
+        gr = np.zeros(nm, np.float32)
+        self.check(self.lib.pgx_diff_adjoint(self.h, spp, seed, max_depth, ptr(d), ptr(ge), ptr(ga), ptr(gr)))
+        return ge, ga, gr
+
     def cache_knn(self, queries: np.ndarray, k: int) -> tuple[np.ndarray, np.ndarray]:
         q = np.ascontiguousarray(queries, np.float32).reshape(-1, 3)
         idx = np.zeros((len(q), k), np.int32)

@@ -78,6 +78,7 @@ int make_batch(pgx_ctx* ctx, const pgx_material* mat, BsdfBatch& b) {
         d.eta[k] = mat->eta[k];
         d.k[k] = mat->k[k];
         d.emission[k] = mat->emission[k];
+        d.alb_off[k] = 0.f;
         b.albedo[k] = mat->albedo[k];
     }
     d.int_ior = mat->int_ior;

@@ -56,6 +56,7 @@ struct DevMaterial {
     float alpha;      // 1.62142 * sqrt(roughness)
     float sigma;
     float emission[3];
+    float alb_off[3];  // added to the sampled albedo (0 except in differentiable renders)
 };
 
 struct DevTexture {

@@ -125,7 +125,8 @@ static __device__ F3 tex_sample_raw(const float* texels, long long offset, int W
 }
 __device__ __forceinline__ F3 albedo_of(const TexView& tv, const DevMaterial& m, const Shading& sd) {
     DevTexture t = tv.info[m.tex];
-    return tex_sample_raw(tv.texels, t.offset, t.width, t.height, sd.tu, sd.tv);
+    F3 a = tex_sample_raw(tv.texels, t.offset, t.width, t.height, sd.tu, sd.tv);
+    return f3(a.x + m.alb_off[0], a.y + m.alb_off[1], a.z + m.alb_off[2]);
 }
 
 // ---- Fresnel and GGX (ShadingHelper, Materials.h:34-119) ---------------------

@@ -100,6 +100,9 @@ struct RenderState {
     int graph_spp0 = -1;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t prof[kProfEvents] = {};
+    // differentiable rendering: evaluation parameters and scratch
+    DevBuf d_mats, d_env, d_partial, d_img, d_dimg, d_genv, d_galb, d_grough;
+    bool d_params = false;
 };
 
 struct SceneView {
@@ -132,6 +135,24 @@ struct FrameParams {
     float train_keep;  // probability of keeping one radiance sample
 };
 
+// Camera::generateRay (Scene.h:45-57) direction for film position (px, py).
+__device__ __forceinline__ F3 camera_dir(const DevCamera& cam, float px, float py) {
+    float xc = (2.f * px / cam.width) - 1.f;
+    float yc = (2.f * (1.f - (py / cam.height))) - 1.f;
+    const float* m = cam.inv_proj;
+    float vx = ((xc * m[0] + yc * m[1]) + 0.f * m[2]) + m[3];
+    float vy = ((xc * m[4] + yc * m[5]) + 0.f * m[6]) + m[7];
+    float vz = ((xc * m[8] + yc * m[9]) + 0.f * m[10]) + m[11];
+    float w = ((m[12] * xc + m[13] * yc) + m[14] * 0.f) + m[15];
+    w = 1.f / w;
+    vx = vx * w;
+    vy = vy * w;
+    vz = vz * w;
+    const float* c = cam.cam;
+    return normalize(f3((vx * c[0] + vy * c[1]) + vz * c[2], (vx * c[4] + vy * c[5]) + vz * c[6],
+                        (vx * c[8] + vy * c[9]) + vz * c[10]));
+}
+
 // ---- camera rays (Camera::generateRay, Scene.h:253-265; jitter Renderer.h:679-681)
 __global__ void __launch_bounds__(kThreads) k_camgen(SceneView sv, PathState ps, FrameParams fp) {
     const int64_t npix = (int64_t)sv.width * sv.height;
@@ -144,20 +165,7 @@ __global__ void __launch_bounds__(kThreads) k_camgen(SceneView sv, PathState ps,
         float px = (float)xpix + pgx_rng_next(rng);
         float py = (float)ypix + pgx_rng_next(rng);
         const DevCamera& cam = sv.cam;
-        float xc = (2.f * px / cam.width) - 1.f;
-        float yc = (2.f * (1.f - (py / cam.height))) - 1.f;
-        const float* m = cam.inv_proj;
-        float vx = ((xc * m[0] + yc * m[1]) + 0.f * m[2]) + m[3];
-        float vy = ((xc * m[4] + yc * m[5]) + 0.f * m[6]) + m[7];
-        float vz = ((xc * m[8] + yc * m[9]) + 0.f * m[10]) + m[11];
-        float w = ((m[12] * xc + m[13] * yc) + m[14] * 0.f) + m[15];
-        w = 1.f / w;
-        vx = vx * w;
-        vy = vy * w;
-        vz = vz * w;
-        const float* c = cam.cam;
-        F3 dir = normalize(f3((vx * c[0] + vy * c[1]) + vz * c[2], (vx * c[4] + vy * c[5]) + vz * c[6],
-                              (vx * c[8] + vy * c[9]) + vz * c[10]));
+        F3 dir = camera_dir(cam, px, py);
         ps.o[i] = make_float4(cam.origin[0], cam.origin[1], cam.origin[2], 0.f);
         ps.d[i] = make_float4(dir.x, dir.y, dir.z, 0.f);
         ps.T[i] = make_float4(1.f, 1.f, 1.f, 0.f);
@@ -856,6 +864,401 @@ __global__ void __launch_bounds__(kThreads) k_finalize(SceneView sv, PathState p
     }
 }
 
+// ---- differentiable rendering ---------------------------------------------------------
+// Plain path tracing with NEE + MIS (the estimator of k_shade<PLAIN>) as one
+// thread per pixel looping over its samples, in two flavours sharing
+// diff_path:
+//  * primal: sampling decisions (directions, pdfs, MIS weights, Russian
+//    roulette, the environment's sampling tables) use the uploaded scene,
+//    while radiance is evaluated with the "evaluation" parameters -- the
+//    environment texels, a per-material albedo offset and GGX roughness.
+//    Each thread sums its samples per target pixel in double, and a gather
+//    kernel adds the 4 neighbours' partial sums in a fixed order, so the
+//    image is deterministic and a finite difference between two parameter
+//    sets differs only through the samples a parameter touches;
+//  * adjoint: with evaluation = uploaded parameters, each sample is traced
+//    twice from its seed.  The first pass gives its radiance L; the second
+//    replays the path and at every vertex j accumulates
+//      d/dtheta of the terms added there (NEE: albedo, roughness, the
+//      environment texels under the light direction; escaped rays: the
+//      texels under the ray), and
+//      (L - L_up_to_j) * d log beta_j / dtheta for the continuation weight
+//      beta_j = f(wi) |cos| / pdf(wi) (path replay backpropagation, Vicini
+//      et al. 2021), with pdf detached,
+//    each weighted by dLoss/dImage at the sample's pixel / spp.
+struct DiffView {
+    const DevMaterial* __restrict__ mats_e;  // evaluation materials
+    DevEnv env_e;                            // evaluation environment (sampling tables of sv.env)
+    int spp, max_depth;
+    uint64_t seed;
+    double* partial;          // primal: [npix][4][3]
+    const float* dimg;        // adjoint: dLoss/dImage [npix][3]
+    float* g_env;             // [env W*H*3]
+    float* g_alb;             // [nmats*3]
+    float* g_rough;           // [nmats]
+    int nmats;
+};
+
+// Materials whose BSDF value (and sampled weight) is proportional to the
+// albedo, so d log f / d albedo_c = 1 / albedo_c.
+__device__ __forceinline__ bool albedo_linear(const DevMaterial& m) {
+    return !m.layered && (m.kind == PGX_BSDF_DIFFUSE || m.kind == PGX_BSDF_ORENNAYAR ||
+                          m.kind == PGX_BSDF_MIRROR || m.kind == PGX_BSDF_CONDUCTOR);
+}
+
+// d log f / d roughness of a rough GGX conductor at (wil, wol): from D
+// (d log D / d alpha = 2/alpha - 4 alpha c^2 / (c^2 (alpha^2 - 1) + 1)) and
+// both Smith G1 factors (d log G1 / d alpha = -(d Lambda / d alpha) /
+// (1 + Lambda), d Lambda / d alpha = alpha tan^2 / (2 sqrt(1 + alpha^2
+// tan^2))), times d alpha / d roughness = 1.62142^2 / (2 alpha).
+__device__ float conductor_dlogf_drough(const DevMaterial& m, F3 wil, F3 wol) {
+    if (m.kind != PGX_BSDF_CONDUCTOR || m.layered || m.alpha < PGX_EPSILON) return 0.f;
+    if (wil.z <= 0.f || wol.z <= 0.f) return 0.f;
+    F3 h = wil + wol;
+    if (length_sq(h) < PGX_EPSILON) return 0.f;
+    h = normalize(h);
+    const float a = m.alpha, a2 = a * a;
+    float c2 = h.z * h.z;
+    float d = 2.f / a - 4.f * a * c2 / (c2 * (a2 - 1.f) + 1.f);
+    auto dlg1 = [&](F3 w) {
+        float wc2 = w.z * w.z;
+        float t2 = fabsf(fmaxf(1.f - wc2, 0.f) / wc2);
+        float r = sqrtf(1.f + a2 * t2);
+        float lam = (r - 1.f) * 0.5f;
+        return -(a * t2 / (2.f * r)) / (1.f + lam);
+    };
+    d += dlg1(wil) + dlg1(wol);
+    return d * (1.62142f * 1.62142f) / (2.f * a);
+}
+
+// Adds g (rgb) times the bilinear weights of the environment lookup of wi
+// (env_eval's texel choice) to the texel gradients.
+__device__ void env_scatter(const DevEnv& e, F3 wi, F3 g, float* grad) {
+    if (!e.valid || !grad) return;
+    float u = atan2f(wi.z, wi.x);
+    u = (u < 0.f) ? (float)((double)u + 2.0 * PGX_PI_D) : u;
+    u = (float)((double)u / (2.0 * PGX_PI_D));
+    float v = (float)((double)acosf(wi.y) / PGX_PI_D);
+    const int W = e.width, H = e.height;
+    float uu = fmaxf(0.f, fabsf(u)) * (float)W;
+    float vv = fmaxf(0.f, fabsf(v)) * (float)H;
+    float fu = floorf(uu), fv = floorf(vv);
+    int x = (fu >= -2147483648.f && fu < 2147483648.f) ? (int)fu : 0;
+    int y = (fv >= -2147483648.f && fv < 2147483648.f) ? (int)fv : 0;
+    float au = uu - (float)x, av = vv - (float)y;
+    float w[4] = {(1.f - au) * (1.f - av), au * (1.f - av), (1.f - au) * av, au * av};
+    x = wrap_index(x, W);
+    y = wrap_index(y, H);
+    int x1 = wrap_index(x + 1, W), y1 = wrap_index(y + 1, H);
+    long long idx[4] = {(long long)y * W + x, (long long)y * W + x1, (long long)y1 * W + x, (long long)y1 * W + x1};
+    for (int k = 0; k < 4; k++) {
+        if (w[k] == 0.f) continue;
+        atomicAdd(grad + 3 * idx[k] + 0, g.x * w[k]);
+        atomicAdd(grad + 3 * idx[k] + 1, g.y * w[k]);
+        atomicAdd(grad + 3 * idx[k] + 2, g.z * w[k]);
+    }
+}
+
+struct DiffAcc {
+    float* alb;    // shared memory [nmats*3] or global
+    float* rough;  // [nmats]
+};
+
+__device__ __forceinline__ void add_alb(const DiffAcc& acc, int mat, F3 g) {
+    atomicAdd(acc.alb + 3 * mat + 0, g.x);
+    atomicAdd(acc.alb + 3 * mat + 1, g.y);
+    atomicAdd(acc.alb + 3 * mat + 2, g.z);
+}
+
+__device__ __forceinline__ F3 safe_div3(F3 a, F3 b) {
+    return f3(a.x / fmaxf(b.x, 1e-6f), a.y / fmaxf(b.y, 1e-6f), a.z / fmaxf(b.z, 1e-6f));
+}
+
+// One path from its seed.  GRAD: L_total is the first pass's radiance and
+// delta the adjoint of the sample's value.  Returns the path's radiance.
+template <bool GRAD>
+__device__ F3 diff_path(const SceneView& sv, const DiffView& dv, uint64_t rng, F3 o, F3 dir, F3 L_total, F3 delta,
+                        const DiffAcc& acc) {
+    F3 T = f3(1.f, 1.f, 1.f), Ts = T, L = zero3();
+    bool prev_spec = false;
+    float prev_pdf = 0.f;
+    for (int depth = 0; depth <= dv.max_depth; depth++) {
+        int id;
+        float t, hu, hv;
+        int status;
+        unsigned long long ni = 0, nt = 0;
+        bvh_trace<false, false>(sv.bvh, mk(o.x, o.y, o.z), mk(dir.x, dir.y, dir.z), FLT_MAX, id, t, hu, hv, status,
+                                ni, nt);
+        if (status) id = -1;
+        if (id < 0) {
+            // Background (k_shade<PLAIN>'s miss branch); decisions on the
+            // sampling environment, radiance from the evaluation one.
+            F3 bg_s = env_eval(sv.env, dir);
+            F3 bg = env_eval(dv.env_e, dir);
+            float w = 0.f;
+            if (depth == 0 || prev_spec) {
+                w = 1.f;
+            } else if (!(lum(bg_s) < 1e-8f)) {
+                float pmf = 1.f / (float)sv.nlights;
+                float pdf_light = env_pdf(sv.env, dir);
+                if (pmf > 0.f && pdf_light > 0.f) w = power_heuristic(prev_pdf, pmf * pdf_light);
+            }
+            if (w > 0.f) {
+                L = L + (T * bg) * w;
+                if (GRAD) env_scatter(dv.env_e, dir, (delta * T) * w, dv.g_env);
+            }
+            break;
+        }
+        Shading sd;
+        DevMaterial ms;
+        F3 tri_gn;
+        float tri_area;
+        shading_data(sv, make_float4(o.x, o.y, o.z, 0.f), make_float4(dir.x, dir.y, dir.z, 0.f),
+                     make_float4(__int_as_float(id), t, hu, hv), sd, ms, tri_gn, tri_area);
+        const DevMaterial me = dv.mats_e[sd.mat];
+        if (ms.is_light) {
+            F3 em = f3(ms.emission[0], ms.emission[1], ms.emission[2]);
+            if (depth == 0 || prev_spec) {
+                L = L + T * em;
+            } else {
+                float pmf = 1.f / (float)sv.nlights;
+                float cos_tp = s_max(dot(-dir, tri_gn), 0.f);
+                float d2 = sd.t * sd.t;
+                if (cos_tp > 0.f && !(d2 < PGX_EPSILON)) {
+                    float pab = (prev_pdf * cos_tp) / d2;
+                    L = L + (T * em) * power_heuristic(pab, (1.f / tri_area) * pmf);
+                }
+            }
+            break;
+        }
+        // ---- next-event estimation (next_event with detached pdfs) ----
+        if (!bsdf_pure_specular(ms) && sv.nlights > 0) {
+            float pmf = 1.f / (float)sv.nlights;
+            unsigned nl = (unsigned)sv.nlights;
+            unsigned idx = (unsigned)floorf(pgx_rng_next(rng) * (float)nl);
+            idx = (nl - 1u < idx) ? nl - 1u : idx;
+            F3 target, wi, emitted;
+            float pal = 0.f, wd = 0.f, geo = 0.f;
+            bool ok = false, env_light = false;
+            if (sv.has_env_light && idx == 0) {
+                F3 col_s;
+                float pdf_light;
+                F3 d0 = env_sample(sv.env, rng, col_s, pdf_light);
+                if (pdf_light > 0.f) {
+                    wi = normalize(d0);
+                    float cos_t = s_max(dot(wi, sd.sn), 0.f);
+                    if (cos_t > 0.f) {
+                        emitted = env_eval(dv.env_e, wi);
+                        pal = pdf_light * pmf;
+                        wd = power_heuristic(pal, bsdf_pdf(ms, sv.tex, sd, wi));
+                        geo = cos_t;
+                        target = f3(sv.bounds.centre[0], sv.bounds.centre[1], sv.bounds.centre[2]) +
+                                 wi * sv.bounds.radius;
+                        ok = true;
+                        env_light = true;
+                    }
+                }
+            } else {
+                const DevAreaLight& Lt = sv.lights[idx - (unsigned)sv.has_env_light];
+                float r1 = pgx_rng_next(rng);
+                float r2 = pgx_rng_next(rng);
+                float sq = sqrtf(r1);
+                float a = 1.f - sq, b = r2 * sq, c = (1.f - a) - b;
+                float pdf_light = 1.f / Lt.p0.w;
+                target = ((f3(Lt.p0) * a) + (f3(Lt.p1) * b)) + (f3(Lt.p2) * c);
+                emitted = f3(Lt.emission);
+                if (pdf_light > 0.f) {
+                    F3 stl = target - sd.x;
+                    wi = normalize(stl);
+                    float den = length_sq(stl);
+                    if (!(den < PGX_EPSILON)) {
+                        float cos_t = s_max(dot(wi, sd.sn), 0.f);
+                        float cos_tp = s_max(dot(-wi, f3(Lt.gn)), 0.f);
+                        geo = (cos_t * cos_tp) / den;
+                        pal = pdf_light * pmf;
+                        float pab = (bsdf_pdf(ms, sv.tex, sd, wi) * cos_tp) / den;
+                        wd = power_heuristic(pal, pab);
+                        ok = geo > 0.f;
+                    }
+                }
+            }
+            if (ok) {
+                F3 fe = bsdf_eval(me, sv.tex, sd, wi);
+                F3 cw = divs(fe * (geo * wd), pal);  // radiance weight of the light sample
+                F3 contrib = emitted * cw;
+                if (contrib.x != 0.f || contrib.y != 0.f || contrib.z != 0.f) {
+                    float sgn = (dot(wi, sd.gn) >= 0.f) ? 1.f : -1.f;
+                    F3 p1 = sd.x + sd.gn * (PGX_EPSILON * sgn);
+                    F3 dvv = target - p1;
+                    float max_t = length(dvv) - (2.f * PGX_EPSILON);
+                    dvv = normalize(dvv);
+                    F3 org = p1 + dvv * PGX_EPSILON;
+                    int sid, sst;
+                    float st_, su, sv_;
+                    bool occluded = bvh_trace<true, false>(sv.bvh, mk(org.x, org.y, org.z), mk(dvv.x, dvv.y, dvv.z),
+                                                           max_t, sid, st_, su, sv_, sst, ni, nt);
+                    if (!occluded && !sst) {
+                        F3 C = T * contrib;
+                        L = L + C;
+                        if (GRAD) {
+                            F3 g = delta * C;
+                            if (albedo_linear(me)) add_alb(acc, sd.mat, safe_div3(g, albedo_of(sv.tex, me, sd)));
+                            float dr = conductor_dlogf_drough(me, to_local(sd.frame, wi), to_local(sd.frame, sd.wo));
+                            if (dr != 0.f) atomicAdd(acc.rough + sd.mat, (g.x + g.y + g.z) * dr);
+                            if (env_light) env_scatter(dv.env_e, wi, delta * (T * cw), dv.g_env);
+                        }
+                    }
+                }
+            }
+        }
+        // ---- Russian roulette on the sampling throughput ----
+        if (depth > 3) {
+            float q = s_min(s_max(PGX_EPSILON, lum(Ts)), 1.f);
+            if (pgx_rng_next(rng) < q) {
+                T = divs(T, q);
+                Ts = divs(Ts, q);
+            } else {
+                break;
+            }
+        }
+        if (depth == dv.max_depth) break;
+        // ---- continuation: sampled with the sampling material ----
+        const bool spec = bsdf_pure_specular(ms);
+        uint64_t rng0 = rng;
+        F3 fs;
+        float pdf;
+        F3 wi = bsdf_sample(ms, sv.tex, sd, rng, fs, pdf);
+        float cos_t = fabsf(dot(wi, sd.sn));
+        if (pdf <= 0.f || cos_t <= 0.f) break;
+        F3 fe;
+        if (spec) {
+            // deterministic directions: the evaluation material's own sample
+            float pe;
+            uint64_t r2 = rng0;
+            bsdf_sample(me, sv.tex, sd, r2, fe, pe);
+        } else {
+            fe = bsdf_eval(me, sv.tex, sd, wi);
+        }
+        if (GRAD) {
+            F3 g = delta * (L_total - L);  // radiance collected after this vertex
+            if (albedo_linear(me)) add_alb(acc, sd.mat, safe_div3(g, albedo_of(sv.tex, me, sd)));
+            if (!spec) {
+                float dr = conductor_dlogf_drough(me, to_local(sd.frame, wi), to_local(sd.frame, sd.wo));
+                if (dr != 0.f) atomicAdd(acc.rough + sd.mat, (g.x + g.y + g.z) * dr);
+            }
+        }
+        T = divs(T * fe * cos_t, pdf);
+        Ts = divs(Ts * fs * cos_t, pdf);
+        if (lum(Ts) <= 0.f) break;
+        if (isnan(Ts.x) || isnan(Ts.y) || isnan(Ts.z)) break;
+        if (isinf(Ts.x) || isinf(Ts.y) || isinf(Ts.z)) break;
+        if (Ts.x < 0.f || Ts.y < 0.f || Ts.z < 0.f) break;
+        float sgn = (dot(wi, sd.gn) >= 0.f) ? 1.f : -1.f;
+        o = sd.x + sd.gn * (PGX_EPSILON * sgn);
+        dir = wi;
+        prev_spec = spec;
+        prev_pdf = pdf;
+    }
+    return L;
+}
+
+// Sample s of pixel (x, y): jitter, camera ray, target pixel of the box
+// filter (Film::splat: the pixel round(x + U, y + U), -1 when outside).
+__device__ __forceinline__ int diff_camera(const SceneView& sv, const DiffView& dv, int64_t pixel, int s, uint64_t& rng,
+                                           F3& dir) {
+    int x = (int)(pixel % sv.width), y = (int)(pixel / sv.width);
+    rng = pgx_rng_init(dv.seed, (uint64_t)pixel, (uint64_t)s);
+    float px = (float)x + pgx_rng_next(rng);
+    float py = (float)y + pgx_rng_next(rng);
+    dir = camera_dir(sv.cam, px, py);
+    int bx = (int)floorf(px + 0.5f), by = (int)floorf(py + 0.5f);
+    if (bx < 0 || bx >= sv.width || by < 0 || by >= sv.height) return -1;
+    if (!(fabsf((float)bx - px) < 0.5f && fabsf((float)by - py) < 0.5f)) return -1;
+    return (by - y) * 2 + (bx - x);  // 0..3: which neighbour (right, down)
+}
+
+__global__ void __launch_bounds__(kThreads) k_diff_primal(SceneView sv, DiffView dv) {
+    const int64_t npix = (int64_t)sv.width * sv.height;
+    const F3 origin = f3(sv.cam.origin[0], sv.cam.origin[1], sv.cam.origin[2]);
+    for (int64_t pixel = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; pixel < npix;
+         pixel += (int64_t)gridDim.x * blockDim.x) {
+        double acc[4][3] = {};
+        DiffAcc none{nullptr, nullptr};
+        for (int s = 0; s < dv.spp; s++) {
+            uint64_t rng;
+            F3 dir;
+            int k = diff_camera(sv, dv, pixel, s, rng, dir);
+            F3 c = diff_path<false>(sv, dv, rng, origin, dir, zero3(), zero3(), none);
+            if (k < 0 || !valid(c)) continue;
+            acc[k][0] += (double)c.x;
+            acc[k][1] += (double)c.y;
+            acc[k][2] += (double)c.z;
+        }
+        double* out = dv.partial + pixel * 12;
+        for (int k = 0; k < 4; k++)
+            for (int c = 0; c < 3; c++) out[3 * k + c] = acc[k][c];
+    }
+}
+
+// image[p] = (partials of p, of its left, upper and upper-left neighbours
+// aimed at p) / spp, in a fixed order.
+__global__ void k_diff_gather(const double* __restrict__ partial, int W, int H, int spp, double* __restrict__ img) {
+    const int64_t npix = (int64_t)W * H;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += (int64_t)gridDim.x * blockDim.x) {
+        int x = (int)(p % W), y = (int)(p / W);
+        double v[3] = {0.0, 0.0, 0.0};
+        for (int dy = 0; dy <= 1; dy++)
+            for (int dx = 0; dx <= 1; dx++) {
+                int sx = x - dx, sy = y - dy;
+                if (sx < 0 || sy < 0) continue;
+                const double* q = partial + ((int64_t)sy * W + sx) * 12 + 3 * (dy * 2 + dx);
+                for (int c = 0; c < 3; c++) v[c] += q[c];
+            }
+        for (int c = 0; c < 3; c++) img[p * 3 + c] = v[c] / (double)spp;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_diff_adjoint(SceneView sv, DiffView dv) {
+    extern __shared__ float sacc[];  // [nmats*3 + nmats] when it fits
+    const bool shared_acc = dv.nmats * 4 * (int)sizeof(float) <= 32 * 1024;
+    DiffAcc acc;
+    if (shared_acc) {
+        for (int i = threadIdx.x; i < dv.nmats * 4; i += blockDim.x) sacc[i] = 0.f;
+        __syncthreads();
+        acc.alb = sacc;
+        acc.rough = sacc + dv.nmats * 3;
+    } else {
+        acc.alb = dv.g_alb;
+        acc.rough = dv.g_rough;
+    }
+    const int64_t npix = (int64_t)sv.width * sv.height;
+    const F3 origin = f3(sv.cam.origin[0], sv.cam.origin[1], sv.cam.origin[2]);
+    const float inv_spp = 1.f / (float)dv.spp;
+    for (int64_t pixel = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; pixel < npix;
+         pixel += (int64_t)gridDim.x * blockDim.x) {
+        int x = (int)(pixel % sv.width), y = (int)(pixel / sv.width);
+        for (int s = 0; s < dv.spp; s++) {
+            uint64_t rng;
+            F3 dir;
+            int k = diff_camera(sv, dv, pixel, s, rng, dir);
+            if (k < 0) continue;
+            int64_t tp = (int64_t)(y + k / 2) * sv.width + (x + k % 2);
+            F3 delta = f3(dv.dimg[3 * tp], dv.dimg[3 * tp + 1], dv.dimg[3 * tp + 2]) * inv_spp;
+            if (delta.x == 0.f && delta.y == 0.f && delta.z == 0.f) continue;
+            F3 L = diff_path<false>(sv, dv, rng, origin, dir, zero3(), zero3(), acc);
+            if (!valid(L)) continue;  // the film drops these samples
+            diff_path<true>(sv, dv, rng, origin, dir, L, delta, acc);
+        }
+    }
+    if (shared_acc) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < dv.nmats * 3; i += blockDim.x)
+            if (sacc[i] != 0.f) atomicAdd(dv.g_alb + i, sacc[i]);
+        for (int i = threadIdx.x; i < dv.nmats; i += blockDim.x)
+            if (sacc[dv.nmats * 3 + i] != 0.f) atomicAdd(dv.g_rough + i, sacc[dv.nmats * 3 + i]);
+    }
+}
+
 inline unsigned grid_for(int64_t n) {
     int64_t b = (n + kThreads - 1) / kThreads;
     return (unsigned)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 16));
@@ -1299,5 +1702,134 @@ extern "C" int pgx_film_tonemap(pgx_ctx* ctx, float exposure, float lmax_white, 
 extern "C" int pgx_render_get_stats(pgx_ctx* ctx, pgx_render_stats* out) {
     if (!ctx || !out) return PGX_ERR_INVALID_ARG;
     *out = ctx->rstats;
+    return PGX_OK;
+}
+
+// ---- differentiable rendering API ----------------------------------------------------------
+namespace {
+
+int diff_check(pgx_ctx* ctx, const char* who) {
+    if (!ctx) return PGX_ERR_INVALID_ARG;
+    ctx->err.clear();
+    if (!ctx->has_scene) return pgx_fail(ctx, PGX_ERR_STATE, "%s: no scene", who);
+    if (!ctx->has_bvh) return pgx_fail(ctx, PGX_ERR_STATE, "%s: no BVH", who);
+    PGX_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    return PGX_OK;
+}
+
+size_t env_floats(const pgx_ctx* ctx) {
+    return ctx->env.valid ? (size_t)ctx->env.width * ctx->env.height * 3 : 0;
+}
+
+// Evaluation parameters: a copy of the uploaded materials with albedo
+// offsets and roughness replaced, and of the environment texels.
+int diff_params(pgx_ctx* ctx, RenderState* rs, const float* env_rgb, const float* albedo_offset,
+                const float* roughness) {
+    const size_t nm = (size_t)ctx->nmats;
+    std::vector<DevMaterial> m(nm);
+    if (nm)
+        PGX_CUDA_TRY(ctx, cudaMemcpy(m.data(), ctx->mats.p, sizeof(DevMaterial) * nm, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < nm; i++) {
+        for (int c = 0; c < 3; c++) m[i].alb_off[c] = albedo_offset ? albedo_offset[3 * i + c] : 0.f;
+        float r = roughness ? roughness[i] : ctx->host_mats[i].roughness;
+        if (!(r >= 0.f)) return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_diff_set_params: roughness must be >= 0");
+        m[i].alpha = 1.62142f * sqrtf(r);
+    }
+    PGX_CUDA_TRY(ctx, rs->d_mats.reserve(sizeof(DevMaterial) * std::max<size_t>(nm, 1)));
+    if (nm)
+        PGX_CUDA_TRY(ctx, cudaMemcpy(rs->d_mats.p, m.data(), sizeof(DevMaterial) * nm, cudaMemcpyHostToDevice));
+    const size_t ef = env_floats(ctx);
+    PGX_CUDA_TRY(ctx, rs->d_env.reserve(sizeof(float) * std::max<size_t>(ef, 1)));
+    if (ef) {
+        if (env_rgb)
+            PGX_CUDA_TRY(ctx, cudaMemcpy(rs->d_env.p, env_rgb, sizeof(float) * ef, cudaMemcpyHostToDevice));
+        else
+            PGX_CUDA_TRY(ctx, cudaMemcpy(rs->d_env.p, ctx->env.texels, sizeof(float) * ef, cudaMemcpyDeviceToDevice));
+    }
+    rs->d_params = true;
+    return PGX_OK;
+}
+
+DiffView diff_view(pgx_ctx* ctx, RenderState* rs, int spp, uint64_t seed, int max_depth) {
+    DiffView dv{};
+    dv.mats_e = rs->d_mats.as<DevMaterial>();
+    dv.env_e = ctx->env;
+    dv.env_e.texels = rs->d_env.as<float>();
+    dv.spp = spp;
+    dv.seed = seed;
+    dv.max_depth = max_depth;
+    dv.nmats = ctx->nmats;
+    return dv;
+}
+
+int diff_args(pgx_ctx* ctx, int32_t spp, int32_t max_depth, const char* who) {
+    if (spp <= 0 || max_depth < 0 || max_depth > kMaxDepthCap)
+        return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "%s: spp must be > 0 and max_depth in [0, %d]", who, kMaxDepthCap);
+    return PGX_OK;
+}
+
+}  // namespace
+
+extern "C" int pgx_diff_set_params(pgx_ctx* ctx, const float* env_rgb, const float* albedo_offset,
+                                   const float* roughness) {
+    PGX_TRY(diff_check(ctx, "pgx_diff_set_params"));
+    return diff_params(ctx, state_of(ctx), env_rgb, albedo_offset, roughness);
+}
+
+extern "C" int pgx_diff_render(pgx_ctx* ctx, int32_t spp, uint64_t seed, int32_t max_depth, double* image) {
+    PGX_TRY(diff_check(ctx, "pgx_diff_render"));
+    PGX_TRY(diff_args(ctx, spp, max_depth, "pgx_diff_render"));
+    if (!image) return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_diff_render: null image");
+    RenderState* rs = state_of(ctx);
+    if (!rs->d_params) PGX_TRY(diff_params(ctx, rs, nullptr, nullptr, nullptr));
+    const int64_t npix = (int64_t)ctx->width * ctx->height;
+    PGX_CUDA_TRY(ctx, rs->d_partial.reserve(sizeof(double) * 12 * npix));
+    PGX_CUDA_TRY(ctx, rs->d_img.reserve(sizeof(double) * 3 * npix));
+    DiffView dv = diff_view(ctx, rs, spp, seed, max_depth);
+    dv.partial = rs->d_partial.as<double>();
+    SceneView sv = scene_view(ctx);
+    cudaStream_t s = ctx->stream;
+    k_diff_primal<<<grid_for(npix), kThreads, 0, s>>>(sv, dv);
+    k_diff_gather<<<grid_for(npix), kThreads, 0, s>>>(dv.partial, ctx->width, ctx->height, spp, rs->d_img.as<double>());
+    PGX_CUDA_TRY(ctx, cudaGetLastError());
+    PGX_CUDA_TRY(ctx, cudaMemcpyAsync(image, rs->d_img.p, sizeof(double) * 3 * npix, cudaMemcpyDeviceToHost, s));
+    PGX_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    return PGX_OK;
+}
+
+extern "C" int pgx_diff_adjoint(pgx_ctx* ctx, int32_t spp, uint64_t seed, int32_t max_depth, const float* dloss_dimage,
+                                float* grad_env, float* grad_albedo, float* grad_roughness) {
+    PGX_TRY(diff_check(ctx, "pgx_diff_adjoint"));
+    PGX_TRY(diff_args(ctx, spp, max_depth, "pgx_diff_adjoint"));
+    if (!dloss_dimage) return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_diff_adjoint: null dloss_dimage");
+    RenderState* rs = state_of(ctx);
+    if (!rs->d_params) PGX_TRY(diff_params(ctx, rs, nullptr, nullptr, nullptr));
+    const int64_t npix = (int64_t)ctx->width * ctx->height;
+    const size_t ef = env_floats(ctx), nm = (size_t)ctx->nmats;
+    cudaStream_t s = ctx->stream;
+    PGX_CUDA_TRY(ctx, rs->d_dimg.reserve(sizeof(float) * 3 * npix));
+    PGX_CUDA_TRY(ctx, rs->d_genv.reserve(sizeof(float) * std::max<size_t>(ef, 1)));
+    PGX_CUDA_TRY(ctx, rs->d_galb.reserve(sizeof(float) * std::max<size_t>(3 * nm, 1)));
+    PGX_CUDA_TRY(ctx, rs->d_grough.reserve(sizeof(float) * std::max<size_t>(nm, 1)));
+    PGX_CUDA_TRY(ctx, cudaMemcpyAsync(rs->d_dimg.p, dloss_dimage, sizeof(float) * 3 * npix, cudaMemcpyHostToDevice, s));
+    PGX_CUDA_TRY(ctx, cudaMemsetAsync(rs->d_genv.p, 0, sizeof(float) * std::max<size_t>(ef, 1), s));
+    PGX_CUDA_TRY(ctx, cudaMemsetAsync(rs->d_galb.p, 0, sizeof(float) * std::max<size_t>(3 * nm, 1), s));
+    PGX_CUDA_TRY(ctx, cudaMemsetAsync(rs->d_grough.p, 0, sizeof(float) * std::max<size_t>(nm, 1), s));
+    DiffView dv = diff_view(ctx, rs, spp, seed, max_depth);
+    dv.dimg = rs->d_dimg.as<float>();
+    dv.g_env = ef ? rs->d_genv.as<float>() : nullptr;
+    dv.g_alb = rs->d_galb.as<float>();
+    dv.g_rough = rs->d_grough.as<float>();
+    const size_t sm = nm * 4 * sizeof(float) <= 32 * 1024 ? nm * 4 * sizeof(float) : 0;
+    SceneView sv = scene_view(ctx);
+    k_diff_adjoint<<<grid_for(npix), kThreads, sm, s>>>(sv, dv);
+    PGX_CUDA_TRY(ctx, cudaGetLastError());
+    if (grad_env && ef)
+        PGX_CUDA_TRY(ctx, cudaMemcpyAsync(grad_env, rs->d_genv.p, sizeof(float) * ef, cudaMemcpyDeviceToHost, s));
+    if (grad_albedo && nm)
+        PGX_CUDA_TRY(ctx, cudaMemcpyAsync(grad_albedo, rs->d_galb.p, sizeof(float) * 3 * nm, cudaMemcpyDeviceToHost, s));
+    if (grad_roughness && nm)
+        PGX_CUDA_TRY(ctx, cudaMemcpyAsync(grad_roughness, rs->d_grough.p, sizeof(float) * nm, cudaMemcpyDeviceToHost, s));
+    PGX_CUDA_TRY(ctx, cudaStreamSynchronize(s));
     return PGX_OK;
 }

@@ -282,6 +282,77 @@ def interior(seed: int = 2, target_tris: int = 200_000, n_objects: int = 400, wi
     return SceneDesc(mb.triangles(), np.array(mats, MATERIAL), cam, env=env, name="interior")
 
 
+def fbm(n: int, seed: int, octaves: int = 6, lacunarity: float = 2.0, gain: float = 0.5, base: int = 4) -> np.ndarray:
+    """Fractional Brownian motion of value noise on an n x n grid over [0,1]^2:
+    sum over octaves o of gain^o * noise(base * lacunarity^o * x), each noise a
+    random lattice smoothly (smoothstep) interpolated.  Values ~ [-1, 1]."""
+    rng = np.random.default_rng(seed)
+    x = np.linspace(0.0, 1.0, n)
+    h = np.zeros((n, n))
+    amp, freq, norm = 1.0, float(base), 0.0
+    for _ in range(octaves):
+        m = int(math.ceil(freq)) + 2
+        lat = rng.uniform(-1.0, 1.0, (m, m))
+        t = x * freq
+        i = np.floor(t).astype(np.int64)
+        f = t - i
+        f = f * f * (3.0 - 2.0 * f)
+        a = lat[i[:, None], i[None, :]]
+        b = lat[i[:, None], i[None, :] + 1]
+        c = lat[i[:, None] + 1, i[None, :]]
+        d = lat[i[:, None] + 1, i[None, :] + 1]
+        fy, fx = f[:, None], f[None, :]
+        h += amp * ((a * (1 - fx) + b * fx) * (1 - fy) + (c * (1 - fx) + d * fx) * fy)
+        norm += amp
+        amp *= gain
+        freq *= lacunarity
+    return h / norm
+
+
+def terrain(grid: int = 1024, seed: int = 4, n_materials: int = 32, width: int = 512, height: int = 512,
+            env_width: int = 512, env_height: int = 256, height_scale: float = 0.35, sun_peak: float = 60.0) -> SceneDesc:
+    """The differentiable-rendering heightfield: a grid x grid vertex
+    heightfield over [-1,1]^2 (2 (grid-1)^2 triangles) with fBm heights (6
+    octaves, lacunarity 2, gain 0.5), `n_materials` GGX conductor materials
+    (albedo U[0.1,0.8]^3, roughness U[0.05,0.5], F0 U[0.5,1]) assigned by
+    height band, lit only by a sky environment map."""
+    rng = np.random.default_rng(seed)
+    hgt = fbm(grid, seed + 1) * height_scale
+    xs = np.linspace(-1.0, 1.0, grid)
+    X, Z = np.meshgrid(xs, xs, indexing="xy")
+    P = np.stack([X, hgt, Z], -1)
+    # vertex normals from central differences of the height
+    gx = np.gradient(hgt, xs, axis=1)
+    gz = np.gradient(hgt, xs, axis=0)
+    Nrm = np.stack([-gx, np.ones_like(hgt), -gz], -1)
+    Nrm /= np.linalg.norm(Nrm, axis=-1, keepdims=True)
+    UV = np.stack([(X + 1) * 0.5, (Z + 1) * 0.5], -1)
+    i, j = np.meshgrid(np.arange(grid - 1), np.arange(grid - 1), indexing="ij")
+    v00 = (i * grid + j).ravel()
+    v01 = v00 + 1
+    v10 = v00 + grid
+    v11 = v10 + 1
+    tri_idx = np.concatenate([np.stack([v00, v10, v11], 1), np.stack([v00, v11, v01], 1)])
+    Pf, Nf, UVf = P.reshape(-1, 3), Nrm.reshape(-1, 3), UV.reshape(-1, 2)
+    t = np.zeros(len(tri_idx), TRIANGLE)
+    t["v"]["p"] = Pf[tri_idx]
+    t["v"]["n"] = Nf[tri_idx]
+    t["v"]["u"] = UVf[tri_idx, 0]
+    t["v"]["v"] = UVf[tri_idx, 1]
+    centre_h = Pf[tri_idx][:, :, 1].mean(axis=1)
+    lo, hi = hgt.min(), hgt.max()
+    band = np.clip(((centre_h - lo) / max(hi - lo, 1e-9) * n_materials).astype(np.int64), 0, n_materials - 1)
+    t["material"] = band
+    mats = []
+    for _ in range(n_materials):
+        m = conductor_from_f0(rng.uniform(0.5, 1.0), rng.uniform(0.05, 0.5))
+        m["albedo"] = rng.uniform(0.1, 0.8, 3)
+        mats.append(m)
+    cam = dict(from_=(0.0, 1.25, 2.1), to=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0), fov=45.0, width=width, height=height)
+    env = sky_envmap(env_width, env_height, sun_dir=(0.5, 0.6, -0.4), sun_sigma_deg=4.0, sun_peak=sun_peak)
+    return SceneDesc(t, np.array(mats, MATERIAL), cam, env=env, name="terrain")
+
+
 def triangle_soup(n: int, seed: int = 0, extent: float = 10.0, size: float = 0.5) -> SceneDesc:
     """n random triangles in a cube, for traversal checks."""
     rng = np.random.default_rng(seed)
