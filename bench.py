@@ -368,6 +368,195 @@ def run_relmse_study(args) -> dict:
     }
 
 
+def run_adjoint_study(args) -> dict:
+    """Differentiable rendering of the fBm heightfield (2,093,058 triangles,
+    32 GGX conductor materials, 512x256 environment, 512x512): a target at
+    256 spp from parameters perturbed by N(0, 0.05), the L2 loss of a 64-spp
+    render, its gradient with respect to every environment texel and the 32
+    albedo (rgb) and 32 roughness values by the adjoint kernel, and central
+    finite differences (h = 1e-3) of the same renderer on random parameters."""
+    import time
+    from pathguidingdissertation_gb300 import build as pkg_build
+    from pathguidingdissertation_gb300 import scenes
+    from pathguidingdissertation_gb300.api import Context
+
+    pkg_build.build()
+    desc = scenes.terrain()
+    ctx = Context(0)
+    ctx.upload(desc)
+    ctx.bvh_build()
+    nm = len(desc.materials)
+    rng = np.random.default_rng(1)
+    depth, spp, seed = 8, 64, 11
+    env0 = desc.env.astype(np.float32)
+    rough0 = desc.materials["roughness"].astype(np.float32)
+    ctx.diff_set_params(env=(env0 + rng.normal(0, 0.05, env0.shape) * np.maximum(env0, 1e-3)).astype(np.float32)
+                        .clip(0.0, None),
+                        albedo_offset=rng.normal(0, 0.05, (nm, 3)).astype(np.float32),
+                        roughness=np.clip(rough0 + rng.normal(0, 0.05, nm), 0.02, 1.0).astype(np.float32))
+    t0 = time.perf_counter()
+    target = ctx.diff_render(256, seed=99, max_depth=depth)
+    target_s = time.perf_counter() - t0
+    ctx.diff_set_params()
+    t0 = time.perf_counter()
+    img = ctx.diff_render(spp, seed, depth)
+    primal_s = time.perf_counter() - t0
+    loss = float(np.sum((img - target) ** 2))
+    dimg = (2.0 * (img - target)).astype(np.float32)
+    t0 = time.perf_counter()
+    g_env, g_alb, g_rough = ctx.diff_adjoint(dimg, spp, seed, depth)
+    adjoint_s = time.perf_counter() - t0
+    h = 1e-3
+    n_fd = args.fd_params
+    kinds = rng.choice(3, n_fd, p=[0.5, 0.25, 0.25])
+    res = []
+    t0 = time.perf_counter()
+    used = np.unique(desc.triangles["material"])
+    nz_env = np.flatnonzero(np.abs(g_env).ravel() > 0)
+    for k in kinds:
+        if k == 0:
+            idx = int(rng.choice(nz_env))
+            e1 = env0.copy().ravel(); e1[idx] += h
+            e2 = env0.copy().ravel(); e2[idx] -= h
+            lp = (dict(env=e1.reshape(env0.shape)), dict(env=e2.reshape(env0.shape)))
+            g = float(g_env.ravel()[idx]); name = f"env[{idx}]"
+        elif k == 1:
+            m, c = int(rng.choice(used)), int(rng.integers(3))
+            a = np.zeros((nm, 3), np.float32); a[m, c] = h
+            lp = (dict(albedo_offset=a), dict(albedo_offset=-a))
+            g = float(g_alb[m, c]); name = f"albedo[{m},{c}]"
+        else:
+            m = int(rng.choice(used))
+            r1 = rough0.copy(); r1[m] += h
+            r2 = rough0.copy(); r2[m] -= h
+            lp = (dict(roughness=r1), dict(roughness=r2))
+            g = float(g_rough[m]); name = f"roughness[{m}]"
+        vals = []
+        for kw in lp:
+            ctx.diff_set_params(**kw)
+            vals.append(float(np.sum((ctx.diff_render(spp, seed, depth) - target) ** 2)))
+        res.append((name, (vals[0] - vals[1]) / (2 * h), g))
+    fd_s = time.perf_counter() - t0
+    ctx.diff_set_params()
+    ctx.close()
+    fd = np.array([r[1] for r in res])
+    ad = np.array([r[2] for r in res])
+    rel = np.abs(ad - fd) / np.maximum(np.abs(fd), 1e-30)
+    scale = np.abs(fd).max()
+    significant = np.abs(fd) > 1e-3 * scale
+    paths = 512 * 512 * spp
+    return {
+        "study": "adjoint gradients vs central finite differences (h = 1e-3), fBm heightfield",
+        "workload": f"terrain {desc.ntris} tris, {nm} materials, env 512x256, 512x512, depth {depth}",
+        "loss": loss, "spp": spp, "target_spp": 256,
+        "primal_s": primal_s, "adjoint_s": adjoint_s, "target_s": target_s,
+        "primal_mpaths_per_s": paths / primal_s / 1e6, "adjoint_mpaths_per_s": paths / adjoint_s / 1e6,
+        "gradient_entries": int(g_env.size + g_alb.size + g_rough.size),
+        "fd_params": n_fd, "fd_s": fd_s,
+        "rel_err_median": float(np.median(rel)), "rel_err_max_significant": float(rel[significant].max()),
+        "frac_within_1e-3_rel": float(np.mean(rel <= 1e-3)),
+        "frac_significant_within_1e-3_rel": float(np.mean(rel[significant] <= 1e-3)),
+        "n_significant": int(significant.sum()),
+        "worst": sorted(res, key=lambda r: -abs(r[2] - r[1]) / max(abs(r[1]), 1e-30))[:5],
+    }
+
+
+def run_batch_study(args) -> dict:
+    """Batched rendering: `batch_scenes` Cornell-box scenes (the plain
+    configuration's generator) with triangle counts log-uniform in 1k-2M and
+    resolutions from {128^2, 256^2, 512^2, 1024^2}, 32 spp, depth 8, in one
+    persistent graph-captured launch (autotuned), against rendering the
+    scenes one after another with pgx_render; per-scene relMSE of the batch
+    image and of the reference CPU renderer's image (same spp) against a
+    converged GPU image, for the scenes small enough for the CPU."""
+    import time
+    from pathguidingdissertation_gb300 import abi, scenes
+    from pathguidingdissertation_gb300 import build as pkg_build
+    from pathguidingdissertation_gb300.api import Batch, Context
+
+    pkg_build.build()
+    rng = np.random.default_rng(0)
+    n = args.batch_scenes
+    spp, depth = 32, 8
+    specs = []
+    for i in range(n):
+        tris = int(np.exp(rng.uniform(np.log(1e3), np.log(2e6))))
+        res = int(rng.choice([128, 256, 512, 1024]))
+        specs.append(dict(seed=i + 1, width=res, height=res, target_tris=tris))
+    t0 = time.perf_counter()
+    descs = [scenes.cornell_box(**sp) for sp in specs]
+    gen_s = time.perf_counter() - t0
+    ctxs = []
+    build_ms = 0.0
+    for d in descs:
+        c = Context(0)
+        c.upload(d)
+        c.bvh_build()
+        build_ms += c.bvh_stats().build_ms
+        ctxs.append(c)
+    b = Batch(ctxs)
+    tuning = b.autotune(spp=1, max_depth=depth)
+    for c in ctxs:
+        c.clear()
+    b.render(spp, seed=1, max_depth=depth)
+    st = b.stats()
+    batch_ms = st.ms
+    paths = st.paths
+    # replay of the captured graph (another 32 spp), timed separately
+    imgs = [c.film()[0].astype(np.float64) / spp for c in ctxs]
+    b.render(spp, seed=2, max_depth=depth)
+    replay_ms = b.stats().ms
+    seq_ms = 0.0
+    for c in ctxs:
+        c.clear()
+        left = spp
+        while left > 0:
+            k = min(left, 256)
+            c.render(k, mode=abi.MODE_PLAIN, seed=1, max_depth=depth)
+            seq_ms += c.render_stats().ms_total
+            left -= k
+    per_scene = []
+    ref = None
+    try:
+        from oracle.ffi import Reference, reference_available
+        if reference_available():
+            ref = Reference(variant="plain_fast")
+    except Exception:
+        ref = None
+    for i, (sp, d, c) in enumerate(zip(specs, descs, ctxs)):
+        row = dict(tris=int(d.ntris), res=sp["width"])
+        if sp["width"] <= 256 and d.ntris <= 300_000:
+            c.clear()
+            c.render(1024, mode=abi.MODE_PLAIN, seed=77, max_depth=depth)
+            conv = c.film()[0].astype(np.float64) / 1024
+            row["relmse_batch"] = relmse(imgs[i], conv)
+            if ref is not None:
+                rs = ref.scene(d, threads=os.cpu_count() or 1)
+                film, _, _ = rs.render_pcg(False, 1, 0, spp, threads=os.cpu_count() or 1)
+                rs.close()
+                row["relmse_reference_cpu"] = relmse(film.astype(np.float64) / spp, conv)
+        per_scene.append(row)
+    b.close()
+    for c in ctxs:
+        c.close()
+    rows = [r for r in per_scene if "relmse_reference_cpu" in r]
+    ratio = [r["relmse_batch"] / r["relmse_reference_cpu"] for r in rows if r["relmse_reference_cpu"] > 0]
+    return {
+        "study": "batched wavefront rendering: one persistent graph-captured launch over many scenes",
+        "scenes": n, "spp": spp, "max_depth": depth, "paths": int(paths),
+        "triangles_total": int(sum(d.ntris for d in descs)),
+        "tuning": {"wave_paths": tuning.wave_paths, "trace_blocks_per_sm": tuning.trace_blocks_per_sm,
+                   "shade_blocks_per_sm": tuning.shade_blocks_per_sm},
+        "batch_ms": batch_ms, "batch_mpaths_per_s": paths / batch_ms / 1e3,
+        "graph_replay_ms": replay_ms, "graph_replay_mpaths_per_s": paths / replay_ms / 1e3,
+        "sequential_ms": seq_ms, "sequential_mpaths_per_s": paths / seq_ms / 1e3,
+        "scene_generation_s": gen_s, "bvh_build_ms_total": build_ms,
+        "relmse_checked_scenes": len(rows),
+        "relmse_batch_over_reference_median": float(np.median(ratio)) if ratio else None,
+        "per_scene": per_scene,
+    }
+
+
 def run_traversal_study(args) -> dict:
     """Incoherent secondary-ray closest-hit traversal on the ~2M-triangle
     interior: 10^7 rays whose origins are 1-spp first hits and whose
@@ -524,7 +713,7 @@ def main() -> None:
     ap.add_argument("--mode", choices=["plain", "guided_quadtree"], default="plain")
     ap.add_argument("--workload", choices=["interior", "cornell"], default="interior")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--study", choices=["relmse", "traversal"], default=None,
+    ap.add_argument("--study", choices=["relmse", "traversal", "adjoint", "batch"], default=None,
                     help="instead of the throughput line, run the equal-time relMSE study")
     ap.add_argument("--study-res", default="640x360")
     ap.add_argument("--ref-spp", type=int, default=16384)
@@ -538,6 +727,8 @@ def main() -> None:
     ap.add_argument("--mlp-decay", type=float, default=0.998)
     ap.add_argument("--mlp-steps", type=int, default=4)
     ap.add_argument("--trav-rays", type=int, default=10_000_000)
+    ap.add_argument("--fd-params", type=int, default=256)
+    ap.add_argument("--batch-scenes", type=int, default=64)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     if args.gpus != 1 or int(os.environ.get("WORLD_SIZE", "1")) != 1:
@@ -552,6 +743,12 @@ def main() -> None:
         return
     if args.study == "traversal":
         print(json.dumps(run_traversal_study(args)))
+        return
+    if args.study == "adjoint":
+        print(json.dumps(run_adjoint_study(args)))
+        return
+    if args.study == "batch":
+        print(json.dumps(run_batch_study(args)))
         return
     out = run_reference(args) if args.impl == "reference" else run_pgx(args)
     print(json.dumps(out))

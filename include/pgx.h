@@ -464,6 +464,48 @@ int pgx_diff_render(pgx_ctx* ctx, int32_t spp, uint64_t seed, int32_t max_depth,
 int pgx_diff_adjoint(pgx_ctx* ctx, int32_t spp, uint64_t seed, int32_t max_depth, const float* dloss_dimage,
                      float* grad_env, float* grad_albedo, float* grad_roughness);
 
+/* ---- batched rendering (extension) ----------------------------------------
+ * Renders many independent scenes -- each uploaded into its own context on
+ * the same device, with its BVH built -- as one wavefront: their traversal
+ * nodes, triangles, shading data, materials, textures and area lights are
+ * merged into one set of arrays at pgx_batch_create, and a render runs the
+ * extend / shade / shadow pipeline over waves of (scene, pixel, sample)
+ * items whose paths share the queues and every launch; each path starts
+ * traversal at its scene's root and samples its scene's lights.  Paths use
+ * PGX_MODE_PLAIN's estimator (NEE + MIS, box filter) and the PCG32 key
+ * (seed, pixel, sample) of pgx_render, so a scene's image equals
+ * pgx_render's for the same seed.  The waves of one call are captured in
+ * one CUDA graph, replayed while spp, max_depth and the tuning stay the
+ * same.  Scenes with an environment map are rejected (area lights only). */
+typedef struct pgx_batch pgx_batch;
+
+typedef struct pgx_batch_tuning {
+    int64_t wave_paths;           /* queue capacity: paths per wave            */
+    int32_t trace_blocks_per_sm;  /* persistent traversal blocks per SM (1-8)  */
+    int32_t shade_blocks_per_sm;  /* camera / shade / splat blocks per SM      */
+} pgx_batch_tuning;
+
+typedef struct pgx_batch_stats {
+    int64_t paths;          /* items of the last pgx_batch_render           */
+    double ms;              /* its device time                              */
+    int32_t graph_replayed; /* 1 when the captured graph was replayed       */
+} pgx_batch_stats;
+
+/* The contexts must outlive the batch; their films accumulate.  Geometry
+ * changed after creation is not seen (the arrays are copied). */
+int pgx_batch_create(pgx_ctx* const* scenes, int32_t n, pgx_batch** out);
+int pgx_batch_destroy(pgx_batch* batch);
+/* Adds spp samples per pixel to every scene's film. */
+int pgx_batch_render(pgx_batch* batch, int32_t spp, uint64_t seed, int32_t max_depth);
+/* Times every candidate tuning (wave capacity 1M-8M paths, traversal and
+ * shading grid sizes) on `spp` samples of the batch into a scratch film
+ * (the scenes' films are not touched), keeps the fastest and returns it.
+ * The traversal stack depth is fixed at 64 entries, as in the reference. */
+int pgx_batch_autotune(pgx_batch* batch, int32_t spp, int32_t max_depth, pgx_batch_tuning* best);
+int pgx_batch_set_tuning(pgx_batch* batch, const pgx_batch_tuning* tuning);
+int pgx_batch_get_stats(pgx_batch* batch, pgx_batch_stats* stats);
+const char* pgx_batch_last_error(pgx_batch* batch);
+
 #ifdef __cplusplus
 }
 #endif

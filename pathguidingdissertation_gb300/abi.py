@@ -95,6 +95,14 @@ class CacheStats(C.Structure):
                 ("mean_leaf_depth", C.c_double), ("build_ms", C.c_double)]
 
 
+class BatchTuning(C.Structure):
+    _fields_ = [("wave_paths", C.c_int64), ("trace_blocks_per_sm", C.c_int32), ("shade_blocks_per_sm", C.c_int32)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("paths", C.c_int64), ("ms", C.c_double), ("graph_replayed", C.c_int32)]
+
+
 _P = C.c_void_p
 _I64 = C.c_int64
 _I32 = C.c_int32
@@ -145,6 +153,13 @@ SIGNATURES = {
     "pgx_diff_set_params": (C.c_int, [_P, _P, _P, _P]),
     "pgx_diff_render": (C.c_int, [_P, _I32, C.c_uint64, _I32, _P]),
     "pgx_diff_adjoint": (C.c_int, [_P, _I32, C.c_uint64, _I32, _P, _P, _P, _P]),
+    "pgx_batch_create": (C.c_int, [_P, _I32, C.POINTER(_P)]),
+    "pgx_batch_destroy": (C.c_int, [_P]),
+    "pgx_batch_render": (C.c_int, [_P, _I32, C.c_uint64, _I32]),
+    "pgx_batch_autotune": (C.c_int, [_P, _I32, _I32, C.POINTER(BatchTuning)]),
+    "pgx_batch_set_tuning": (C.c_int, [_P, C.POINTER(BatchTuning)]),
+    "pgx_batch_get_stats": (C.c_int, [_P, C.POINTER(BatchStats)]),
+    "pgx_batch_last_error": (C.c_char_p, [_P]),
 }
 
 _lib: C.CDLL | None = None

@@ -311,6 +311,53 @@ class Context:
         return idx, d2
 
 
+class Batch:
+    """Many scenes (one Context each, same device) rendered by one persistent,
+    graph-captured launch (pgx_batch_*)."""
+
+    def __init__(self, contexts: list[Context]):
+        self.contexts = list(contexts)
+        self.lib = abi.load()
+        arr = (C.c_void_p * len(self.contexts))(*[c.h for c in self.contexts])
+        h = C.c_void_p()
+        rc = self.lib.pgx_batch_create(arr, len(self.contexts), C.byref(h))
+        if rc != 0:
+            raise PgxError(rc, "pgx_batch_create failed (scenes need a BVH, area lights and no environment map)")
+        self.h = h
+
+    def check(self, rc: int) -> None:
+        if rc != 0:
+            raise PgxError(rc, self.lib.pgx_batch_last_error(self.h).decode())
+
+    def render(self, spp: int, seed: int = 1, max_depth: int = 8) -> None:
+        self.check(self.lib.pgx_batch_render(self.h, spp, seed, max_depth))
+
+    def autotune(self, spp: int = 1, max_depth: int = 8) -> abi.BatchTuning:
+        t = abi.BatchTuning()
+        self.check(self.lib.pgx_batch_autotune(self.h, spp, max_depth, C.byref(t)))
+        return t
+
+    def set_tuning(self, wave_paths: int, trace_blocks_per_sm: int, shade_blocks_per_sm: int) -> None:
+        t = abi.BatchTuning(wave_paths, trace_blocks_per_sm, shade_blocks_per_sm)
+        self.check(self.lib.pgx_batch_set_tuning(self.h, C.byref(t)))
+
+    def stats(self) -> abi.BatchStats:
+        s = abi.BatchStats()
+        self.check(self.lib.pgx_batch_get_stats(self.h, C.byref(s)))
+        return s
+
+    def close(self) -> None:
+        if self.h:
+            self.lib.pgx_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def camera_struct(c: dict) -> abi.Camera:
     return abi.Camera((C.c_float * 3)(*c["from_"]), (C.c_float * 3)(*c["to"]), (C.c_float * 3)(*c["up"]),
                       float(c["fov"]), int(c["width"]), int(c["height"]), int(c.get("flip_x", 0)))

@@ -124,6 +124,8 @@ struct pgx_ctx {
     DevBuf mats;               // DevMaterial[nmats]
     DevBuf textures;           // DevTexture[ntex]
     DevBuf texels;             // float3 pool
+    int32_t ntex = 0;
+    int64_t ntexels = 0;       // float3 entries of the pool
     DevBuf lights;             // DevAreaLight[n_area_lights]
     std::vector<pgx_material> host_mats;
     DevCamera camera{};

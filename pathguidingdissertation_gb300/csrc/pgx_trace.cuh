@@ -155,8 +155,8 @@ struct TraceLane {
     bool finite;  // every component of inv is finite (see ray_box_finite)
 };
 
-// Starts a ray; returns false when the root box is missed (finished).
-__device__ __forceinline__ bool lane_start(const BvhView& bvh, TraceLane& L, xv3 o, xv3 d, float tmax) {
+// Starts a ray at `root`; returns false when the root box is missed (finished).
+__device__ __forceinline__ bool lane_start(const TravRoot& root, TraceLane& L, xv3 o, xv3 d, float tmax) {
     L.o = o;
     L.d = d;
     L.tmax = tmax;
@@ -166,18 +166,22 @@ __device__ __forceinline__ bool lane_start(const BvhView& bvh, TraceLane& L, xv3
     L.sp = 0;
     L.k = 0;
     L.status = 0;
-    if (!bvh.root.valid) return false;
+    if (!root.valid) return false;
     L.inv = mk(x_div(1.f, d.x), x_div(1.f, d.y), x_div(1.f, d.z));
     L.finite = isfinite(L.inv.x) && isfinite(L.inv.y) && isfinite(L.inv.z);
     float tb;
-    if (!ray_box(bvh.root.bmin[0], bvh.root.bmin[1], bvh.root.bmin[2], bvh.root.bmax[0], bvh.root.bmax[1],
-                 bvh.root.bmax[2], o, L.inv, tb))
+    if (!ray_box(root.bmin[0], root.bmin[1], root.bmin[2], root.bmax[0], root.bmax[1], root.bmax[2], o, L.inv, tb))
         return false;
     if (tb > tmax) return false;
-    L.ref = bvh.root.ref;
-    L.cnt = bvh.root.count;
+    L.ref = root.ref;
+    L.cnt = root.count;
     return true;
 }
+
+// The tree's own root for every ray (one scene).
+struct SceneRoot {
+    __device__ __forceinline__ const TravRoot& operator()(unsigned, const BvhView& bvh) const { return bvh.root; }
+};
 
 // One step; returns true when the ray is finished (for ANY, hit_id >= 0
 // marks an occluder).
@@ -268,12 +272,14 @@ __device__ __forceinline__ bool lane_step(const BvhView& bvh, TraceLane& L, int2
 }
 
 // Persistent warp loop over rays [0, n): `load(i, o, d, tmax)` fetches ray i,
-// `store(i, lane)` consumes a finished ray.  `next` is a zeroed counter.
-// Must be called by whole warps (all 32 lanes).
-template <bool ANY, bool COUNT, class Load, class Store>
+// `store(i, lane)` consumes a finished ray, `root_of(i, bvh)` gives the tree
+// root ray i starts from (several trees can share the node and triangle
+// arrays).  `next` is a zeroed counter.  Must be called by whole warps.
+template <bool ANY, bool COUNT, class Load, class Store, class RootOf = SceneRoot>
 __device__ __forceinline__ void trace_persistent(const BvhView& bvh, unsigned n, unsigned* next, Load load,
                                                  Store store, unsigned long long& n_interior,
-                                                 unsigned long long& n_tris, unsigned& status_or) {
+                                                 unsigned long long& n_tris, unsigned& status_or,
+                                                 RootOf root_of = RootOf()) {
     constexpr unsigned kFull = 0xFFFFFFFFu;
     constexpr int kRefillBelow = 24;  // refill when fewer lanes than this are busy
     constexpr int kMaxSteps = 64;
@@ -298,7 +304,7 @@ __device__ __forceinline__ void trace_persistent(const BvhView& bvh, unsigned n,
                     xv3 o, d;
                     float tmax;
                     load(idx, o, d, tmax);
-                    if (lane_start(bvh, L, o, d, tmax)) {
+                    if (lane_start(root_of(idx, bvh), L, o, d, tmax)) {
                         ray = (int)idx;
                     } else {
                         store(idx, L);  // missed the root: finished

@@ -26,6 +26,8 @@
 #include <vector>
 
 #include "pgx_ctx.h"
+#include <cstdarg>
+
 #include "pgx_guide.cuh"
 #include "pgx_mlp.cuh"
 #include "pgx_shade.cuh"
@@ -78,13 +80,14 @@ struct PathState {
     float* train;     // radiance samples, 13 floats each
     unsigned* ntrain;
     int64_t tcapacity;
+    int* scene;       // batched rendering: scene of each path
 };
 
 struct RenderState {
     DevBuf o, d, T, L, hit, pix, rng, flags, nrec, q0, q1, sh_path, sh_o, sh_d, sh_c;
     DevBuf rec_pos, rec_nrm, rec_wi, rec_w, rec_e;
     DevBuf counters, vertices;
-    DevBuf guide, rec_wo, rec_f, train;
+    DevBuf guide, rec_wo, rec_f, train, scene;
     int64_t capacity = 0;
     int rec_depth = 0;
     int64_t guide_capacity = 0;
@@ -135,6 +138,38 @@ struct FrameParams {
     float train_keep;  // probability of keeping one radiance sample
 };
 
+// Batched rendering: what differs between the scenes of a batch whose
+// node, triangle, shading, material, texture and light arrays are merged
+// into one set (pgx_batch_create).
+struct BatchInfo {
+    TravRoot root;        // the scene's tree in the merged node array
+    int light_base;       // its area lights in the merged light array
+    int n_lights;
+    DevCamera cam;
+    SceneBoundsDev bounds;
+    int width, height;
+    float* film;
+    int spp0;             // samples already in the film
+    int64_t npix;
+};
+
+struct BatchWave {
+    const BatchInfo* __restrict__ info;
+    const int64_t* __restrict__ prefix;  // items before scene s (items = pixels x spp)
+    int n;
+    int64_t base, count;                 // this wave's items
+    const uint64_t* seed;
+};
+
+__device__ __forceinline__ int batch_scene_of(const BatchWave& bw, int64_t item) {
+    int lo = 0, hi = bw.n - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (bw.prefix[mid] <= item) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
 // Camera::generateRay (Scene.h:45-57) direction for film position (px, py).
 __device__ __forceinline__ F3 camera_dir(const DevCamera& cam, float px, float py) {
     float xc = (2.f * px / cam.width) - 1.f;
@@ -179,6 +214,44 @@ __global__ void __launch_bounds__(kThreads) k_camgen(SceneView sv, PathState ps,
     if (blockIdx.x == 0 && threadIdx.x == 0) ps.qcount[0] = (unsigned)n;
 }
 
+// Camera rays of one wave of a batch: item -> (scene, pixel, sample), the
+// same PCG32 key and draws as k_camgen.
+__global__ void __launch_bounds__(kThreads) k_camgen_batch(PathState ps, BatchWave bw) {
+    const uint64_t seed = *bw.seed;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < bw.count; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t item = bw.base + i;
+        const int sc = batch_scene_of(bw, item);
+        const BatchInfo& bi = bw.info[sc];
+        const int64_t local = item - bw.prefix[sc];
+        const int64_t pixel = local % bi.npix;
+        const int sample = bi.spp0 + (int)(local / bi.npix);
+        int xpix = (int)(pixel % bi.width), ypix = (int)(pixel / bi.width);
+        uint64_t rng = pgx_rng_init(seed, (uint64_t)pixel, (uint64_t)sample);
+        float px = (float)xpix + pgx_rng_next(rng);
+        float py = (float)ypix + pgx_rng_next(rng);
+        F3 dir = camera_dir(bi.cam, px, py);
+        ps.o[i] = make_float4(bi.cam.origin[0], bi.cam.origin[1], bi.cam.origin[2], 0.f);
+        ps.d[i] = make_float4(dir.x, dir.y, dir.z, 0.f);
+        ps.T[i] = make_float4(1.f, 1.f, 1.f, 0.f);
+        ps.L[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        ps.pix[i] = make_float2(px, py);
+        ps.rng[i] = rng;
+        ps.flags[i] = 0;
+        ps.nrec[i] = 0;
+        ps.scene[i] = sc;
+        ps.queue[0][i] = (int)i;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) ps.qcount[0] = (unsigned)bw.count;
+}
+
+// Root of a batched path's scene (RootOf of trace_persistent).
+struct BatchRoot {
+    const BatchInfo* info;
+    const int* scene;
+    const int* path;  // queue entry -> path index
+    __device__ __forceinline__ TravRoot operator()(unsigned i, const BvhView&) const { return info[scene[path[i]]].root; }
+};
+
 // ---- closest hit for the queue of this depth ----------------------------------
 __device__ __forceinline__ void add_counts(unsigned long long* dst, unsigned long long a, unsigned long long b) {
     for (int o = 16; o > 0; o >>= 1) {
@@ -195,8 +268,9 @@ constexpr int kPersistentBlocksPerSM = 8;
 
 // Closest hit for the queue of this depth: persistent warps with lane refill
 // (trace_persistent) over qcount[depth] rays.
-template <bool COUNT>
-__global__ void __launch_bounds__(kThreads, kPersistentBlocksPerSM) k_extend(SceneView sv, PathState ps, int depth) {
+template <bool COUNT, bool BATCH = false>
+__global__ void __launch_bounds__(kThreads, kPersistentBlocksPerSM) k_extend(SceneView sv, PathState ps, int depth,
+                                                                            const BatchInfo* binfo = nullptr) {
     const unsigned n = ps.qcount[depth];
     const int* __restrict__ q = ps.queue[depth & 1];
     unsigned long long ni = 0, nt = 0;
@@ -213,15 +287,20 @@ __global__ void __launch_bounds__(kThreads, kPersistentBlocksPerSM) k_extend(Sce
         int id = L.status ? -1 : L.hit_id;  // corrupt tree or stack overflow: a miss
         ps.hit[p] = make_float4(__int_as_float(id), L.tmax, L.hu, L.hv);
     };
-    trace_persistent<false, COUNT>(sv.bvh, n, &ps.wcount[depth], load, store, ni, nt, status);
+    if (BATCH)
+        trace_persistent<false, COUNT>(sv.bvh, n, &ps.wcount[depth], load, store, ni, nt, status,
+                                       BatchRoot{binfo, ps.scene, q});
+    else
+        trace_persistent<false, COUNT>(sv.bvh, n, &ps.wcount[depth], load, store, ni, nt, status);
     if (COUNT) add_counts(&ps.stats[2], ni, nt);
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ps.stats[0], (unsigned long long)n);
 }
 
 // Any hit for the shadow queue of this depth; unoccluded rays add their
 // contribution to the path's radiance.
-template <bool COUNT>
-__global__ void __launch_bounds__(kThreads, kPersistentBlocksPerSM) k_shadow(SceneView sv, PathState ps, int depth) {
+template <bool COUNT, bool BATCH = false>
+__global__ void __launch_bounds__(kThreads, kPersistentBlocksPerSM) k_shadow(SceneView sv, PathState ps, int depth,
+                                                                            const BatchInfo* binfo = nullptr) {
     const unsigned n = ps.scount[depth];
     unsigned long long ni = 0, nt = 0;
     unsigned status = 0;
@@ -239,7 +318,11 @@ __global__ void __launch_bounds__(kThreads, kPersistentBlocksPerSM) k_shadow(Sce
             ps.L[p] = make_float4(l.x + c.x, l.y + c.y, l.z + c.z, 0.f);
         }
     };
-    trace_persistent<true, COUNT>(sv.bvh, n, &ps.wcount[kMaxDepthCap + 2 + depth], load, store, ni, nt, status);
+    if (BATCH)
+        trace_persistent<true, COUNT>(sv.bvh, n, &ps.wcount[kMaxDepthCap + 2 + depth], load, store, ni, nt, status,
+                                      BatchRoot{binfo, ps.scene, ps.sh_path});
+    else
+        trace_persistent<true, COUNT>(sv.bvh, n, &ps.wcount[kMaxDepthCap + 2 + depth], load, store, ni, nt, status);
     if (COUNT) add_counts(&ps.stats[4], ni, nt);
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ps.stats[1], (unsigned long long)n);
 }
@@ -477,9 +560,9 @@ __device__ __forceinline__ void push_shadow(PathState& ps, int depth, int p, flo
     }
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(kThreads, 8) k_shade(SceneView sv, PathState ps, FrameParams fp, int depth,
-                                                    GuideView gv) {
+template <int MODE, bool BATCH = false>
+__global__ void __launch_bounds__(kThreads, 8) k_shade(SceneView sv0, PathState ps, FrameParams fp, int depth,
+                                                    GuideView gv, const BatchInfo* binfo = nullptr) {
     const unsigned n = ps.qcount[depth];
     const int* __restrict__ q = ps.queue[depth & 1];
     int* __restrict__ qn = ps.queue[(depth + 1) & 1];
@@ -495,6 +578,21 @@ __global__ void __launch_bounds__(kThreads, 8) k_shade(SceneView sv, PathState p
         float4 so = make_float4(0.f, 0.f, 0.f, 0.f), sdir = so;
         F3 sc = zero3();
         int p = active ? q[i] : 0;
+        SceneView svb;
+        if (BATCH) {
+            // the path's scene: its lights and bounds in the merged arrays
+            svb = sv0;
+            if (active) {
+                const BatchInfo& bi = binfo[ps.scene[p]];
+                svb.lights = sv0.lights + bi.light_base;
+                svb.nlights = bi.n_lights;
+                svb.n_area_lights = bi.n_lights;
+                svb.bounds = bi.bounds;
+                svb.width = bi.width;
+                svb.height = bi.height;
+            }
+        }
+        const SceneView& sv = BATCH ? svb : sv0;
         // Recording for the cache outside guided-Li: the radiance the path has
         // gathered up to here (after the previous vertex's NEE) is the
         // baseline from which k_finalize recovers that vertex's incident Li.
@@ -1259,6 +1357,18 @@ __global__ void __launch_bounds__(kThreads) k_diff_adjoint(SceneView sv, DiffVie
     }
 }
 
+// End of a batch wave: NaN/Inf drop and the box-filter splat into each
+// path's scene film.
+__global__ void __launch_bounds__(kThreads) k_finalize_batch(PathState ps, BatchWave bw) {
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < bw.count; p += (int64_t)gridDim.x * blockDim.x) {
+        F3 col = f3(ps.L[p]);
+        if (!valid(col)) continue;
+        const BatchInfo& bi = bw.info[ps.scene[p]];
+        float2 xy = ps.pix[p];
+        splat(bi.film, nullptr, bi.width, bi.height, xy.x, xy.y, col, false);
+    }
+}
+
 inline unsigned grid_for(int64_t n) {
     int64_t b = (n + kThreads - 1) / kThreads;
     return (unsigned)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 16));
@@ -1270,7 +1380,7 @@ RenderState* state_of(pgx_ctx* ctx) {
 }
 
 int ensure_state(pgx_ctx* ctx, RenderState* rs, int64_t cap, int rec_depth, int64_t vcap, bool guide = false,
-                 int train_depth = 0, int64_t tcap = 0) {
+                 int train_depth = 0, int64_t tcap = 0, bool batch = false) {
     if (cap > rs->capacity) {
         PGX_CUDA_TRY(ctx, rs->o.reserve(sizeof(float4) * cap));
         PGX_CUDA_TRY(ctx, rs->d.reserve(sizeof(float4) * cap));
@@ -1317,6 +1427,7 @@ int ensure_state(pgx_ctx* ctx, RenderState* rs, int64_t cap, int rec_depth, int6
         PGX_CUDA_TRY(ctx, rs->train.reserve(sizeof(float) * 13 * tcap));
         rs->tcapacity = tcap;
     }
+    if (batch) PGX_CUDA_TRY(ctx, rs->scene.reserve(sizeof(int) * rs->capacity));
     PGX_CUDA_TRY(ctx, rs->counters.reserve(sizeof(unsigned) * 4 * (kMaxDepthCap + 2) + sizeof(unsigned long long) * kStats +
                                            sizeof(unsigned) * 4));
     if (!rs->ev0) {
@@ -1364,6 +1475,7 @@ PathState path_view(RenderState* rs) {
     ps.train = rs->train.as<float>();
     ps.ntrain = c + 4 * (kMaxDepthCap + 2) + 2 * kStats + 1;
     ps.tcapacity = rs->tcapacity;
+    ps.scene = rs->scene.as<int>();
     return ps;
 }
 
@@ -1831,5 +1943,365 @@ extern "C" int pgx_diff_adjoint(pgx_ctx* ctx, int32_t spp, uint64_t seed, int32_
     if (grad_roughness && nm)
         PGX_CUDA_TRY(ctx, cudaMemcpyAsync(grad_roughness, rs->d_grough.p, sizeof(float) * nm, cudaMemcpyDeviceToHost, s));
     PGX_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    return PGX_OK;
+}
+
+// ---- batched rendering ----------------------------------------------------------------------
+// pgx_batch_create merges the scenes' traversal nodes, triangles, shading
+// records, materials, textures and area lights into one set of arrays held
+// by an internal context (child references, triangle ids, material,
+// texture and texel indexes shifted by each scene's base) and keeps per
+// scene its root, light range, camera, bounds and film (BatchInfo).  A
+// render runs the wavefront pipeline over waves of (scene, pixel, sample)
+// items: paths of all scenes share the queues and every launch, and each
+// path finds its tree root and lights through its scene index.  The waves
+// of one call are captured in one CUDA graph.
+namespace {
+
+__global__ void k_merge_nodes(TravNode* n, int64_t cnt, int rec_base, int tri_base) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += (int64_t)gridDim.x * blockDim.x) {
+        TravNode t = n[i];
+        int lc = __float_as_int(t.lmax.w), rc = __float_as_int(t.rmax.w);
+        t.lmin.w = __int_as_float(__float_as_int(t.lmin.w) + (lc > 0 ? tri_base : rec_base));
+        t.rmin.w = __int_as_float(__float_as_int(t.rmin.w) + (rc > 0 ? tri_base : rec_base));
+        n[i] = t;
+    }
+}
+__global__ void k_merge_tris(TravTri* t, int64_t cnt, int tri_base) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += (int64_t)gridDim.x * blockDim.x)
+        t[i].v0.w = __int_as_float(__float_as_int(t[i].v0.w) + tri_base);
+}
+__global__ void k_merge_shade(TriShade* sh, int64_t cnt, int mat_base) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += (int64_t)gridDim.x * blockDim.x)
+        sh[i].vv.w = __int_as_float(__float_as_int(sh[i].vv.w) + mat_base);
+}
+__global__ void k_merge_mats(DevMaterial* m, int cnt, int tex_base) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) m[i].tex += tex_base;
+}
+__global__ void k_merge_textures(DevTexture* t, int cnt, long long texel_base) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) t[i].offset += texel_base;
+}
+__global__ void k_merge_lights(DevAreaLight* l, int cnt, int tri_base) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x)
+        l[i].p1.w = __int_as_float(__float_as_int(l[i].p1.w) + tri_base);
+}
+
+}  // namespace
+
+struct pgx_batch {
+    std::vector<pgx_ctx*> ctx;
+    pgx_ctx* host = nullptr;        // merged arrays, stream, error text, path state
+    std::vector<BatchInfo> info;    // per scene (roots and bases fixed at creation)
+    DevBuf d_info, d_prefix, d_seed;
+    pgx_batch_tuning tuning{1 << 22, 8, 16};
+    pgx_batch_stats stats{};
+    cudaGraphExec_t graph = nullptr;
+    int g_spp = -1, g_depth = -1;
+    pgx_batch_tuning g_tuning{};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int sms = 0;
+};
+
+namespace {
+
+int batch_fail(pgx_batch* b, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    b->host->err = buf;
+    return code;
+}
+
+bool tuning_ok(const pgx_batch_tuning& t) {
+    return t.wave_paths >= (1 << 16) && t.wave_paths <= (1LL << 25) && t.trace_blocks_per_sm >= 1 &&
+           t.trace_blocks_per_sm <= kPersistentBlocksPerSM && t.shade_blocks_per_sm >= 1 && t.shade_blocks_per_sm <= 16;
+}
+
+// Per-scene tables for `spp` samples; films of the scenes, or one scratch
+// film for all (autotuning).
+int batch_tables(pgx_batch* b, int spp, float* scratch) {
+    const int n = (int)b->ctx.size();
+    std::vector<BatchInfo> t = b->info;
+    std::vector<int64_t> prefix((size_t)n + 1, 0);
+    for (int i = 0; i < n; i++) {
+        pgx_ctx* c = b->ctx[(size_t)i];
+        if (ensure_film(c) != PGX_OK) return batch_fail(b, PGX_ERR_CUDA, "%s", c->err.c_str());
+        t[(size_t)i].film = scratch ? scratch : c->film.as<float>();
+        t[(size_t)i].spp0 = c->spp;
+        prefix[(size_t)i + 1] = prefix[(size_t)i] + t[(size_t)i].npix * spp;
+    }
+    cudaStream_t s = b->host->stream;
+    PGX_CUDA_TRY(b->host, cudaMemcpyAsync(b->d_info.p, t.data(), sizeof(BatchInfo) * (size_t)n, cudaMemcpyHostToDevice, s));
+    PGX_CUDA_TRY(b->host, cudaMemcpyAsync(b->d_prefix.p, prefix.data(), sizeof(int64_t) * (size_t)(n + 1),
+                                          cudaMemcpyHostToDevice, s));
+    PGX_CUDA_TRY(b->host, cudaStreamSynchronize(s));
+    b->stats.paths = prefix[(size_t)n];
+    return PGX_OK;
+}
+
+// Enqueues every wave of one call: camera rays, (extend, shade, shadow) per
+// depth, splat.
+int batch_enqueue(pgx_batch* b, int64_t total, int depth, const pgx_batch_tuning& tu) {
+    pgx_ctx* h = b->host;
+    RenderState* rs = state_of(h);
+    SceneView sv = scene_view(h);
+    PathState ps = path_view(rs);
+    GuideView gv{};
+    const BatchInfo* info = b->d_info.as<BatchInfo>();
+    cudaStream_t s = h->stream;
+    FrameParams fp{};
+    fp.mode = PGX_MODE_PLAIN;
+    fp.max_depth = depth;
+    fp.batch = 1;
+    const unsigned tg = (unsigned)(b->sms * tu.trace_blocks_per_sm);
+    const unsigned sg = (unsigned)(b->sms * tu.shade_blocks_per_sm);
+    for (int64_t base = 0; base < total; base += tu.wave_paths) {
+        BatchWave bw{info, b->d_prefix.as<int64_t>(), (int)b->ctx.size(), base, std::min<int64_t>(tu.wave_paths, total - base),
+                     b->d_seed.as<uint64_t>()};
+        cudaMemsetAsync(ps.qcount, 0, sizeof(unsigned) * 4 * (kMaxDepthCap + 2), s);
+        k_camgen_batch<<<sg, kThreads, 0, s>>>(ps, bw);
+        for (int d = 0; d <= depth; d++) {
+            k_extend<false, true><<<tg, kThreads, 0, s>>>(sv, ps, d, info);
+            k_shade<PGX_MODE_PLAIN, true><<<sg, kThreads, 0, s>>>(sv, ps, fp, d, gv, info);
+            k_shadow<false, true><<<tg, kThreads, 0, s>>>(sv, ps, d, info);
+        }
+        k_finalize_batch<<<sg, kThreads, 0, s>>>(ps, bw);
+    }
+    PGX_CUDA_TRY(h, cudaGetLastError());
+    return PGX_OK;
+}
+
+int batch_state(pgx_batch* b, const pgx_batch_tuning& tu) {
+    return ensure_state(b->host, state_of(b->host), tu.wave_paths, 0, 0, false, 0, 0, true);
+}
+
+}  // namespace
+
+extern "C" int pgx_batch_create(pgx_ctx* const* scenes, int32_t n, pgx_batch** out) {
+    if (!out) return PGX_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (!scenes || n <= 0) return PGX_ERR_INVALID_ARG;
+    int64_t recs = 0, tris = 0, texels = 0;
+    int64_t mats = 0, texs = 0, lights = 0;
+    for (int32_t i = 0; i < n; i++) {
+        pgx_ctx* c = scenes[i];
+        if (!c || c->device != scenes[0]->device) return PGX_ERR_INVALID_ARG;
+        if (!c->has_scene || !c->has_bvh) return PGX_ERR_STATE;
+        if (c->env.valid || c->n_area_lights == 0) return PGX_ERR_INVALID_ARG;
+        recs += c->n_records;
+        tris += c->ntris;
+        mats += c->nmats;
+        texs += c->ntex;
+        texels += c->ntexels;
+        lights += c->n_area_lights;
+    }
+    if (recs >= INT32_MAX || tris >= INT32_MAX || texs >= INT32_MAX) return PGX_ERR_OVERFLOW;
+    pgx_batch* b = new pgx_batch();
+    b->ctx.assign(scenes, scenes + n);
+    b->host = new pgx_ctx();
+    pgx_ctx* h = b->host;
+    h->device = scenes[0]->device;
+    auto fail = [&](int code) {
+        pgx_batch_destroy(b);
+        return code;
+    };
+    if (cudaSetDevice(h->device) != cudaSuccess || cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess ||
+        cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, h->device) != cudaSuccess)
+        return fail(PGX_ERR_CUDA);
+    if (h->trav_nodes.reserve(sizeof(TravNode) * std::max<int64_t>(recs, 1)) != cudaSuccess ||
+        h->trav_tris.reserve(sizeof(TravTri) * tris) != cudaSuccess || h->shade.reserve(sizeof(TriShade) * tris) != cudaSuccess ||
+        h->mats.reserve(sizeof(DevMaterial) * mats) != cudaSuccess ||
+        h->textures.reserve(sizeof(DevTexture) * std::max<int64_t>(texs, 1)) != cudaSuccess ||
+        h->texels.reserve(sizeof(float) * 3 * std::max<int64_t>(texels, 1)) != cudaSuccess ||
+        h->lights.reserve(sizeof(DevAreaLight) * lights) != cudaSuccess || b->d_info.reserve(sizeof(BatchInfo) * n) != cudaSuccess ||
+        b->d_prefix.reserve(sizeof(int64_t) * (n + 1)) != cudaSuccess || b->d_seed.reserve(sizeof(uint64_t)) != cudaSuccess)
+        return fail(PGX_ERR_OOM);
+    cudaStream_t s = h->stream;
+    int64_t rb = 0, tb = 0, mb = 0, xb = 0, eb = 0, lb = 0;
+    b->info.resize((size_t)n);
+    for (int32_t i = 0; i < n; i++) {
+        pgx_ctx* c = scenes[i];
+        cudaStreamSynchronize(c->stream);
+        bool ok = cudaMemcpyAsync(h->trav_nodes.as<TravNode>() + rb, c->trav_nodes.p, sizeof(TravNode) * c->n_records,
+                                  cudaMemcpyDeviceToDevice, s) == cudaSuccess &&
+                  cudaMemcpyAsync(h->trav_tris.as<TravTri>() + tb, c->trav_tris.p, sizeof(TravTri) * c->ntris,
+                                  cudaMemcpyDeviceToDevice, s) == cudaSuccess &&
+                  cudaMemcpyAsync(h->shade.as<TriShade>() + tb, c->shade.p, sizeof(TriShade) * c->ntris,
+                                  cudaMemcpyDeviceToDevice, s) == cudaSuccess &&
+                  cudaMemcpyAsync(h->mats.as<DevMaterial>() + mb, c->mats.p, sizeof(DevMaterial) * c->nmats,
+                                  cudaMemcpyDeviceToDevice, s) == cudaSuccess &&
+                  cudaMemcpyAsync(h->textures.as<DevTexture>() + xb, c->textures.p, sizeof(DevTexture) * c->ntex,
+                                  cudaMemcpyDeviceToDevice, s) == cudaSuccess &&
+                  cudaMemcpyAsync(h->texels.as<float>() + 3 * eb, c->texels.p, sizeof(float) * 3 * c->ntexels,
+                                  cudaMemcpyDeviceToDevice, s) == cudaSuccess &&
+                  cudaMemcpyAsync(h->lights.as<DevAreaLight>() + lb, c->lights.p, sizeof(DevAreaLight) * c->n_area_lights,
+                                  cudaMemcpyDeviceToDevice, s) == cudaSuccess;
+        if (!ok) return fail(PGX_ERR_CUDA);
+        const unsigned g = 256;
+        if (c->n_records) k_merge_nodes<<<g, 256, 0, s>>>(h->trav_nodes.as<TravNode>() + rb, c->n_records, (int)rb, (int)tb);
+        k_merge_tris<<<g, 256, 0, s>>>(h->trav_tris.as<TravTri>() + tb, c->ntris, (int)tb);
+        k_merge_shade<<<g, 256, 0, s>>>(h->shade.as<TriShade>() + tb, c->ntris, (int)mb);
+        k_merge_mats<<<g, 256, 0, s>>>(h->mats.as<DevMaterial>() + mb, c->nmats, (int)xb);
+        k_merge_textures<<<g, 256, 0, s>>>(h->textures.as<DevTexture>() + xb, c->ntex, (long long)eb);
+        k_merge_lights<<<g, 256, 0, s>>>(h->lights.as<DevAreaLight>() + lb, c->n_area_lights, (int)tb);
+        BatchInfo& bi = b->info[(size_t)i];
+        bi = BatchInfo{};
+        bi.root = c->root;
+        bi.root.ref += (c->root.count > 0) ? (int)tb : (int)rb;
+        bi.light_base = (int)lb;
+        bi.n_lights = c->n_area_lights;
+        bi.cam = c->camera;
+        bi.bounds = c->bounds;
+        bi.width = c->width;
+        bi.height = c->height;
+        bi.npix = (int64_t)c->width * c->height;
+        rb += c->n_records;
+        tb += c->ntris;
+        mb += c->nmats;
+        xb += c->ntex;
+        eb += c->ntexels;
+        lb += c->n_area_lights;
+    }
+    if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) return fail(PGX_ERR_CUDA);
+    h->n_records = recs;
+    h->ntris = tris;
+    h->nmats = (int32_t)mats;
+    h->ntex = (int32_t)texs;
+    h->ntexels = texels;
+    h->n_area_lights = (int32_t)lights;
+    h->nlights = (int32_t)lights;
+    h->has_scene = true;
+    h->has_bvh = true;
+    h->root.valid = 0;  // every path starts from its scene's root
+    h->env.valid = 0;
+    h->width = h->height = 1;  // per-path sizes come from BatchInfo
+    *out = b;
+    return PGX_OK;
+}
+
+extern "C" int pgx_batch_destroy(pgx_batch* b) {
+    if (!b) return PGX_OK;
+    if (b->host) {
+        cudaSetDevice(b->host->device);
+        if (b->host->stream) cudaStreamSynchronize(b->host->stream);
+        if (b->graph) cudaGraphExecDestroy(b->graph);
+        if (b->ev0) cudaEventDestroy(b->ev0);
+        if (b->ev1) cudaEventDestroy(b->ev1);
+        b->d_info.release();
+        b->d_prefix.release();
+        b->d_seed.release();
+        render_state_free(b->host);
+        if (b->host->stream) cudaStreamDestroy(b->host->stream);
+        delete b->host;
+    }
+    delete b;
+    return PGX_OK;
+}
+
+extern "C" const char* pgx_batch_last_error(pgx_batch* b) { return (b && b->host) ? b->host->err.c_str() : "null batch"; }
+
+extern "C" int pgx_batch_set_tuning(pgx_batch* b, const pgx_batch_tuning* t) {
+    if (!b || !t) return PGX_ERR_INVALID_ARG;
+    if (!tuning_ok(*t)) return batch_fail(b, PGX_ERR_INVALID_ARG, "pgx_batch_set_tuning: out of range");
+    b->tuning = *t;
+    return PGX_OK;
+}
+
+extern "C" int pgx_batch_get_stats(pgx_batch* b, pgx_batch_stats* st) {
+    if (!b || !st) return PGX_ERR_INVALID_ARG;
+    *st = b->stats;
+    return PGX_OK;
+}
+
+extern "C" int pgx_batch_render(pgx_batch* b, int32_t spp, uint64_t seed, int32_t max_depth) {
+    if (!b) return PGX_ERR_INVALID_ARG;
+    pgx_ctx* h = b->host;
+    h->err.clear();
+    if (spp <= 0 || max_depth < 0 || max_depth > kMaxDepthCap)
+        return batch_fail(b, PGX_ERR_INVALID_ARG, "pgx_batch_render: bad spp or max_depth");
+    PGX_CUDA_TRY(h, cudaSetDevice(h->device));
+    for (pgx_ctx* c : b->ctx) PGX_CUDA_TRY(h, cudaStreamSynchronize(c->stream));
+    PGX_TRY(batch_state(b, b->tuning));
+    PGX_TRY(batch_tables(b, spp, nullptr));
+    PGX_CUDA_TRY(h, cudaMemcpyAsync(b->d_seed.p, &seed, sizeof(uint64_t), cudaMemcpyHostToDevice, h->stream));
+    const bool replay = b->graph && b->g_spp == spp && b->g_depth == max_depth &&
+                        b->g_tuning.wave_paths == b->tuning.wave_paths &&
+                        b->g_tuning.trace_blocks_per_sm == b->tuning.trace_blocks_per_sm &&
+                        b->g_tuning.shade_blocks_per_sm == b->tuning.shade_blocks_per_sm;
+    if (!replay) {
+        if (b->graph) cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+        cudaGraph_t g;
+        PGX_CUDA_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = batch_enqueue(b, b->stats.paths, max_depth, b->tuning);
+        cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
+        if (rc != PGX_OK) return rc;
+        PGX_CUDA_TRY(h, ec);
+        cudaError_t e = cudaGraphInstantiate(&b->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            b->graph = nullptr;
+            return batch_fail(b, PGX_ERR_CUDA, "pgx_batch_render: graph instantiation: %s", cudaGetErrorString(e));
+        }
+        b->g_spp = spp;
+        b->g_depth = max_depth;
+        b->g_tuning = b->tuning;
+    }
+    PGX_CUDA_TRY(h, cudaEventRecord(b->ev0, h->stream));
+    PGX_CUDA_TRY(h, cudaGraphLaunch(b->graph, h->stream));
+    PGX_CUDA_TRY(h, cudaEventRecord(b->ev1, h->stream));
+    PGX_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    float ms = 0.f;
+    PGX_CUDA_TRY(h, cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    b->stats.ms = ms;
+    b->stats.graph_replayed = replay ? 1 : 0;
+    for (pgx_ctx* c : b->ctx) c->spp += spp;
+    return PGX_OK;
+}
+
+extern "C" int pgx_batch_autotune(pgx_batch* b, int32_t spp, int32_t max_depth, pgx_batch_tuning* best) {
+    if (!b) return PGX_ERR_INVALID_ARG;
+    pgx_ctx* h = b->host;
+    h->err.clear();
+    if (spp <= 0 || max_depth < 0 || max_depth > kMaxDepthCap)
+        return batch_fail(b, PGX_ERR_INVALID_ARG, "pgx_batch_autotune: bad spp or max_depth");
+    PGX_CUDA_TRY(h, cudaSetDevice(h->device));
+    int64_t max_film = 0;
+    for (const BatchInfo& bi : b->info) max_film = std::max(max_film, bi.npix * 3);
+    DevBuf scratch;
+    PGX_CUDA_TRY(h, scratch.reserve(sizeof(float) * (size_t)max_film));
+    PGX_TRY(batch_tables(b, spp, scratch.as<float>()));
+    uint64_t seed = 0x5eedULL;
+    PGX_CUDA_TRY(h, cudaMemcpyAsync(b->d_seed.p, &seed, sizeof(uint64_t), cudaMemcpyHostToDevice, h->stream));
+    const int64_t total = b->stats.paths;
+    const int64_t waves[] = {1 << 20, 1 << 21, 1 << 22, 1 << 23};
+    const int trace_bps[] = {4, 8};
+    const int shade_bps[] = {8, 16};
+    float best_ms = 1e30f;
+    pgx_batch_tuning pick = b->tuning;
+    for (int64_t w : waves) {
+        if (w > 2 * total && w != waves[0]) continue;  // larger waves than the work change nothing
+        for (int tbp : trace_bps)
+            for (int sbp : shade_bps) {
+                pgx_batch_tuning t{w, tbp, sbp};
+                PGX_TRY(batch_state(b, t));
+                PGX_TRY(batch_enqueue(b, total, max_depth, t));  // warm-up
+                PGX_CUDA_TRY(h, cudaEventRecord(b->ev0, h->stream));
+                PGX_TRY(batch_enqueue(b, total, max_depth, t));
+                PGX_CUDA_TRY(h, cudaEventRecord(b->ev1, h->stream));
+                PGX_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+                float ms = 0.f;
+                PGX_CUDA_TRY(h, cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+                if (ms < best_ms) {
+                    best_ms = ms;
+                    pick = t;
+                }
+            }
+    }
+    b->tuning = pick;
+    if (best) *best = pick;
     return PGX_OK;
 }

@@ -284,6 +284,8 @@ extern "C" int pgx_scene_upload(pgx_ctx* ctx, const pgx_triangle* tris, int64_t 
     }
     PGX_CUDA_TRY(ctx, ctx->textures.reserve(sizeof(DevTexture) * tex_info.size()));
     PGX_CUDA_TRY(ctx, ctx->texels.reserve(sizeof(float) * pool.size()));
+    ctx->ntex = (int32_t)tex_info.size();
+    ctx->ntexels = (int64_t)(pool.size() / 3);
     PGX_CUDA_TRY(ctx, ctx->mats.reserve(sizeof(DevMaterial) * std::max<size_t>(dm.size(), 1)));
     PGX_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->textures.p, tex_info.data(), sizeof(DevTexture) * tex_info.size(),
                                       cudaMemcpyHostToDevice, s));

@@ -173,26 +173,30 @@ class MeshBuilder:
         return out
 
 
-def cornell_box(seed: int = 1, width: int = 256, height: int = 256) -> SceneDesc:
-    """The plain path-tracing configuration (36 triangles)."""
+def cornell_box(seed: int = 1, width: int = 256, height: int = 256, target_tris: int | None = None) -> SceneDesc:
+    """The plain path-tracing configuration (36 triangles).  With
+    `target_tris`, walls and boxes are tessellated into res x res cells
+    (34 res^2 + 2 triangles, res = round(sqrt((target - 2) / 34))); the
+    geometry and the light stay the same."""
     rng = np.random.default_rng(seed)
     mb = MeshBuilder()
     mats = []
+    res = 1 if target_tris is None else max(1, int(round(math.sqrt(max(target_tris - 2, 34) / 34.0))))
 
     def lambert():
         mats.append(material(BSDF_DIFFUSE, albedo=tuple(rng.uniform(0.1, 0.8, 3))))
         return len(mats) - 1
 
     # Five walls of the box [-1,1] x [0,2] x [-1,1], open towards +z, normals inward.
-    mb.quad_grid((-1, 0, -1), (2, 0, 0), (0, 0, 2), (0, 1, 0), 1, lambert())       # floor
-    mb.quad_grid((-1, 2, -1), (2, 0, 0), (0, 0, 2), (0, -1, 0), 1, lambert())      # ceiling
-    mb.quad_grid((-1, 0, -1), (2, 0, 0), (0, 2, 0), (0, 0, 1), 1, lambert())       # back
-    mb.quad_grid((-1, 0, -1), (0, 0, 2), (0, 2, 0), (1, 0, 0), 1, lambert())       # left
-    mb.quad_grid((1, 0, -1), (0, 0, 2), (0, 2, 0), (-1, 0, 0), 1, lambert())       # right
+    mb.quad_grid((-1, 0, -1), (2, 0, 0), (0, 0, 2), (0, 1, 0), res, lambert())       # floor
+    mb.quad_grid((-1, 2, -1), (2, 0, 0), (0, 0, 2), (0, -1, 0), res, lambert())      # ceiling
+    mb.quad_grid((-1, 0, -1), (2, 0, 0), (0, 2, 0), (0, 0, 1), res, lambert())       # back
+    mb.quad_grid((-1, 0, -1), (0, 0, 2), (0, 2, 0), (1, 0, 0), res, lambert())       # left
+    mb.quad_grid((1, 0, -1), (0, 0, 2), (0, 2, 0), (-1, 0, 0), res, lambert())       # right
     for cx, cz in ((-0.4, -0.3), (0.4, 0.35)):
         s = rng.uniform(0.4, 0.9)
         yaw = math.radians(rng.uniform(0.0, 90.0))
-        mb.box((cx, s * 0.5, cz), (s, s, s), yaw, lambert())
+        mb.box((cx, s * 0.5, cz), (s, s, s), yaw, lambert(), res=res)
     mats.append(material(BSDF_DIFFUSE, albedo=(0.0, 0.0, 0.0), emission=(17.0, 17.0, 17.0)))
     mb.quad_grid((-0.25, 1.999, -0.25), (0.5, 0, 0), (0, 0, 0.5), (0, -1, 0), 1, len(mats) - 1)
     cam = dict(from_=(0.0, 1.0, 3.8), to=(0.0, 1.0, 0.0), up=(0.0, 1.0, 0.0), fov=40.0, width=width, height=height)
