@@ -140,13 +140,19 @@ def run_pgx(args) -> dict:
 
     pkg_build.build()
     desc, depth, wl = make_workload(args.workload)
-    mode = {"plain": abi.MODE_PLAIN, "guided_quadtree": abi.MODE_GUIDED_QUADTREE}[args.mode]
+    mode = {"plain": abi.MODE_PLAIN, "guided_quadtree": abi.MODE_GUIDED_QUADTREE,
+            "guided_mlp": abi.MODE_GUIDED_MLP}[args.mode]
     ctx = Context(0)
     ctx.upload(desc)
     ctx.bvh_build()
     if mode == abi.MODE_GUIDED_QUADTREE:
         # Radiance cache from a 1-spp guided-Li pass (the reference's records).
         ctx.render(1, mode=abi.MODE_GUIDED_LI, seed=99, max_depth=depth, record_paths=True)
+    if mode == abi.MODE_GUIDED_MLP:
+        # The learned guide, trained online on 16 frames (not timed).
+        ctx.mlp_init(3)
+        ctx.mlp_configure(lr=5e-3, decay=0.998, batch=1 << 18, steps=4)
+        ctx.render(16, mode=mode, seed=99, max_depth=depth, train_guide=True)
     ctx.clear()
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     for i in range(args.warmup):
@@ -480,8 +486,8 @@ def run_batch_study(args) -> dict:
     spp, depth = 32, 8
     specs = []
     for i in range(n):
-        tris = int(np.exp(rng.uniform(np.log(1e3), np.log(2e6))))
-        res = int(rng.choice([128, 256, 512, 1024]))
+        tris = int(np.exp(rng.uniform(np.log(1e3), np.log(args.batch_max_tris))))
+        res = int(rng.choice([128, 256, 512, 1024])) if args.batch_res == 0 else args.batch_res
         specs.append(dict(seed=i + 1, width=res, height=res, target_tris=tris))
     t0 = time.perf_counter()
     descs = [scenes.cornell_box(**sp) for sp in specs]
@@ -542,8 +548,9 @@ def run_batch_study(args) -> dict:
     rows = [r for r in per_scene if "relmse_reference_cpu" in r]
     ratio = [r["relmse_batch"] / r["relmse_reference_cpu"] for r in rows if r["relmse_reference_cpu"] > 0]
     return {
-        "study": "batched wavefront rendering: one persistent graph-captured launch over many scenes",
+        "study": "batched wavefront rendering: one graph-captured launch over many scenes",
         "scenes": n, "spp": spp, "max_depth": depth, "paths": int(paths),
+        "resolutions": sorted({sp["width"] for sp in specs}), "max_tris_drawn": args.batch_max_tris,
         "triangles_total": int(sum(d.ntris for d in descs)),
         "tuning": {"wave_paths": tuning.wave_paths, "trace_blocks_per_sm": tuning.trace_blocks_per_sm,
                    "shade_blocks_per_sm": tuning.shade_blocks_per_sm},
@@ -710,7 +717,7 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["pgx", "reference"], default="pgx")
-    ap.add_argument("--mode", choices=["plain", "guided_quadtree"], default="plain")
+    ap.add_argument("--mode", choices=["plain", "guided_quadtree", "guided_mlp"], default="plain")
     ap.add_argument("--workload", choices=["interior", "cornell"], default="interior")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--study", choices=["relmse", "traversal", "adjoint", "batch"], default=None,
@@ -729,6 +736,8 @@ def main() -> None:
     ap.add_argument("--trav-rays", type=int, default=10_000_000)
     ap.add_argument("--fd-params", type=int, default=256)
     ap.add_argument("--batch-scenes", type=int, default=64)
+    ap.add_argument("--batch-res", type=int, default=0, help="0: resolutions drawn from {128,256,512,1024}")
+    ap.add_argument("--batch-max-tris", type=float, default=2e6)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     if args.gpus != 1 or int(os.environ.get("WORLD_SIZE", "1")) != 1:
