@@ -296,8 +296,15 @@ def run_relmse_study(args) -> dict:
         return rgb.astype(np.float64) / spp
 
     ctx.clear()
-    ref_ms = render_ms(args.ref_spp, abi.MODE_PLAIN, 1000)
-    ref = image()
+    cache = Path(args.ref_cache) if args.ref_cache else None
+    if cache is not None and cache.exists():
+        ref = np.load(cache)
+        ref_ms = float("nan")
+    else:
+        ref_ms = render_ms(args.ref_spp, abi.MODE_PLAIN, 1000)
+        ref = image()
+        if cache is not None:
+            np.save(cache, ref)
     metric = relmse_robust if args.metric == "robust" else relmse
 
     # Plain: its error at plain_spp and the time it takes.
@@ -314,12 +321,15 @@ def run_relmse_study(args) -> dict:
         # Learned guide: online training on the first `train_frames` frames
         # (one Adam step per frame, batch 2^18), which stay in the image.
         ctx.mlp_init(3)
-        ctx.mlp_configure(lr=args.mlp_lr, decay=args.mlp_decay, batch=1 << 18, steps=args.mlp_steps)
+        ctx.mlp_configure(lr=args.mlp_lr, decay=args.mlp_decay, batch=1 << 18, steps=args.mlp_steps,
+                          direct=not args.mlp_indirect)
         mode = abi.MODE_GUIDED_MLP
-        train_ms = render_ms(args.train_frames, mode, 13, guide_fraction=args.guide_fraction, train_guide=True)
+        train_ms = render_ms(args.train_frames, mode, 13, guide_fraction=args.guide_fraction, train_guide=True,
+                             guide_depth=args.guide_depth)
         train_spp = args.train_frames
         extra = {"train_frames": args.train_frames, "lr": args.mlp_lr, "lr_decay": args.mlp_decay,
-                 "adam_steps_per_frame": args.mlp_steps}
+                 "adam_steps_per_frame": args.mlp_steps, "guide_depth": args.guide_depth,
+                 "target": "indirect" if args.mlp_indirect else "full incident radiance"}
     else:
         # QuadTree: train the cache over `train_iters` iterations of 1, 2, 4,
         # ... frames (the first plain, the rest guided by the previous cache;
@@ -340,7 +350,8 @@ def run_relmse_study(args) -> dict:
     chunk = max(1, args.plain_spp // 32)
     total = train_spp if args.guide == "mlp" else 0
     while total < 4 * args.plain_spp:
-        guided_ms += render_ms(chunk, mode, 17 + total, guide_fraction=args.guide_fraction)
+        guided_ms += render_ms(chunk, mode, 17 + total, guide_fraction=args.guide_fraction,
+                               guide_depth=args.guide_depth)
         total += chunk
         err = metric(image(), ref)
         curve.append((total, train_ms + guided_ms, err))
@@ -733,6 +744,9 @@ def main() -> None:
     ap.add_argument("--mlp-lr", type=float, default=5e-3)
     ap.add_argument("--mlp-decay", type=float, default=0.998)
     ap.add_argument("--mlp-steps", type=int, default=4)
+    ap.add_argument("--ref-cache", default=None, help="npy file keeping the converged image between study runs")
+    ap.add_argument("--guide-depth", type=int, default=0, help="guide the first N bounces only (0: all)")
+    ap.add_argument("--mlp-indirect", action="store_true", help="train the learned guide on indirect light only")
     ap.add_argument("--trav-rays", type=int, default=10_000_000)
     ap.add_argument("--fd-params", type=int, default=256)
     ap.add_argument("--batch-scenes", type=int, default=64)

@@ -185,6 +185,8 @@ typedef struct pgx_render_config {
                             * NEE+MIS incident radiance.  The cache is rebuilt
                             * from the records when the call ends. */
     int32_t flags;         /* PGX_RENDER_PROFILE: per-stage events/counters */
+    int32_t guide_depth;   /* guided modes: guide the first guide_depth
+                            * bounces only (0: every bounce)               */
 } pgx_render_config;
 
 /* pgx_render_config.flags */
@@ -433,8 +435,10 @@ int pgx_mlp_train_step(pgx_ctx* ctx, const pgx_radiance_sample* samples, int64_t
 /* Online training inside pgx_render (PGX_RENDER_TRAIN_GUIDE): after every
  * frame, `steps` Adam steps on disjoint batches of at most `batch` of that
  * frame's radiance samples, learning rate lr * decay^step (defaults 5e-3,
- * 0.998, 262144, 4). */
-int pgx_mlp_configure(pgx_ctx* ctx, float lr, float decay, int64_t batch, int32_t steps);
+ * 0.998, 262144, 4).  direct = 1 trains on the full incident radiance of a
+ * continuation (the default); 0 leaves out the emission reached directly
+ * from the vertex, which next-event estimation also samples. */
+int pgx_mlp_configure(pgx_ctx* ctx, float lr, float decay, int64_t batch, int32_t steps, int32_t direct);
 
 /* ---- differentiable rendering (extension; the reference renders forward only) ----
  * Plain path tracing with NEE + MIS (PGX_MODE_PLAIN's estimator, box

@@ -117,6 +117,7 @@ class RayTracer {
         cfg_.guide_fraction = 0.5f;
         cfg_.record_paths = mode == PGX_MODE_GUIDED_LI ? 1 : 0;
         cfg_.flags = 0;
+        cfg_.guide_depth = 0;
     }
 
     // RayTracer::init (Renderer.h:251-263).

@@ -77,7 +77,8 @@ RENDER_FILTER_MITCHELL = 2
 
 class RenderConfig(C.Structure):
     _fields_ = [("mode", C.c_int32), ("max_depth", C.c_int32), ("seed", C.c_uint64),
-                ("guide_fraction", C.c_float), ("record_paths", C.c_int32), ("flags", C.c_int32)]
+                ("guide_fraction", C.c_float), ("record_paths", C.c_int32), ("flags", C.c_int32),
+                ("guide_depth", C.c_int32)]
 
 
 class RenderStats(C.Structure):
@@ -149,7 +150,7 @@ SIGNATURES = {
     "pgx_mlp_sample": (C.c_int, [_P, _P, _P, _I64, _P, _P]),
     "pgx_mlp_gradient": (C.c_int, [_P, _P, _I64, _P, C.POINTER(C.c_double)]),
     "pgx_mlp_train_step": (C.c_int, [_P, _P, _I64, C.c_float, C.POINTER(C.c_double)]),
-    "pgx_mlp_configure": (C.c_int, [_P, C.c_float, C.c_float, _I64, _I32]),
+    "pgx_mlp_configure": (C.c_int, [_P, C.c_float, C.c_float, _I64, _I32, _I32]),
     "pgx_diff_set_params": (C.c_int, [_P, _P, _P, _P]),
     "pgx_diff_render": (C.c_int, [_P, _I32, C.c_uint64, _I32, _P]),
     "pgx_diff_adjoint": (C.c_int, [_P, _I32, C.c_uint64, _I32, _P, _P, _P, _P]),

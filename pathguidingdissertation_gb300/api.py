@@ -128,10 +128,10 @@ class Context:
 
     def render(self, frames: int = 1, mode: int = abi.MODE_PLAIN, seed: int = 1, max_depth: int = 8,
                guide_fraction: float = 0.5, record_paths: int | bool = 0, profile: bool = False,
-               mitchell: bool = False, train_guide: bool = False) -> None:
+               mitchell: bool = False, train_guide: bool = False, guide_depth: int = 0) -> None:
         flags = (abi.RENDER_PROFILE if profile else 0) | (abi.RENDER_FILTER_MITCHELL if mitchell else 0) | \
             (abi.RENDER_TRAIN_GUIDE if train_guide else 0)
-        cfg = abi.RenderConfig(mode, max_depth, seed, guide_fraction, int(record_paths), flags)
+        cfg = abi.RenderConfig(mode, max_depth, seed, guide_fraction, int(record_paths), flags, guide_depth)
         self.check(self.lib.pgx_render(self.h, C.byref(cfg), frames))
 
     def clear(self) -> None:
@@ -275,8 +275,9 @@ class Context:
         self.check(self.lib.pgx_mlp_train_step(self.h, ptr(s), len(s), lr, C.byref(loss)))
         return loss.value
 
-    def mlp_configure(self, lr: float = 5e-3, decay: float = 0.998, batch: int = 262144, steps: int = 4) -> None:
-        self.check(self.lib.pgx_mlp_configure(self.h, lr, decay, batch, steps))
+    def mlp_configure(self, lr: float = 5e-3, decay: float = 0.998, batch: int = 262144, steps: int = 4,
+                      direct: bool = True) -> None:
+        self.check(self.lib.pgx_mlp_configure(self.h, lr, decay, batch, steps, int(direct)))
 
     # ---- differentiable rendering ----
     def diff_set_params(self, env: np.ndarray | None = None, albedo_offset: np.ndarray | None = None,

@@ -43,6 +43,7 @@ struct MlpState {
     float lr = 5e-3f, decay = 0.998f;
     int64_t batch = 262144;
     int steps = 4;
+    int direct = 1;
     int64_t step = 0;
     bool valid = false;
     int sms = 0;
@@ -98,11 +99,15 @@ __global__ void __launch_bounds__(kThreads) k_query(const uint8_t* __restrict__ 
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint64_t mbar;
     __shared__ uint32_t tslot;
+    __shared__ int flag;
     FwdSmem s;
     s.w = smem;
     s.bias = reinterpret_cast<float*>(smem + kImageBytes);
     s.act = smem + kImageBytes + kBiasFloats * 4;
     s.mbar = &mbar;
+    s.flag = &flag;
+    s.bar = 1;
+    s.tg = threadIdx.x;
     load_weights(image, s.w, s.bias);
     if (threadIdx.x == 0) tc::mbar_init(&mbar, 1);
     if (threadIdx.x < 32) {
@@ -180,12 +185,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_train(const uint8_t* __restrict
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint64_t mbar;
     __shared__ uint32_t tslot;
+    __shared__ int flag;
     const int t = threadIdx.x, warp = t >> 5;
     FwdSmem s;
     s.w = smem + kTrainWOffset;
     s.bias = reinterpret_cast<float*>(smem + kTrainWOffset + kImageBytes);
     s.act = smem + x_offset(0);
     s.mbar = &mbar;
+    s.flag = &flag;
+    s.bar = 1;
+    s.tg = t;
     uint8_t* xs[kLayers];
     for (int l = 0; l < kLayers; l++) xs[l] = smem + x_offset(l);
     uint8_t* dy = smem + kDyOffset;
@@ -245,7 +254,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_train(const uint8_t* __restrict
             }
         }
         for (int lay = kLayers - 1; lay >= 0; lay--) {
-            publish_smem();
+            publish_smem(s.bar);
             if (t == 0) {
                 // dW^T (+)= X^T dY
                 const uint32_t xa = tc::smem_addr(xs[lay]), ya = tc::smem_addr(dy);
@@ -267,13 +276,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_train(const uint8_t* __restrict
                 }
                 tc::mma_commit(&mbar);
             }
-            bool ok = tc::mbar_wait(&mbar, phase, kWaitPolls);
-            phase ^= 1u;
-            if (__syncthreads_or(!ok)) {
+            if (!group_wait(s, phase)) {
                 failed = true;
                 break;
             }
-            tc::fence_after_sync();
             if (lay > 0) {
                 float acc[64];
                 tc::tmem_ld32(tc::tmem_at(s.tmem, warp * 32, 0), acc);
@@ -569,17 +575,22 @@ extern "C" int pgx_mlp_train_step(pgx_ctx* ctx, const pgx_radiance_sample* sampl
     return train_host(ctx, samples, n, lr, loss, nullptr, true, "pgx_mlp_train_step");
 }
 
-extern "C" int pgx_mlp_configure(pgx_ctx* ctx, float lr, float decay, int64_t batch, int32_t steps) {
+extern "C" int pgx_mlp_configure(pgx_ctx* ctx, float lr, float decay, int64_t batch, int32_t steps,
+                                 int32_t direct) {
     PGX_TRY(ensure_ready(ctx, "pgx_mlp_configure"));
-    if (!(lr > 0.f) || !(decay > 0.f) || decay > 1.f || batch <= 0 || steps <= 0 || steps > 64)
+    if (!(lr > 0.f) || !(decay > 0.f) || decay > 1.f || batch <= 0 || steps <= 0 || steps > 64 ||
+        (direct != 0 && direct != 1))
         return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_mlp_configure: bad arguments");
     MlpState* st = state(ctx);
     st->lr = lr;
     st->decay = decay;
     st->batch = batch;
     st->steps = steps;
+    st->direct = direct;
     return PGX_OK;
 }
+
+int mlp_train_direct(pgx_ctx* ctx) { return state(ctx)->direct; }
 
 // Online training inside pgx_render: `steps` Adam steps on consecutive
 // slices of the frame's samples (the last slice only if at least a quarter

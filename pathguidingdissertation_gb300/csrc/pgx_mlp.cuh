@@ -90,12 +90,17 @@ __device__ __forceinline__ void encode_row(uint8_t* tile, int r, const Bounds& b
         float t = (p[c] - b.bmin[c]) * b.inv_ext[c];
         t = fminf(fmaxf(t, 0.f), 1.f);
         float v[24];
+        // sin/cos of 2^j pi t by the double-angle recurrence from j = 0
+        // (absolute error below 2^j ulp, far under the bf16 step of 2^-8)
+        float sn, cs;
+        sincospif(t, &sn, &cs);
 #pragma unroll
         for (int j = 0; j < kFreq; j++) {
-            float s, co;
-            sincospif(t * (float)(1 << j), &s, &co);
-            v[2 * j] = s;
-            v[2 * j + 1] = co;
+            v[2 * j] = sn;
+            v[2 * j + 1] = cs;
+            float s2 = 2.f * sn * cs;
+            cs = (cs - sn) * (cs + sn);
+            sn = s2;
         }
         store_chunk(tile, r, 3 * c, v);
         store_chunk(tile, r, 3 * c + 1, v + 8);
@@ -280,16 +285,25 @@ __device__ __forceinline__ float loss_grad(const float* raw, F3 wi, float weight
 }
 
 // ---- one forward pass of a 128-row tile on the tensor cores ------------------------
-// Shared memory the caller provides: the six weight images (kImageBytes),
-// biases (kBiasFloats floats), an activation tile of kIn/8 chunks, an
-// mbarrier and the TMEM base address (64 columns at least).
+// A tile is processed by a group of 128 threads (4 warps; thread t of the
+// group owns row t, and its warp reads TMEM lanes 32 * (warp % 4) ..).  A CTA
+// may run several groups on independent tiles; each group has its own
+// activation tile, mbarrier, TMEM columns, wait flag and named barrier, and
+// they share the weight images and biases.
 struct FwdSmem {
-    uint8_t* w;      // weight images
+    uint8_t* w;      // weight images (shared by the CTA's groups)
     float* bias;
-    uint8_t* act;    // activation tile (row-major chunks), at least kIn/8 chunks
-    uint64_t* mbar;
-    uint32_t tmem;   // accumulator: 64 columns
+    uint8_t* act;    // the group's activation tile, at least kIn/8 chunks
+    uint64_t* mbar;  // the group's mbarrier
+    int* flag;       // the group's wait result (shared memory)
+    uint32_t tmem;   // the group's accumulator: 64 columns
+    int bar;         // the group's named barrier (1..15)
+    int tg;          // thread index within the group
 };
+
+__device__ __forceinline__ void group_sync(int bar) {
+    asm volatile("bar.sync %0, 128;" ::"r"(bar) : "memory");
+}
 
 // Issue layer l: D(128 x 64) = act(128 x K) * W_l^T (one thread).
 __device__ __forceinline__ void issue_layer(const FwdSmem& s, int l, const uint8_t* act) {
@@ -304,52 +318,64 @@ __device__ __forceinline__ void issue_layer(const FwdSmem& s, int l, const uint8
     tc::mma_commit(s.mbar);
 }
 
-// Makes this thread's shared-memory writes visible to the tensor core and
+// Makes the group's shared-memory writes visible to the tensor core and
 // orders them before the MMA issue.
-__device__ __forceinline__ void publish_smem() {
+__device__ __forceinline__ void publish_smem(int bar) {
     tc::fence_async_smem();
     tc::fence_before_sync();
-    __syncthreads();
+    group_sync(bar);
     tc::fence_after_sync();
 }
 
 constexpr uint32_t kWaitPolls = 1u << 22;
 
-// Runs the six layers on the tile already encoded in s.act; thread t
-// (0..127) receives row t's 40 raw outputs.  `phase` is the mbarrier parity
-// to wait for next (updated).  Returns false if an MMA did not complete in
-// time (uniform across the CTA).  When keep_acts is given, layer l's input
-// tile is s.act for l = 0 and keep_acts[l] for l > 0 (each kIn/8 or
-// kHid/8 + 1 chunks), and is left in place for a backward pass.
+// Thread 0 of the group waits (bounded) for the MMAs committed to s.mbar;
+// the result reaches every thread of the group.  Returns false on timeout.
+__device__ __forceinline__ bool group_wait(const FwdSmem& s, uint32_t& phase) {
+    if (s.tg == 0) *s.flag = tc::mbar_wait(s.mbar, phase, kWaitPolls) ? 0 : 1;
+    phase ^= 1u;
+    group_sync(s.bar);
+    bool ok = *s.flag == 0;
+    tc::fence_after_sync();
+    return ok;
+}
+
+// Runs the six layers on the tile already encoded in s.act; thread tg of
+// the group receives row tg's 40 raw outputs.  `phase` is the mbarrier
+// parity to wait for next (updated).  Returns false if an MMA did not
+// complete in time (uniform across the group).  When keep_acts is given,
+// layer l's input tile is s.act for l = 0 and keep_acts[l] for l > 0 (each
+// kIn/8 or kHid/8 + 1 chunks), and is left in place for a backward pass.
 __device__ __forceinline__ bool forward_tile(const FwdSmem& s, uint32_t& phase, float* out,
                                              uint8_t* const* keep_acts = nullptr) {
-    const int t = threadIdx.x;
+    const int t = s.tg;
     const int warp = t >> 5;
     for (int l = 0; l < kLayers; l++) {
         uint8_t* in = (l == 0 || !keep_acts) ? s.act : keep_acts[l];
-        publish_smem();
+        publish_smem(s.bar);
         if (t == 0) issue_layer(s, l, in);
-        bool ok = tc::mbar_wait(s.mbar, phase, kWaitPolls);
-        phase ^= 1u;
-        if (__syncthreads_or(!ok)) return false;
-        tc::fence_after_sync();
-        float acc[64];
-        tc::tmem_ld32(tc::tmem_at(s.tmem, warp * 32, 0), acc);
-        tc::tmem_ld32(tc::tmem_at(s.tmem, warp * 32, 32), acc + 32);
+        if (!group_wait(s, phase)) return false;
         const float* b = s.bias + l * kHid;
-        if (l < kLayers - 1) {
-            uint8_t* dst = keep_acts ? keep_acts[l + 1] : s.act;
-            // the MMA that read s.act has completed, so it may be overwritten
+        // two halves of 32 accumulator columns, to keep registers low
 #pragma unroll
-            for (int c = 0; c < kHid / 8; c++) {
-                float v[8];
+        for (int half = 0; half < 2; half++) {
+            float acc[32];
+            tc::tmem_ld32(tc::tmem_at(s.tmem, warp * 32, 32 * half), acc);
+            if (l < kLayers - 1) {
+                uint8_t* dst = keep_acts ? keep_acts[l + 1] : s.act;
+                // the MMA that read s.act has completed, so it may be overwritten
 #pragma unroll
-                for (int j = 0; j < 8; j++) v[j] = fmaxf(acc[8 * c + j] + b[8 * c + j], 0.f);
-                store_chunk(dst, t, c, v);
+                for (int c = 0; c < 4; c++) {
+                    float v[8];
+#pragma unroll
+                    for (int j = 0; j < 8; j++) v[j] = fmaxf(acc[8 * c + j] + b[32 * half + 8 * c + j], 0.f);
+                    store_chunk(dst, t, 4 * half + c, v);
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < 32; j++)
+                    if (32 * half + j < kOut) out[32 * half + j] = acc[j] + b[32 * half + j];
             }
-        } else {
-#pragma unroll
-            for (int j = 0; j < kOut; j++) out[j] = acc[j] + b[j];
         }
         tc::fence_before_sync();
     }
@@ -369,3 +395,4 @@ int mlp_train_device(pgx_ctx* ctx, const float* samples, int64_t n, float lr, do
 int mlp_query_device(pgx_ctx* ctx, const float* q, const float* aux, int64_t n, int mode, float* out, float* out2);
 int mlp_online_step(pgx_ctx* ctx, const float* samples, int64_t n);
 int64_t mlp_train_batch(pgx_ctx* ctx);
+int mlp_train_direct(pgx_ctx* ctx);

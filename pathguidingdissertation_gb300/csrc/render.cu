@@ -135,7 +135,9 @@ struct FrameParams {
     int profile;     // count node/triangle fetches
     int mitchell;    // Mitchell-Netravali splat instead of the box filter
     int train;       // learned guide: emit radiance samples of recorded vertices
+                     // (1: indirect light only, 2: full incident radiance)
     float train_keep;  // probability of keeping one radiance sample
+    int guide_depth;   // guided modes: bounces guided (max_depth + 1: all)
 };
 
 // Batched rendering: what differs between the scenes of a batch whose
@@ -466,6 +468,9 @@ static __device__ __noinline__ F3 mlp_guided_sample(const float4* __restrict__ m
     } else {
         float bp;
         wi = bsdf_sample(m, tv, sd, rng, f, bp);
+        // non-specular: bsdf_sample's pdf is bsdf_pdf(wi)
+        pdf = frac * mlp::packed_pdf(mix, wi) + (1.f - frac) * bp;
+        return wi;
     }
     float bp = bsdf_pdf(m, tv, sd, wi);
     pdf = frac * mlp::packed_pdf(mix, wi) + (1.f - frac) * bp;
@@ -478,19 +483,30 @@ __device__ __forceinline__ bool mlp_guided_surface(const DevMaterial& m) {
 
 // Learned guide, one depth: the network evaluated on the tensor cores for
 // every queued path, 128 paths per tile; paths whose hit is a guided
-// surface get their vMF mixture (10 float4) in ps.guide.
-constexpr int kInferSmem = mlp::kImageBytes + mlp::kBiasFloats * 4 + (mlp::kIn / 8) * mlp::kChunk;
+// surface get their packed vMF mixture in ps.guide.  Each CTA runs
+// kInferGroups groups of 128 threads on independent tiles (they share the
+// weights in shared memory), so one group's gathers and epilogues overlap
+// another's MMAs.
+constexpr int kInferGroups = 3;
+constexpr int kInferAct = (mlp::kIn / 8) * mlp::kChunk;
+constexpr int kInferSmem = mlp::kImageBytes + mlp::kBiasFloats * 4 + kInferGroups * kInferAct;
+constexpr uint32_t kInferCols = 256;  // >= 64 per group, a power of two
 
-__global__ void __launch_bounds__(kThreads) k_guide_infer(SceneView sv, PathState ps, int depth, MlpView mv,
-                                                          int* status) {
+__global__ void __launch_bounds__(128 * kInferGroups, 2) k_guide_infer(SceneView sv, PathState ps, int depth, MlpView mv,
+                                                                   int* status) {
     extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ uint64_t mbar;
+    __shared__ uint64_t mbar[kInferGroups];
+    __shared__ int flag[kInferGroups];
     __shared__ uint32_t tslot;
+    const int g = threadIdx.x >> 7;
     mlp::FwdSmem s;
     s.w = smem;
     s.bias = reinterpret_cast<float*>(smem + mlp::kImageBytes);
-    s.act = smem + mlp::kImageBytes + mlp::kBiasFloats * 4;
-    s.mbar = &mbar;
+    s.act = smem + mlp::kImageBytes + mlp::kBiasFloats * 4 + g * kInferAct;
+    s.mbar = &mbar[g];
+    s.flag = &flag[g];
+    s.bar = 1 + g;
+    s.tg = threadIdx.x & 127;
     {
         const uint4* src = reinterpret_cast<const uint4*>(mv.image);
         uint4* dst = reinterpret_cast<uint4*>(s.w);
@@ -498,20 +514,21 @@ __global__ void __launch_bounds__(kThreads) k_guide_infer(SceneView sv, PathStat
         const float* b = reinterpret_cast<const float*>(mv.image + mlp::kImageBytes);
         for (int i = threadIdx.x; i < mlp::kBiasFloats; i += blockDim.x) s.bias[i] = b[i];
     }
-    if (threadIdx.x == 0) tc::mbar_init(&mbar, 1);
+    if (threadIdx.x < kInferGroups) tc::mbar_init(&mbar[threadIdx.x], 1);
     if (threadIdx.x < 32) {
-        tc::tmem_alloc(&tslot, 64);
+        tc::tmem_alloc(&tslot, kInferCols);
         tc::tmem_relinquish();
     }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    s.tmem = tslot;
+    s.tmem = tslot + (uint32_t)(g * 64);
     uint32_t phase = 0;
     const unsigned n = ps.qcount[depth];
     const int* __restrict__ q = ps.queue[depth & 1];
-    for (unsigned tile = blockIdx.x; tile * (unsigned)mlp::kRows < n; tile += gridDim.x) {
-        const unsigned i = tile * mlp::kRows + threadIdx.x;
+    const unsigned groups = gridDim.x * kInferGroups;
+    for (unsigned tile = blockIdx.x * kInferGroups + g; tile * (unsigned)mlp::kRows < n; tile += groups) {
+        const unsigned i = tile * mlp::kRows + s.tg;
         int p = 0;
         bool need = false;
         F3 x = zero3(), nn = zero3(), wo = zero3();
@@ -530,23 +547,23 @@ __global__ void __launch_bounds__(kThreads) k_guide_infer(SceneView sv, PathStat
                 wo = sd.wo;
             }
         }
-        mlp::encode_row(s.act, threadIdx.x, mv.bounds, x, nn, wo);
+        mlp::encode_row(s.act, s.tg, mv.bounds, x, nn, wo);
         float raw[mlp::kOut];
         if (!mlp::forward_tile(s, phase, raw)) {
-            if (threadIdx.x == 0) atomicAdd(status, 1);
+            if (s.tg == 0) atomicAdd(status, 1);
             break;
         }
         if (need) {
-            float4 g[mlp::kPacked];
-            mlp::pack_mixture(raw, g);
+            float4 gm[mlp::kPacked];
+            mlp::pack_mixture(raw, gm);
             float4* dst = ps.guide + (size_t)p * mlp::kPacked;
 #pragma unroll
-            for (int j = 0; j < mlp::kPacked; j++) dst[j] = g[j];
+            for (int j = 0; j < mlp::kPacked; j++) dst[j] = gm[j];
         }
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (threadIdx.x < 32) tc::tmem_dealloc(s.tmem, 64);
+    if (threadIdx.x < 32) tc::tmem_dealloc(tslot, kInferCols);
 }
 
 __device__ __forceinline__ void push_shadow(PathState& ps, int depth, int p, float4 so, float4 sdir, F3 c,
@@ -643,9 +660,9 @@ __global__ void __launch_bounds__(kThreads, 8) k_shade(SceneView sv0, PathState 
                     }
                 } else {
                     int qroot = -1;
-                    if (MODE == PGX_MODE_GUIDED_QUADTREE && !bsdf_pure_specular(m))
+                    if (MODE == PGX_MODE_GUIDED_QUADTREE && depth < fp.guide_depth && !bsdf_pure_specular(m))
                         qroot = guide_region_root(gv, sd.x);
-                    const bool use_mix = MODE == PGX_MODE_GUIDED_MLP && mlp_guided_surface(m);
+                    const bool use_mix = MODE == PGX_MODE_GUIDED_MLP && depth < fp.guide_depth && mlp_guided_surface(m);
                     const float4* mix = use_mix ? ps.guide + (size_t)p * mlp::kPacked : nullptr;
                     if (MODE == PGX_MODE_GUIDED_LI) {
                         next_event_draws(sv, m, rng);
@@ -744,16 +761,19 @@ __global__ void __launch_bounds__(kThreads, 8) k_shade(SceneView sv0, PathState 
                 ps.rec_e[ri] = make_float4(r_e.x, r_e.y, r_e.z, 0.f);
                 ps.nrec[p] = depth + 1;
             } else {
-                float4 l = ps.L[p];
-                // Baseline of the previous vertex's incident radiance: the
-                // cache records the full Li (snapshot before this vertex's
-                // emission); the learned guide trains on indirect light only
-                // (after it), since next-event estimation covers the direct.
-                if (rec_on && depth > 0)
-                    ps.rec_e[(size_t)(depth - 1) * cap + p] =
-                        fp.train ? make_float4(l.x + add.x, l.y + add.y, l.z + add.z, 0.f) : l;
-                if (add.x != 0.f || add.y != 0.f || add.z != 0.f || !valid(add))
-                    ps.L[p] = make_float4(l.x + add.x, l.y + add.y, l.z + add.z, 0.f);
+                const bool adds = add.x != 0.f || add.y != 0.f || add.z != 0.f || !valid(add);
+                const bool snap = rec_on && depth > 0;
+                if (adds || snap) {
+                    float4 l = ps.L[p];
+                    // Baseline of the previous vertex's incident radiance: the
+                    // full Li is what the path gathers from this vertex's
+                    // emission on (snapshot before it); the indirect-only
+                    // target of the learned guide starts after it.
+                    if (snap)
+                        ps.rec_e[(size_t)(depth - 1) * cap + p] =
+                            fp.train == 1 ? make_float4(l.x + add.x, l.y + add.y, l.z + add.z, 0.f) : l;
+                    if (adds) ps.L[p] = make_float4(l.x + add.x, l.y + add.y, l.z + add.z, 0.f);
+                }
                 if (rec_on) {
                     size_t ri = (size_t)depth * cap + p;
                     ps.rec_pos[ri] = make_float4(r_pos.x, r_pos.y, r_pos.z, (cont && r_store) ? 1.f : 0.f);
@@ -1526,10 +1546,11 @@ int enqueue_frame(pgx_ctx* ctx, RenderState* rs, const FrameParams& fp, cudaStre
         else
             k_extend<false><<<pg, kThreads, 0, s>>>(sv, ps, depth);
         if (prof) cudaEventRecord(rs->prof[4 * depth + 1], s);
-        if (fp.mode == PGX_MODE_GUIDED_MLP) {
+        if (fp.mode == PGX_MODE_GUIDED_MLP && depth < fp.guide_depth) {
             const int64_t tiles = (n + mlp::kRows - 1) / mlp::kRows;
-            const unsigned ig = (unsigned)std::max<int64_t>(1, std::min<int64_t>(tiles, 152 * 3));
-            k_guide_infer<<<ig, kThreads, kInferSmem, s>>>(sv, ps, depth, mv, mlp_status);
+            const int64_t ctas = (tiles + kInferGroups - 1) / kInferGroups;
+            const unsigned ig = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ctas, 152 * 2));
+            k_guide_infer<<<ig, 128 * kInferGroups, kInferSmem, s>>>(sv, ps, depth, mv, mlp_status);
             launches++;
         }
         switch (fp.mode) {
@@ -1692,7 +1713,8 @@ extern "C" int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t fr
         fp.guide_fraction = cfg->guide_fraction;
         fp.profile = prof ? 1 : 0;
         fp.mitchell = (cfg->flags & PGX_RENDER_FILTER_MITCHELL) ? 1 : 0;
-        fp.train = train ? 1 : 0;
+        fp.train = train ? (mlp_train_direct(ctx) ? 2 : 1) : 0;
+        fp.guide_depth = cfg->guide_depth > 0 ? cfg->guide_depth : kMaxDepthCap + 1;
         fp.train_keep = 1.f;
         if (train && rs->train_last > 0)
             fp.train_keep = (float)std::min(1.0, (double)tcap / (1.25 * (double)rs->train_last * fp.batch));
