@@ -155,22 +155,25 @@ def run_pgx(args) -> dict:
         ctx.render(16, mode=mode, seed=99, max_depth=depth, train_guide=True)
     ctx.clear()
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    spp = args.spp_per_step
     for i in range(args.warmup):
-        ctx.render(1, mode=mode, seed=1, max_depth=depth, profile=True)
+        ctx.render(spp, mode=mode, seed=1, max_depth=depth, profile=True)
     torch.cuda.synchronize()
-    rays = paths = 0
-    ms = ms_ext = 0.0
+    rays = paths = ext_rays = 0
+    ms = ms_ext = ms_shade = 0.0
     ext_visits = ext_tris = ext_launches = launches = 0
     with ClockSampler() as clk:
         for k in range(args.steps):
             flush.zero_()
             torch.cuda.synchronize()
-            ctx.render(1, mode=mode, seed=1, max_depth=depth, profile=True)
+            ctx.render(spp, mode=mode, seed=1, max_depth=depth, profile=True)
             st = ctx.render_stats()
             rays += st.extension_rays + st.shadow_rays
             paths += st.paths
             ms += st.ms_total
             ms_ext += st.ms_extend
+            ms_shade += st.ms_shade
+            ext_rays += st.extension_rays
             ext_visits += st.extend_interior_visits
             ext_tris += st.extend_tri_tests
             ext_launches += st.extend_launches
@@ -186,13 +189,13 @@ def run_pgx(args) -> dict:
     from pathguidingdissertation_gb300.api import camera_struct
     cam = camera_struct(desc.camera)
     cfg = abi.RenderConfig(mode, depth, 1, 0.5, 0, 0)
-    spp = C.c_int32()
+    spp_read = C.c_int32()
     e2e_rays = 0
     t0 = time.perf_counter()
     for k in range(args.steps):
         ctx.check(ctx.lib.pgx_set_camera(ctx.h, C.byref(cam)))
-        ctx.check(ctx.lib.pgx_render(ctx.h, C.byref(cfg), 1))
-        ctx.check(ctx.lib.pgx_film_read(ctx.h, host_film.data_ptr(), None, C.byref(spp)))
+        ctx.check(ctx.lib.pgx_render(ctx.h, C.byref(cfg), spp))
+        ctx.check(ctx.lib.pgx_film_read(ctx.h, host_film.data_ptr(), None, C.byref(spp_read)))
         st = ctx.render_stats()
         e2e_rays += st.extension_rays + st.shadow_rays
     e2e_s = time.perf_counter() - t0
@@ -216,7 +219,26 @@ def run_pgx(args) -> dict:
         "avg_launch_ms": ms_ext / max(ext_launches, 1),
         "extend_share_of_step": ms_ext / ms if ms else None,
     }
+    # k_shade: one launch per depth, one path vertex per extension ray; per
+    # vertex it reads the path state (80 B) and the hit triangle's shading
+    # record (80 B), writes the continuation (64 B) and a shadow-ray record
+    # (52 B) and updates the radiance (32 B): 308 B.
+    shade_bytes = 308.0 * ext_rays
+    shade_achieved = shade_bytes / (ms_shade * 1e-3) / 1e9 if ms_shade > 0 else None
+    roofline_shade = {
+        "kernel": "k_shade (path vertex: integrator step, BSDF, NEE)",
+        "bound": "hbm",
+        "achieved": shade_achieved,
+        "peak": peaks["hbm_gbs"],
+        "unit": "GB/s",
+        "frac": (shade_achieved / peaks["hbm_gbs"]) if shade_achieved else None,
+        "alg_bytes_per_vertex": 308,
+        "shade_share_of_step": ms_shade / ms if ms else None,
+        "note": "latency-bound (dependent gathers of shading data, 64 registers); traffic not captured",
+    }
+    print("[bench] device runs done; CPU baseline next", file=sys.stderr, flush=True)
     cpu = cpu_baseline_reference(desc) if not args.no_cpu_baseline else None
+    print("[bench] CPU baseline done", file=sys.stderr, flush=True)
     return {
         "metric": "Mrays/s",
         "value": value,
@@ -231,13 +253,14 @@ def run_pgx(args) -> dict:
         "dtype": "f32",
         "data": "synthetic (seeded procedural scene)",
         "config": {"workload": wl, "mode": args.mode, "paths_per_step": paths // max(args.steps, 1),
-                   "spp_per_step": 1, "l2": "flushed (256 MiB write) before every timed step"},
+                   "spp_per_step": spp, "l2": "flushed (256 MiB write) before every timed step"},
         "mpaths_per_s": paths / (ms * 1e-3) / 1e6,
         "rays_per_path": rays / max(paths, 1),
         "gpu_launches": launches,
         "e2e": {"value": e2e_rays / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": C.sizeof(abi.Camera),
                 "d2h_bytes_per_step": H * W * 3 * 4},
         "roofline": roofline,
+        "roofline_shade": roofline_shade,
         "cpu_baseline": cpu,
         "clocks": clocks,
     }
@@ -731,6 +754,8 @@ def main() -> None:
     ap.add_argument("--mode", choices=["plain", "guided_quadtree", "guided_mlp"], default="plain")
     ap.add_argument("--workload", choices=["interior", "cornell"], default="interior")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--spp-per-step", type=int, default=4,
+                    help="samples per pixel of one step: one pgx_render call, one wavefront")
     ap.add_argument("--study", choices=["relmse", "traversal", "adjoint", "batch"], default=None,
                     help="instead of the throughput line, run the equal-time relMSE study")
     ap.add_argument("--study-res", default="640x360")

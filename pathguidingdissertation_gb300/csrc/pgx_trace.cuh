@@ -283,6 +283,7 @@ __device__ __forceinline__ void trace_persistent(const BvhView& bvh, unsigned n,
     constexpr unsigned kFull = 0xFFFFFFFFu;
     constexpr int kRefillBelow = 24;  // refill when fewer lanes than this are busy
     constexpr int kMaxSteps = 64;
+    constexpr int kCheckEvery = 8;    // steps between occupancy votes
     const int lane = threadIdx.x & 31;
     int2 stack[PGX_STACK_SIZE];
     TraceLane L;
@@ -323,6 +324,7 @@ __device__ __forceinline__ void trace_persistent(const BvhView& bvh, unsigned n,
                     ray = -1;
                 }
             }
+            if (kCheckEvery > 1 && (s % kCheckEvery) != kCheckEvery - 1) continue;
             unsigned busy = __ballot_sync(kFull, ray >= 0);
             if (__popc(busy) < kRefillBelow && !__all_sync(kFull, exhausted || ray >= 0)) break;
             if (busy == 0) break;
