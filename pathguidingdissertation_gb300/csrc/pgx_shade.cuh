@@ -5,7 +5,8 @@
 //
 // render.cu is compiled with -fmad=false, so every a*b+c below rounds twice
 // like the reference's scalar code; where the reference promotes to double
-// (M_PI and long literals) the same promotion is written out.  Random numbers
+// (M_PI and long literals) the expression is computed in float (see
+// PGX_PI_F), within an ulp or two of the reference.  Random numbers
 // are drawn in exactly the reference's order so a path driven by the same
 // stream follows the same decisions.
 #pragma once
@@ -14,6 +15,14 @@
 
 #define PGX_PI_D 3.14159265358979323846
 #define PGX_INV_PI_F 0.318309886183790671538f
+// Single-precision forms of the reference's double-promoted pi expressions
+// (M_PI * x, x / (2 M_PI), ...): the hot path computes them in float, within
+// an ulp or two of the reference's double-then-float rounding, because FP64
+// runs at a small fraction of the FP32 rate on this GPU.
+#define PGX_PI_F 3.14159265358979323846f
+#define PGX_2PI_F 6.28318530717958647692f
+#define PGX_INV_2PI_F 0.159154943091895335769f
+#define PGX_2PI2_F 19.7392088021787172376f
 
 struct F3 {
     float x, y, z;
@@ -80,7 +89,7 @@ __device__ __forceinline__ F3 spherical_to_world(float theta, float phi) {
 }
 __device__ __forceinline__ float spherical_phi(F3 w) {
     float p = atan2f(w.y, w.x);
-    return (p < 0.f) ? (float)((double)p + (2.0 * PGX_PI_D)) : p;
+    return (p < 0.f) ? p + PGX_2PI_F : p;
 }
 
 // ---- shading data (ShadingData, Materials.h:12-32) -----------------------------
@@ -180,7 +189,7 @@ __device__ __forceinline__ float d_ggx(F3 h, float alpha) {
     float a2 = alpha * alpha;
     float c2 = h.z * h.z;
     float t = c2 * (a2 - 1.f) + 1.f;
-    float den = (float)(PGX_PI_D * (double)t * (double)t);
+    float den = (PGX_PI_F * t) * t;
     if (den <= 0.f) return 0.f;
     return a2 / den;
 }
@@ -189,20 +198,20 @@ __device__ __forceinline__ float d_ggx(F3 h, float alpha) {
 __device__ __forceinline__ F3 ggx_sample_h(float alpha, float r1, float r2) {
     float a2 = alpha * alpha;
     float theta = acosf(sqrtf((1.f - r1) / (r1 * (a2 - 1.f) + 1.f)));
-    float phi = (float)(2.0 * PGX_PI_D * (double)r2);
+    float phi = PGX_2PI_F * r2;
     return spherical_to_world(theta, phi);
 }
 
 // Cosine hemisphere sample / pdf (Sampling.h:92-101).
 __device__ __forceinline__ F3 cosine_sample(float r1, float r2) {
     float theta = acosf(sqrtf(r1));
-    float phi = (float)(2.0 * PGX_PI_D * (double)r2);
+    float phi = PGX_2PI_F * r2;
     return spherical_to_world(theta, phi);
 }
 __device__ __forceinline__ float cosine_pdf(F3 wl) {
     float theta = acosf(wl.z);
     float c = cosf(theta);
-    return (c > 0.f) ? (float)((double)c * 0.318309886183790671538) : 0.f;
+    return (c > 0.f) ? c * PGX_INV_PI_F : 0.f;
 }
 
 // ---- BSDF dispatch ------------------------------------------------------------
@@ -329,9 +338,9 @@ static __device__ __noinline__ F3 bsdf_eval(const DevMaterial& m, const TexView&
             float e = plastic_exponent(m.alpha);
             float ks = fresnel_dielectric(dot(wol, h), m.int_ior, m.ext_ior);
             float kd = 1.f - ks;
-            float norm = (float)((double)(e + 2.f) / (4.0 * PGX_PI_D * (double)(2.f - powf(2.f, -e * 0.5f))));
-            float lo = (float)((double)(e + 2.f) / (8.0 * PGX_PI_D));
-            float hi = (float)((double)(e + 4.f) / (8.0 * PGX_PI_D));
+            float norm = (e + 2.f) / ((4.f * PGX_PI_F) * (2.f - powf(2.f, -e * 0.5f)));
+            float lo = (e + 2.f) * (1.f / (8.f * PGX_PI_F));
+            float hi = (e + 4.f) * (1.f / (8.f * PGX_PI_F));
             norm = s_min(s_max(lo, norm), hi);
             float glossy = powf(s_max(h.z, 0.f), e);
             F3 diffuse = albedo_of(tv, m, sd) * PGX_INV_PI_F;
@@ -365,7 +374,7 @@ static __device__ __noinline__ float bsdf_pdf(const DevMaterial& m, const TexVie
             float e = plastic_exponent(m.alpha);
             float ks = fresnel_dielectric(dot(wol, h), m.int_ior, m.ext_ior);
             float kd = 1.f - ks;
-            float ph = (float)(((double)(e + 1.f) / (2.0 * PGX_PI_D)) * (double)powf(s_max(h.z, 0.f), e));
+            float ph = ((e + 1.f) * PGX_INV_2PI_F) * powf(s_max(h.z, 0.f), e);
             float gp = dot(wol, h) <= 0.f ? 0.f : (ph / (4.f * dot(wol, h)));
             float dp = cosine_pdf(wil);
             return (kd * dp) + (ks * gp);
@@ -537,7 +546,7 @@ static __device__ __noinline__ F3 bsdf_sample_s(const DevMaterial& m, const TexV
             if (rng.next() < F) {
                 float e = plastic_exponent(m.alpha);
                 float th = acosf(powf(1.f - r1, 1.f / (e + 1.f)));
-                float ph = (float)(2.0 * PGX_PI_D * (double)r2);
+                float ph = PGX_2PI_F * r2;
                 F3 h = normalize(spherical_to_world(th, ph));
                 wil = ((h * 2.f) * dot(wol, h)) - wol;
             } else {
@@ -574,7 +583,7 @@ static __device__ __noinline__ void bsdf_invert(const DevMaterial& m, const Shad
             float phi = spherical_phi(wl);
             float c = cosf(theta);
             u = c * c;
-            v = (float)((double)phi / (2.0 * PGX_PI_D));
+            v = phi * PGX_INV_2PI_F;
             break;
         }
         case PGX_BSDF_CONDUCTOR: {
@@ -591,7 +600,7 @@ static __device__ __noinline__ void bsdf_invert(const DevMaterial& m, const Shad
             float a1 = a2 - 1.f;
             float c = cosf(theta);
             u = (a2 / ((c * c) * (a1 * a1) + a1)) - (1.f / a1);
-            v = (float)((double)phi / (2.0 * PGX_PI_D));
+            v = phi * PGX_INV_2PI_F;
             break;
         }
         case PGX_BSDF_MIRROR:
@@ -635,19 +644,19 @@ __device__ __forceinline__ float sample_continuous(const float* func, const floa
 __device__ __forceinline__ F3 env_eval(const DevEnv& e, F3 wi) {
     if (!e.valid) return zero3();
     float u = atan2f(wi.z, wi.x);
-    u = (u < 0.f) ? (float)((double)u + 2.0 * PGX_PI_D) : u;
-    u = (float)((double)u / (2.0 * PGX_PI_D));
-    float v = (float)((double)acosf(wi.y) / PGX_PI_D);
+    u = (u < 0.f) ? u + PGX_2PI_F : u;
+    u = u * PGX_INV_2PI_F;
+    float v = acosf(wi.y) * PGX_INV_PI_F;
     return tex_sample_raw(e.texels, 0, e.width, e.height, u, v);
 }
 
 // Distribution2D::PDF (Sampling.h:203-208) via EnvironmentMap::PDF.
 static __device__ __noinline__ float env_pdf(const DevEnv& e, F3 wi) {
     float u = atan2f(wi.z, wi.x);
-    u = (u < 0.f) ? (float)((double)u + 2.0 * PGX_PI_D) : u;
-    u = (float)((double)u / (2.0 * PGX_PI_D));
-    float v = (float)((double)acosf(wi.y) / PGX_PI_D);
-    float st = (float)sinpi((double)v);  // sin(pi * v) of EnvironmentMap::PDF (Lights.h:188)
+    u = (u < 0.f) ? u + PGX_2PI_F : u;
+    u = u * PGX_INV_2PI_F;
+    float v = acosf(wi.y) * PGX_INV_PI_F;
+    float st = sinpif(v);  // sin(pi * v) of EnvironmentMap::PDF (Lights.h:188)
     if (st <= 0.f) return 0.f;
     float p;
     if (e.marg_int == 0.f) {
@@ -657,7 +666,7 @@ static __device__ __noinline__ float env_pdf(const DevEnv& e, F3 wi) {
         int iv = min(max((int)(v * (float)e.height), 0), e.height - 1);
         p = e.cond_func[(size_t)iv * e.width + iu] / e.marg_int;
     }
-    return (float)((double)p / (2.0 * PGX_PI_D * PGX_PI_D * (double)st));
+    return p / (PGX_2PI2_F * st);
 }
 
 // EnvironmentMap::sample: direction (y-up), emitted colour and solid-angle pdf.
@@ -670,11 +679,11 @@ static __device__ __noinline__ F3 env_sample(const DevEnv& e, uint64_t& rng, F3&
     float u = sample_continuous(e.cond_func + (size_t)dv * e.width, e.cond_cdf + (size_t)dv * (e.width + 1),
                                 e.cond_int[dv], e.width, ru, pu, du);
     float sp = pu * pv;
-    float theta = (float)(PGX_PI_D * (double)v);
-    float phi = (float)(2.0 * PGX_PI_D * (double)u);
+    float theta = PGX_PI_F * v;
+    float phi = PGX_2PI_F * u;
     float ct = cosf(theta), cp = cosf(phi), st = sinf(theta), sp_ = sinf(phi);
     F3 wi = f3(cp * st, ct, sp_ * st);
-    pdf = (st <= 0.f) ? 0.f : (float)((double)sp / (2.0 * PGX_PI_D * PGX_PI_D * (double)st));
+    pdf = (st <= 0.f) ? 0.f : sp / (PGX_2PI2_F * st);
     col = (pdf <= 0.f) ? zero3() : env_eval(e, wi);
     return wi;
 }

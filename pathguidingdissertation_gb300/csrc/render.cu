@@ -1054,9 +1054,9 @@ __device__ float conductor_dlogf_drough(const DevMaterial& m, F3 wil, F3 wol) {
 __device__ void env_scatter(const DevEnv& e, F3 wi, F3 g, float* grad) {
     if (!e.valid || !grad) return;
     float u = atan2f(wi.z, wi.x);
-    u = (u < 0.f) ? (float)((double)u + 2.0 * PGX_PI_D) : u;
-    u = (float)((double)u / (2.0 * PGX_PI_D));
-    float v = (float)((double)acosf(wi.y) / PGX_PI_D);
+    u = (u < 0.f) ? u + PGX_2PI_F : u;
+    u = u * PGX_INV_2PI_F;
+    float v = acosf(wi.y) * PGX_INV_PI_F;
     const int W = e.width, H = e.height;
     float uu = fmaxf(0.f, fabsf(u)) * (float)W;
     float vv = fmaxf(0.f, fabsf(v)) * (float)H;
