@@ -40,6 +40,9 @@ constexpr int kMaxDepthCap = 16;
 constexpr int kCollectionSPP = 128 / 8;  // Renderer.h:721
 constexpr int kStats = 8;                 // 64-bit statistics counters
 constexpr int kProfEvents = 4 * (kMaxDepthCap + 2);
+// Shading classes: paths of one depth are binned by what they hit and shaded
+// one class per launch, so every SM runs one class's code path at a time.
+constexpr int kShadeClasses = 6;  // miss, emitter, diffuse, conductor, glass, other
 
 // Per-path state, structure of arrays.
 struct PathState {
@@ -66,6 +69,8 @@ struct PathState {
     float4* rec_e;
     // counters: queue length per depth, shadow count per depth, stats
     unsigned* qcount;  // [kMaxDepthCap + 2]
+    int* cqueue;       // per class [kShadeClasses][capacity]
+    unsigned* ccount;  // [kMaxDepthCap + 2][kShadeClasses]
     unsigned* scount;  // [kMaxDepthCap + 2]
     unsigned* wcount;  // [2 * (kMaxDepthCap + 2)] persistent-traversal work counters
     unsigned long long* stats;  // [0] ext rays [1] shadow rays [2,3] extend nodes/tris [4,5] shadow nodes/tris
@@ -86,7 +91,7 @@ struct PathState {
 struct RenderState {
     DevBuf o, d, T, L, hit, pix, rng, flags, nrec, q0, q1, sh_path, sh_o, sh_d, sh_c;
     DevBuf rec_pos, rec_nrm, rec_wi, rec_w, rec_e;
-    DevBuf counters, vertices;
+    DevBuf counters, vertices, cqueue, ccount;
     DevBuf guide, rec_wo, rec_f, train, scene;
     int64_t capacity = 0;
     int rec_depth = 0;
@@ -577,11 +582,43 @@ __device__ __forceinline__ void push_shadow(PathState& ps, int depth, int p, flo
     }
 }
 
-template <int MODE, bool BATCH = false>
-__global__ void __launch_bounds__(kThreads, 8) k_shade(SceneView sv0, PathState ps, FrameParams fp, int depth,
-                                                    GuideView gv, const BatchInfo* binfo = nullptr) {
+// Bins the paths of this depth by shading class (k_shade then runs once per
+// class on its bin).
+__global__ void __launch_bounds__(kThreads) k_classify(SceneView sv, PathState ps, int depth) {
     const unsigned n = ps.qcount[depth];
     const int* __restrict__ q = ps.queue[depth & 1];
+    unsigned* cc = ps.ccount + depth * kShadeClasses;
+    const unsigned stride = gridDim.x * blockDim.x;
+    const unsigned first = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned rounds = (n + stride - 1) / stride;
+    for (unsigned r = 0; r < rounds; r++) {
+        unsigned i = first + r * stride;
+        bool active = i < n;
+        int p = active ? q[i] : 0;
+        int cls = 0;
+        if (active) {
+            int id = __float_as_int(ps.hit[p].x);
+            if (id >= 0) {
+                const DevMaterial& m = sv.mats[__float_as_int(sv.shade[id].vv.w)];
+                cls = m.is_light ? 1
+                                 : (m.kind == PGX_BSDF_DIFFUSE ? 2
+                                                              : (m.kind == PGX_BSDF_CONDUCTOR ? 3 : (m.kind == PGX_BSDF_GLASS ? 4 : 5)));
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < kShadeClasses; c++) {
+            unsigned slot = warp_aggregated_add(&cc[c], active && cls == c);
+            if (active && cls == c) ps.cqueue[(size_t)c * ps.capacity + slot] = p;
+        }
+    }
+}
+
+template <int MODE, bool BATCH = false>
+__global__ void __launch_bounds__(kThreads, 8) k_shade(SceneView sv0, PathState ps, FrameParams fp, int depth,
+                                                    GuideView gv, const BatchInfo* binfo = nullptr, int cls = -1) {
+    // the whole queue of this depth (cls < 0) or one class's bin
+    const unsigned n = cls < 0 ? ps.qcount[depth] : ps.ccount[depth * kShadeClasses + cls];
+    const int* __restrict__ q = cls < 0 ? ps.queue[depth & 1] : ps.cqueue + (size_t)cls * ps.capacity;
     int* __restrict__ qn = ps.queue[(depth + 1) & 1];
     const int64_t cap = ps.capacity;
     // Uniform trip count per warp so the warp-aggregated appends see whole warps.
@@ -1448,6 +1485,8 @@ int ensure_state(pgx_ctx* ctx, RenderState* rs, int64_t cap, int rec_depth, int6
         rs->tcapacity = tcap;
     }
     if (batch) PGX_CUDA_TRY(ctx, rs->scene.reserve(sizeof(int) * rs->capacity));
+    PGX_CUDA_TRY(ctx, rs->cqueue.reserve(sizeof(int) * kShadeClasses * rs->capacity));
+    PGX_CUDA_TRY(ctx, rs->ccount.reserve(sizeof(unsigned) * kShadeClasses * (kMaxDepthCap + 2)));
     PGX_CUDA_TRY(ctx, rs->counters.reserve(sizeof(unsigned) * 4 * (kMaxDepthCap + 2) + sizeof(unsigned long long) * kStats +
                                            sizeof(unsigned) * 4));
     if (!rs->ev0) {
@@ -1482,6 +1521,8 @@ PathState path_view(RenderState* rs) {
     ps.rec_e = rs->rec_e.as<float4>();
     unsigned* c = rs->counters.as<unsigned>();
     ps.qcount = c;
+    ps.cqueue = rs->cqueue.as<int>();
+    ps.ccount = rs->ccount.as<unsigned>();
     ps.scount = c + (kMaxDepthCap + 2);
     ps.wcount = c + 2 * (kMaxDepthCap + 2);
     ps.stats = reinterpret_cast<unsigned long long*>(c + 4 * (kMaxDepthCap + 2));
@@ -1536,6 +1577,7 @@ int enqueue_frame(pgx_ctx* ctx, RenderState* rs, const FrameParams& fp, cudaStre
     const bool prof = fp.profile != 0;
     int launches = 0;
     cudaMemsetAsync(ps.qcount, 0, sizeof(unsigned) * 4 * (kMaxDepthCap + 2), s);
+    cudaMemsetAsync(ps.ccount, 0, sizeof(unsigned) * kShadeClasses * (kMaxDepthCap + 2), s);
     k_camgen<<<g, kThreads, 0, s>>>(sv, ps, fp);
     launches++;
     for (int depth = 0; depth <= fp.max_depth; depth++) {
@@ -1553,21 +1595,24 @@ int enqueue_frame(pgx_ctx* ctx, RenderState* rs, const FrameParams& fp, cudaStre
             k_guide_infer<<<ig, 128 * kInferGroups, kInferSmem, s>>>(sv, ps, depth, mv, mlp_status);
             launches++;
         }
-        switch (fp.mode) {
-            case PGX_MODE_GUIDED_LI:
-                k_shade<PGX_MODE_GUIDED_LI><<<g, kThreads, 0, s>>>(sv, ps, fp, depth, gv);
-                break;
-            case PGX_MODE_GUIDED_QUADTREE:
-                k_shade<PGX_MODE_GUIDED_QUADTREE><<<g, kThreads, 0, s>>>(sv, ps, fp, depth, gv);
-                break;
-            case PGX_MODE_GUIDED_MLP:
-                k_shade<PGX_MODE_GUIDED_MLP><<<g, kThreads, 0, s>>>(sv, ps, fp, depth, gv);
-                break;
-            default:
-                k_shade<PGX_MODE_PLAIN><<<g, kThreads, 0, s>>>(sv, ps, fp, depth, gv);
-                break;
+        k_classify<<<g, kThreads, 0, s>>>(sv, ps, depth);
+        for (int c = 0; c < kShadeClasses; c++) {
+            switch (fp.mode) {
+                case PGX_MODE_GUIDED_LI:
+                    k_shade<PGX_MODE_GUIDED_LI><<<g, kThreads, 0, s>>>(sv, ps, fp, depth, gv, nullptr, c);
+                    break;
+                case PGX_MODE_GUIDED_QUADTREE:
+                    k_shade<PGX_MODE_GUIDED_QUADTREE><<<g, kThreads, 0, s>>>(sv, ps, fp, depth, gv, nullptr, c);
+                    break;
+                case PGX_MODE_GUIDED_MLP:
+                    k_shade<PGX_MODE_GUIDED_MLP><<<g, kThreads, 0, s>>>(sv, ps, fp, depth, gv, nullptr, c);
+                    break;
+                default:
+                    k_shade<PGX_MODE_PLAIN><<<g, kThreads, 0, s>>>(sv, ps, fp, depth, gv, nullptr, c);
+                    break;
+            }
         }
-        launches += 2;
+        launches += 2 + kShadeClasses;
         if (prof) cudaEventRecord(rs->prof[4 * depth + 2], s);
         if (fp.mode != PGX_MODE_GUIDED_LI) {
             if (prof)
