@@ -59,6 +59,12 @@ struct DevMaterial {
     float alb_off[3];  // added to the sampled albedo (0 except in differentiable renders)
 };
 
+// Shading class of a surface (the wavefront shades one class per launch):
+// 1 emitter, 2 diffuse, 3 conductor, 4 glass, 5 other; 0 is a miss.
+__host__ __device__ inline unsigned char shade_class(const DevMaterial& m) {
+    return m.is_light ? 1 : (m.kind == PGX_BSDF_DIFFUSE ? 2 : (m.kind == PGX_BSDF_CONDUCTOR ? 3 : (m.kind == PGX_BSDF_GLASS ? 4 : 5)));
+}
+
 struct DevTexture {
     int width, height;
     long long offset;  // first texel in the texel pool (float3 units)
@@ -121,6 +127,7 @@ struct pgx_ctx {
     int32_t n_area_lights = 0;
     DevBuf tris_in;            // pgx_triangle[ntris]
     DevBuf shade;              // TriShade[ntris]
+    DevBuf tri_class;          // shade_class of each triangle's material (uint8)
     DevBuf mats;               // DevMaterial[nmats]
     DevBuf textures;           // DevTexture[ntex]
     DevBuf texels;             // float3 pool

@@ -116,6 +116,7 @@ struct RenderState {
 struct SceneView {
     BvhView bvh;
     const TriShade* __restrict__ shade;
+    const unsigned char* __restrict__ tri_class;
     const DevMaterial* __restrict__ mats;
     const DevAreaLight* __restrict__ lights;
     TexView tex;
@@ -598,12 +599,7 @@ __global__ void __launch_bounds__(kThreads) k_classify(SceneView sv, PathState p
         int cls = 0;
         if (active) {
             int id = __float_as_int(ps.hit[p].x);
-            if (id >= 0) {
-                const DevMaterial& m = sv.mats[__float_as_int(sv.shade[id].vv.w)];
-                cls = m.is_light ? 1
-                                 : (m.kind == PGX_BSDF_DIFFUSE ? 2
-                                                              : (m.kind == PGX_BSDF_CONDUCTOR ? 3 : (m.kind == PGX_BSDF_GLASS ? 4 : 5)));
-            }
+            if (id >= 0) cls = sv.tri_class[id];
         }
 #pragma unroll
         for (int c = 0; c < kShadeClasses; c++) {
@@ -1544,6 +1540,7 @@ SceneView scene_view(pgx_ctx* ctx) {
     SceneView sv;
     sv.bvh = bvh_view(ctx);
     sv.shade = ctx->shade.as<TriShade>();
+    sv.tri_class = ctx->tri_class.as<unsigned char>();
     sv.mats = ctx->mats.as<DevMaterial>();
     sv.lights = ctx->lights.as<DevAreaLight>();
     sv.tex.info = ctx->textures.as<DevTexture>();
@@ -2128,10 +2125,13 @@ int batch_enqueue(pgx_batch* b, int64_t total, int depth, const pgx_batch_tuning
         BatchWave bw{info, b->d_prefix.as<int64_t>(), (int)b->ctx.size(), base, std::min<int64_t>(tu.wave_paths, total - base),
                      b->d_seed.as<uint64_t>()};
         cudaMemsetAsync(ps.qcount, 0, sizeof(unsigned) * 4 * (kMaxDepthCap + 2), s);
+        cudaMemsetAsync(ps.ccount, 0, sizeof(unsigned) * kShadeClasses * (kMaxDepthCap + 2), s);
         k_camgen_batch<<<sg, kThreads, 0, s>>>(ps, bw);
         for (int d = 0; d <= depth; d++) {
             k_extend<false, true><<<tg, kThreads, 0, s>>>(sv, ps, d, info);
-            k_shade<PGX_MODE_PLAIN, true><<<sg, kThreads, 0, s>>>(sv, ps, fp, d, gv, info);
+            k_classify<<<sg, kThreads, 0, s>>>(sv, ps, d);
+            for (int c = 0; c < kShadeClasses; c++)
+                k_shade<PGX_MODE_PLAIN, true><<<sg, kThreads, 0, s>>>(sv, ps, fp, d, gv, info, c);
             k_shadow<false, true><<<tg, kThreads, 0, s>>>(sv, ps, d, info);
         }
         k_finalize_batch<<<sg, kThreads, 0, s>>>(ps, bw);
@@ -2183,7 +2183,8 @@ extern "C" int pgx_batch_create(pgx_ctx* const* scenes, int32_t n, pgx_batch** o
         h->mats.reserve(sizeof(DevMaterial) * mats) != cudaSuccess ||
         h->textures.reserve(sizeof(DevTexture) * std::max<int64_t>(texs, 1)) != cudaSuccess ||
         h->texels.reserve(sizeof(float) * 3 * std::max<int64_t>(texels, 1)) != cudaSuccess ||
-        h->lights.reserve(sizeof(DevAreaLight) * lights) != cudaSuccess || b->d_info.reserve(sizeof(BatchInfo) * n) != cudaSuccess ||
+        h->lights.reserve(sizeof(DevAreaLight) * lights) != cudaSuccess || h->tri_class.reserve(tris) != cudaSuccess ||
+        b->d_info.reserve(sizeof(BatchInfo) * n) != cudaSuccess ||
         b->d_prefix.reserve(sizeof(int64_t) * (n + 1)) != cudaSuccess || b->d_seed.reserve(sizeof(uint64_t)) != cudaSuccess)
         return fail(PGX_ERR_OOM);
     cudaStream_t s = h->stream;
@@ -2205,6 +2206,8 @@ extern "C" int pgx_batch_create(pgx_ctx* const* scenes, int32_t n, pgx_batch** o
                   cudaMemcpyAsync(h->texels.as<float>() + 3 * eb, c->texels.p, sizeof(float) * 3 * c->ntexels,
                                   cudaMemcpyDeviceToDevice, s) == cudaSuccess &&
                   cudaMemcpyAsync(h->lights.as<DevAreaLight>() + lb, c->lights.p, sizeof(DevAreaLight) * c->n_area_lights,
+                                  cudaMemcpyDeviceToDevice, s) == cudaSuccess &&
+                  cudaMemcpyAsync(h->tri_class.as<unsigned char>() + tb, c->tri_class.p, (size_t)c->ntris,
                                   cudaMemcpyDeviceToDevice, s) == cudaSuccess;
         if (!ok) return fail(PGX_ERR_CUDA);
         const unsigned g = 256;

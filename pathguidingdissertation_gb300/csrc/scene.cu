@@ -303,6 +303,13 @@ extern "C" int pgx_scene_upload(pgx_ctx* ctx, const pgx_triangle* tris, int64_t 
                                                            ctx->shade.as<TriShade>());
         PGX_CUDA_TRY(ctx, cudaGetLastError());
     }
+    PGX_CUDA_TRY(ctx, ctx->tri_class.reserve(std::max<int64_t>(ntris, 1)));
+    if (ntris > 0) {
+        std::vector<unsigned char> cls((size_t)ntris);
+        for (int64_t i = 0; i < ntris; i++) cls[(size_t)i] = shade_class(dm[tris[i].material]);
+        PGX_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->tri_class.p, cls.data(), (size_t)ntris, cudaMemcpyHostToDevice, s));
+        PGX_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    }
 
     // Scene bounds (Scene::init Scene.h:130-135; SceneLoader.h:267-268).
     float bmn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, bmx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
