@@ -91,6 +91,52 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+class Ranks:
+    """One process per GPU under torchrun.  The path does not shard (pixels
+    and samples are independent), so N ranks are N replicas rendering their
+    own samples; the only communication is the timing: barriers around the
+    timed steps, sums of the units and the maximum of the times."""
+
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = False
+        self.device = "cpu"
+
+    def init(self, backend: str) -> None:
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            if backend == "nccl":
+                torch.cuda.set_device(self.local)
+            dist.init_process_group(backend=backend)
+            self.pg = True
+            self.device = f"cuda:{self.local}" if backend == "nccl" else "cpu"
+
+    def barrier(self) -> None:
+        if self.pg:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def reduce(self, x: float, op: str = "sum") -> float:
+        """Sum or maximum of x over the ranks (x itself with one rank)."""
+        if not self.pg:
+            return float(x)
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([float(x)], dtype=torch.float64, device=self.device)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM if op == "sum" else dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self) -> None:
+        if self.pg:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+            self.pg = False
+
+
 def measured_peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -138,11 +184,20 @@ def run_pgx(args) -> dict:
     from pathguidingdissertation_gb300 import build as pkg_build
     from pathguidingdissertation_gb300.api import Context
 
-    pkg_build.build()
+    ranks = Ranks()
+    if ranks.rank == 0:
+        pkg_build.build()
+    ranks.init("nccl")
+    if ranks.rank != 0:
+        ranks.barrier()
+        pkg_build.build()  # rank 0 compiled it; this only loads
+    else:
+        ranks.barrier()
     desc, depth, wl = make_workload(args.workload)
     mode = {"plain": abi.MODE_PLAIN, "guided_quadtree": abi.MODE_GUIDED_QUADTREE,
             "guided_mlp": abi.MODE_GUIDED_MLP}[args.mode]
-    ctx = Context(0)
+    seed = 1 + 1000003 * ranks.rank  # each replica renders its own samples
+    ctx = Context(ranks.local)
     ctx.upload(desc)
     ctx.bvh_build()
     if mode == abi.MODE_GUIDED_QUADTREE:
@@ -157,8 +212,9 @@ def run_pgx(args) -> dict:
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     spp = args.spp_per_step
     for i in range(args.warmup):
-        ctx.render(spp, mode=mode, seed=1, max_depth=depth, profile=True)
+        ctx.render(spp, mode=mode, seed=seed, max_depth=depth, profile=True)
     torch.cuda.synchronize()
+    ranks.barrier()
     rays = paths = ext_rays = 0
     ms = ms_ext = ms_shade = 0.0
     ext_visits = ext_tris = ext_launches = launches = 0
@@ -166,7 +222,7 @@ def run_pgx(args) -> dict:
         for k in range(args.steps):
             flush.zero_()
             torch.cuda.synchronize()
-            ctx.render(spp, mode=mode, seed=1, max_depth=depth, profile=True)
+            ctx.render(spp, mode=mode, seed=seed, max_depth=depth, profile=True)
             st = ctx.render_stats()
             rays += st.extension_rays + st.shadow_rays
             paths += st.paths
@@ -179,8 +235,13 @@ def run_pgx(args) -> dict:
             ext_launches += st.extend_launches
             launches += st.kernel_launches
         torch.cuda.synchronize()
+        ranks.barrier()
     clocks = clk.summary()
-    value = rays / (ms * 1e-3) / 1e6
+    # whole job: every replica's rays over the slowest replica's device time
+    ms_max = ranks.reduce(ms, "max")
+    rays_all = ranks.reduce(rays, "sum")
+    paths_all = ranks.reduce(paths, "sum")
+    value = rays_all / (ms_max * 1e-3) / 1e6
 
     # End to end through the C ABI: camera from host, render, film to pinned host memory.
     H, W = desc.camera["height"], desc.camera["width"]
@@ -188,9 +249,10 @@ def run_pgx(args) -> dict:
     import ctypes as C
     from pathguidingdissertation_gb300.api import camera_struct
     cam = camera_struct(desc.camera)
-    cfg = abi.RenderConfig(mode, depth, 1, 0.5, 0, 0)
+    cfg = abi.RenderConfig(mode, depth, seed, 0.5, 0, 0)
     spp_read = C.c_int32()
     e2e_rays = 0
+    ranks.barrier()
     t0 = time.perf_counter()
     for k in range(args.steps):
         ctx.check(ctx.lib.pgx_set_camera(ctx.h, C.byref(cam)))
@@ -199,6 +261,8 @@ def run_pgx(args) -> dict:
         st = ctx.render_stats()
         e2e_rays += st.extension_rays + st.shadow_rays
     e2e_s = time.perf_counter() - t0
+    ranks.barrier()
+    e2e_value = ranks.reduce(e2e_rays, "sum") / ranks.reduce(e2e_s, "max") / 1e6
     ctx.close()
 
     peaks = measured_peaks()
@@ -237,27 +301,31 @@ def run_pgx(args) -> dict:
         "note": "latency-bound (dependent gathers of shading data, 64 registers); traffic not captured",
     }
     print("[bench] device runs done; CPU baseline next", file=sys.stderr, flush=True)
-    cpu = cpu_baseline_reference(desc) if not args.no_cpu_baseline else None
+    cpu = cpu_baseline_reference(desc) if not args.no_cpu_baseline and ranks.world == 1 else None
     print("[bench] CPU baseline done", file=sys.stderr, flush=True)
+    ranks.close()
+    if ranks.rank != 0:
+        return None
     return {
         "metric": "Mrays/s",
         "value": value,
         "unit": "Mrays/s",
-        "n_gpus": 1,
+        "n_gpus": ranks.world,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": ms / args.steps,
+        "ms_per_step": ms_max / args.steps,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded procedural scene)",
-        "config": {"workload": wl, "mode": args.mode, "paths_per_step": paths // max(args.steps, 1),
-                   "spp_per_step": spp, "l2": "flushed (256 MiB write) before every timed step"},
-        "mpaths_per_s": paths / (ms * 1e-3) / 1e6,
+        "config": {"workload": wl, "mode": args.mode, "paths_per_step": int(paths_all) // max(args.steps, 1),
+                   "spp_per_step": spp, "l2": "flushed (256 MiB write) before every timed step",
+                   "parallelism": "replicas" if ranks.world > 1 else "1 GPU"},
+        "mpaths_per_s": paths_all / (ms_max * 1e-3) / 1e6,
         "rays_per_path": rays / max(paths, 1),
         "gpu_launches": launches,
-        "e2e": {"value": e2e_rays / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": C.sizeof(abi.Camera),
+        "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": C.sizeof(abi.Camera),
                 "d2h_bytes_per_step": H * W * 3 * 4},
         "roofline": roofline,
         "roofline_shade": roofline_shade,
@@ -779,11 +847,16 @@ def main() -> None:
     ap.add_argument("--batch-max-tris", type=float, default=2e6)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
-    if args.gpus != 1 or int(os.environ.get("WORLD_SIZE", "1")) != 1:
-        # The path is replicated, not sharded; this build runs on one GPU.
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.gpus != world:
         if rank == 0:
-            print(json.dumps({"impl": args.impl, "unavailable": "one GPU per run: use --gpus 1"}))
+            print(json.dumps({"impl": args.impl, "unavailable": f"--gpus {args.gpus} needs one process per GPU "
+                                                                "(torchrun --nproc-per-node N)"}))
         return
+    if world > 1 and (args.impl == "reference" or args.study):
+        # the reference arm and the studies run on rank 0 alone
+        if rank != 0:
+            return
     if args.warmup < 0 or args.steps < 1:
         raise SystemExit("--steps must be >= 1 and --warmup >= 0")
     if args.study == "relmse":
@@ -799,7 +872,8 @@ def main() -> None:
         print(json.dumps(run_batch_study(args)))
         return
     out = run_reference(args) if args.impl == "reference" else run_pgx(args)
-    print(json.dumps(out))
+    if out is not None:
+        print(json.dumps(out))
 
 
 if __name__ == "__main__":
