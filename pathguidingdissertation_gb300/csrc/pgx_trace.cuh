@@ -138,6 +138,23 @@ __device__ __forceinline__ bool bvh_trace(const BvhView& bvh, const xv3& o, cons
 }
 
 // ---- persistent traversal with lane refill ----------------------------------
+// Stack of one lane of the persistent traversal: the top kShortStack entries
+// live in shared memory (one column per thread of the block, so a warp's
+// accesses fall in distinct banks), deeper ones spill to local memory.
+constexpr int kShortStack = 8;
+constexpr int kTraceMaxBlock = 128;  // block size of every kernel using trace_persistent
+struct TraceStack {
+    int2* sh;  // this thread's column: entry i at sh[i * kTraceMaxBlock]
+    int2 loc[PGX_STACK_SIZE - kShortStack];
+    __device__ __forceinline__ void put(int i, int2 v) {
+        if (i < kShortStack)
+            sh[i * kTraceMaxBlock] = v;
+        else
+            loc[i - kShortStack] = v;
+    }
+    __device__ __forceinline__ int2 get(int i) const { return i < kShortStack ? sh[i * kTraceMaxBlock] : loc[i - kShortStack]; }
+};
+
 // The same per-ray algorithm as bvh_trace, cut into steps (one interior node
 // or one triangle) so that a warp can keep stepping while its lanes finish at
 // different times: every few steps, lanes whose ray is done fetch the next
@@ -186,7 +203,7 @@ struct SceneRoot {
 // One step; returns true when the ray is finished (for ANY, hit_id >= 0
 // marks an occluder).
 template <bool ANY, bool COUNT>
-__device__ __forceinline__ bool lane_step(const BvhView& bvh, TraceLane& L, int2* stack, unsigned long long& n_interior,
+__device__ __forceinline__ bool lane_step(const BvhView& bvh, TraceLane& L, TraceStack& stack, unsigned long long& n_interior,
                                           unsigned long long& n_tris) {
     if (L.cnt > 0) {
         if ((unsigned)L.ref > (unsigned)bvh.n_tris || L.cnt > bvh.n_tris - L.ref) {
@@ -216,8 +233,11 @@ __device__ __forceinline__ bool lane_step(const BvhView& bvh, TraceLane& L, int2
         L.k = 0;
         if (L.sp == 0) return true;
         --L.sp;
-        L.ref = stack[L.sp].x;
-        L.cnt = stack[L.sp].y;
+        {
+            int2 e = stack.get(L.sp);
+            L.ref = e.x;
+            L.cnt = e.y;
+        }
         return false;
     }
     if (COUNT) n_interior++;
@@ -254,8 +274,11 @@ __device__ __forceinline__ bool lane_step(const BvhView& bvh, TraceLane& L, int2
     if (dl == FLT_MAX) {
         if (L.sp == 0) return true;
         --L.sp;
-        L.ref = stack[L.sp].x;
-        L.cnt = stack[L.sp].y;
+        {
+            int2 e = stack.get(L.sp);
+            L.ref = e.x;
+            L.cnt = e.y;
+        }
         return false;
     }
     L.ref = nref;
@@ -265,7 +288,7 @@ __device__ __forceinline__ bool lane_step(const BvhView& bvh, TraceLane& L, int2
             L.status = 1;
             return true;
         }
-        stack[L.sp] = make_int2(fref, fcnt);
+        stack.put(L.sp, make_int2(fref, fcnt));
         L.sp++;
     }
     return false;
@@ -285,7 +308,9 @@ __device__ __forceinline__ void trace_persistent(const BvhView& bvh, unsigned n,
     constexpr int kMaxSteps = 64;
     constexpr int kCheckEvery = 8;    // steps between occupancy votes
     const int lane = threadIdx.x & 31;
-    int2 stack[PGX_STACK_SIZE];
+    __shared__ int2 s_stack[kShortStack * kTraceMaxBlock];
+    TraceStack stack;
+    stack.sh = s_stack + threadIdx.x;
     TraceLane L;
     int ray = -1;
     bool exhausted = false;
