@@ -584,28 +584,58 @@ __device__ __forceinline__ void push_shadow(PathState& ps, int depth, int p, flo
 }
 
 // Bins the paths of this depth by shading class (k_shade then runs once per
-// class on its bin).
+// class on its bin).  Each block takes tiles of kClassifyTile queue entries,
+// kClassifyItems per thread so the hit and class gathers overlap; entries are
+// ranked within their class by warp match + shared-memory counters and each
+// class bin is reserved with ONE global atomic per tile (a warp-level append
+// would put ~n/32 atomics on each of the six counters).
+constexpr int kClassifyItems = 8;
+constexpr unsigned kClassifyTile = kThreads * kClassifyItems;
+
 __global__ void __launch_bounds__(kThreads) k_classify(SceneView sv, PathState ps, int depth) {
+    __shared__ unsigned s_count[kShadeClasses];
+    __shared__ unsigned s_base[kShadeClasses];
     const unsigned n = ps.qcount[depth];
     const int* __restrict__ q = ps.queue[depth & 1];
     unsigned* cc = ps.ccount + depth * kShadeClasses;
-    const unsigned stride = gridDim.x * blockDim.x;
-    const unsigned first = blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned rounds = (n + stride - 1) / stride;
-    for (unsigned r = 0; r < rounds; r++) {
-        unsigned i = first + r * stride;
-        bool active = i < n;
-        int p = active ? q[i] : 0;
-        int cls = 0;
-        if (active) {
-            int id = __float_as_int(ps.hit[p].x);
-            if (id >= 0) cls = sv.tri_class[id];
+    const unsigned tiles = (n + kClassifyTile - 1) / kClassifyTile;
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    for (unsigned t = blockIdx.x; t < tiles; t += gridDim.x) {  // block-uniform trip count
+        if (threadIdx.x < kShadeClasses) s_count[threadIdx.x] = 0;
+        int p[kClassifyItems], cls[kClassifyItems];
+        unsigned rank[kClassifyItems];
+#pragma unroll
+        for (int j = 0; j < kClassifyItems; j++) {
+            const unsigned i = t * kClassifyTile + j * kThreads + threadIdx.x;
+            p[j] = i < n ? q[i] : -1;
         }
 #pragma unroll
-        for (int c = 0; c < kShadeClasses; c++) {
-            unsigned slot = warp_aggregated_add(&cc[c], active && cls == c);
-            if (active && cls == c) ps.cqueue[(size_t)c * ps.capacity + slot] = p;
+        for (int j = 0; j < kClassifyItems; j++) {
+            cls[j] = -1;
+            if (p[j] >= 0) {
+                const int id = __float_as_int(ps.hit[p[j]].x);
+                cls[j] = id >= 0 ? (int)sv.tri_class[id] : 0;
+            }
         }
+        __syncthreads();  // counters cleared
+#pragma unroll
+        for (int j = 0; j < kClassifyItems; j++) {
+            const unsigned m = __match_any_sync(0xFFFFFFFFu, cls[j]);
+            const int leader = __ffs(m) - 1;
+            unsigned base = 0;
+            if (lane == leader && cls[j] >= 0) base = atomicAdd(&s_count[cls[j]], __popc(m));
+            rank[j] = __shfl_sync(0xFFFFFFFFu, base, leader) + __popc(m & below);
+        }
+        __syncthreads();  // tile counts complete
+        if (threadIdx.x < kShadeClasses) {
+            const unsigned c = s_count[threadIdx.x];
+            s_base[threadIdx.x] = c ? atomicAdd(&cc[threadIdx.x], c) : 0u;
+        }
+        __syncthreads();  // bin bases published
+#pragma unroll
+        for (int j = 0; j < kClassifyItems; j++)
+            if (cls[j] >= 0) ps.cqueue[(size_t)cls[j] * ps.capacity + s_base[cls[j]] + rank[j]] = p[j];
     }
 }
 
@@ -1592,7 +1622,7 @@ int enqueue_frame(pgx_ctx* ctx, RenderState* rs, const FrameParams& fp, cudaStre
             k_guide_infer<<<ig, 128 * kInferGroups, kInferSmem, s>>>(sv, ps, depth, mv, mlp_status);
             launches++;
         }
-        k_classify<<<g, kThreads, 0, s>>>(sv, ps, depth);
+        k_classify<<<grid_for((n + kClassifyItems - 1) / kClassifyItems), kThreads, 0, s>>>(sv, ps, depth);
         for (int c = 0; c < kShadeClasses; c++) {
             switch (fp.mode) {
                 case PGX_MODE_GUIDED_LI:
@@ -2129,7 +2159,7 @@ int batch_enqueue(pgx_batch* b, int64_t total, int depth, const pgx_batch_tuning
         k_camgen_batch<<<sg, kThreads, 0, s>>>(ps, bw);
         for (int d = 0; d <= depth; d++) {
             k_extend<false, true><<<tg, kThreads, 0, s>>>(sv, ps, d, info);
-            k_classify<<<sg, kThreads, 0, s>>>(sv, ps, d);
+            k_classify<<<grid_for((bw.count + kClassifyItems - 1) / kClassifyItems), kThreads, 0, s>>>(sv, ps, d);
             for (int c = 0; c < kShadeClasses; c++)
                 k_shade<PGX_MODE_PLAIN, true><<<sg, kThreads, 0, s>>>(sv, ps, fp, d, gv, info, c);
             k_shadow<false, true><<<tg, kThreads, 0, s>>>(sv, ps, d, info);
