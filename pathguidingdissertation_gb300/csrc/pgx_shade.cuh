@@ -154,12 +154,19 @@ static __device__ float fresnel_dielectric(float cos_theta, float ior_int, float
     return (par * par + perp * perp) * 0.5f;
 }
 
-static __device__ __noinline__ F3 fresnel_conductor(float cos_theta, const float* ior, const float* k) {
+// Each BSDF routine below has a force-inlined core (suffix _i, or a template
+// on the material kind K) and an out-of-line entry point of the original name
+// for the generic shading path.  A wavefront launch that shades a single
+// surface class instantiates the cores with its kind known at compile time:
+// the other kinds' code disappears and no material, shading frame or scene
+// view has to be spilled to local memory to be passed by reference.
+__device__ __forceinline__ F3 fresnel_conductor_i(float cos_theta, const float* ior, const float* k) {
     float ci = s_max(s_min(cos_theta, 1.f), -1.f);
     float ci_sq = s_max(ci * ci, 0.f);
     float si_sq = s_max(1.f - ci_sq, 0.f);
     F3 out;
     float* o = &out.x;
+#pragma unroll
     for (int c = 0; c < 3; c++) {
         float n2 = ior[c] * ior[c];
         float k2 = k[c] * k[c];
@@ -169,6 +176,16 @@ static __device__ __noinline__ F3 fresnel_conductor(float cos_theta, const float
         o[c] = (par + perp) * 0.5f;
     }
     return out;
+}
+static __device__ __noinline__ F3 fresnel_conductor(float cos_theta, const float* ior, const float* k) {
+    return fresnel_conductor_i(cos_theta, ior, k);
+}
+template <int K>
+__device__ __forceinline__ F3 fresnel_conductor_k(float cos_theta, const float* ior, const float* k) {
+    if constexpr (K < 0)
+        return fresnel_conductor(cos_theta, ior, k);
+    else
+        return fresnel_conductor_i(cos_theta, ior, k);
 }
 
 __device__ __forceinline__ float lambda_ggx(F3 wi, float alpha) {
@@ -215,8 +232,9 @@ __device__ __forceinline__ float cosine_pdf(F3 wl) {
 }
 
 // ---- BSDF dispatch ------------------------------------------------------------
-__device__ __forceinline__ bool bsdf_pure_specular(const DevMaterial& m) {
-    switch (m.kind) {
+template <int K>
+__device__ __forceinline__ bool bsdf_pure_specular_k(const DevMaterial& m) {
+    switch (K >= 0 ? K : m.kind) {
         case PGX_BSDF_MIRROR:
         case PGX_BSDF_GLASS:
             return true;
@@ -227,12 +245,14 @@ __device__ __forceinline__ bool bsdf_pure_specular(const DevMaterial& m) {
             return false;
     }
 }
+__device__ __forceinline__ bool bsdf_pure_specular(const DevMaterial& m) { return bsdf_pure_specular_k<-1>(m); }
 __device__ __forceinline__ bool bsdf_two_sided(const DevMaterial& m) {
     if (m.layered) return true;  // LayeredBSDF::isTwoSided, Materials.h:895
     return !(m.kind == PGX_BSDF_GLASS || m.kind == PGX_BSDF_DIELECTRIC);
 }
 
-static __device__ __noinline__ F3 conductor_eval(const DevMaterial& m, F3 alb, F3 wil, F3 wol) {
+template <int K>
+__device__ __forceinline__ F3 conductor_eval_i(const DevMaterial& m, F3 alb, F3 wil, F3 wol) {
     if (wil.z <= 0.f || wol.z <= 0.f) return zero3();
     if (m.alpha < PGX_EPSILON) return zero3();
     F3 h = wil + wol;
@@ -242,8 +262,18 @@ static __device__ __noinline__ F3 conductor_eval(const DevMaterial& m, F3 alb, F
     if (wil.z * wol.z <= 0.f) return zero3();
     float G = g_ggx(wil, wol, m.alpha);
     float D = d_ggx(h, m.alpha);
-    F3 F = fresnel_conductor(dot(wol, h), m.eta, m.k);
+    F3 F = fresnel_conductor_k<K>(dot(wol, h), m.eta, m.k);
     return alb * divs((F * G) * D, (4.f * wil.z) * wol.z);
+}
+static __device__ __noinline__ F3 conductor_eval(const DevMaterial& m, F3 alb, F3 wil, F3 wol) {
+    return conductor_eval_i<-1>(m, alb, wil, wol);
+}
+template <int K>
+__device__ __forceinline__ F3 conductor_eval_k(const DevMaterial& m, F3 alb, F3 wil, F3 wol) {
+    if constexpr (K < 0)
+        return conductor_eval(m, alb, wil, wol);
+    else
+        return conductor_eval_i<K>(m, alb, wil, wol);
 }
 static __device__ float conductor_pdf(const DevMaterial& m, F3 wil, F3 wol) {
     if (wil.z <= 0.f || wol.z <= 0.f) return 0.f;
@@ -258,7 +288,7 @@ static __device__ float conductor_pdf(const DevMaterial& m, F3 wil, F3 wol) {
 }
 
 // Rough dielectric eval/pdf (Materials.h:545-634).
-static __device__ __noinline__ void dielectric_eval_pdf(const DevMaterial& m, F3 alb, F3 wol, F3 wil, F3* f, float* pdf) {
+__device__ __forceinline__ void dielectric_eval_pdf_i(const DevMaterial& m, F3 alb, F3 wol, F3 wil, F3* f, float* pdf) {
     if (f) *f = zero3();
     if (pdf) *pdf = 0.f;
     if (wol.z == 0.f || wil.z == 0.f) return;
@@ -294,6 +324,16 @@ static __device__ __noinline__ void dielectric_eval_pdf(const DevMaterial& m, F3
         if (pdf) *pdf = (1.f - F) * ((D * fabsf(dot(wol, h))) / den);
     }
 }
+static __device__ __noinline__ void dielectric_eval_pdf(const DevMaterial& m, F3 alb, F3 wol, F3 wil, F3* f, float* pdf) {
+    dielectric_eval_pdf_i(m, alb, wol, wil, f, pdf);
+}
+template <int K>
+__device__ __forceinline__ void dielectric_eval_pdf_k(const DevMaterial& m, F3 alb, F3 wol, F3 wil, F3* f, float* pdf) {
+    if constexpr (K < 0)
+        dielectric_eval_pdf(m, alb, wol, wil, f, pdf);
+    else
+        dielectric_eval_pdf_i(m, alb, wol, wil, f, pdf);
+}
 
 __device__ __forceinline__ float plastic_exponent(float alpha) {
     float a = s_max(alpha, 0.001f);
@@ -301,19 +341,20 @@ __device__ __forceinline__ float plastic_exponent(float alpha) {
 }
 
 // BSDF::evaluate for all kinds.
-static __device__ __noinline__ F3 bsdf_eval(const DevMaterial& m, const TexView& tv, const Shading& sd, F3 wi) {
-    switch (m.kind) {
+template <int K>
+__device__ __forceinline__ F3 bsdf_eval_i(const DevMaterial& m, const TexView& tv, const Shading& sd, F3 wi) {
+    switch (K >= 0 ? K : m.kind) {
         case PGX_BSDF_DIFFUSE: {
             F3 wl = to_local(sd.frame, wi);
             if (wl.z <= 0.f) return zero3();
             return albedo_of(tv, m, sd) * PGX_INV_PI_F;
         }
         case PGX_BSDF_CONDUCTOR:
-            return conductor_eval(m, albedo_of(tv, m, sd), to_local(sd.frame, wi), to_local(sd.frame, sd.wo));
+            return conductor_eval_k<K>(m, albedo_of(tv, m, sd), to_local(sd.frame, wi), to_local(sd.frame, sd.wo));
         case PGX_BSDF_DIELECTRIC: {
             F3 f;
-            dielectric_eval_pdf(m, albedo_of(tv, m, sd), to_local(sd.frame, sd.wo), to_local(sd.frame, wi), &f,
-                                nullptr);
+            dielectric_eval_pdf_k<K>(m, albedo_of(tv, m, sd), to_local(sd.frame, sd.wo), to_local(sd.frame, wi), &f,
+                                     nullptr);
             return f;
         }
         case PGX_BSDF_ORENNAYAR: {
@@ -351,10 +392,21 @@ static __device__ __noinline__ F3 bsdf_eval(const DevMaterial& m, const TexView&
             return zero3();
     }
 }
+static __device__ __noinline__ F3 bsdf_eval(const DevMaterial& m, const TexView& tv, const Shading& sd, F3 wi) {
+    return bsdf_eval_i<-1>(m, tv, sd, wi);
+}
+template <int K>
+__device__ __forceinline__ F3 bsdf_eval_k(const DevMaterial& m, const TexView& tv, const Shading& sd, F3 wi) {
+    if constexpr (K < 0)
+        return bsdf_eval(m, tv, sd, wi);
+    else
+        return bsdf_eval_i<K>(m, tv, sd, wi);
+}
 
 // BSDF::PDF for all kinds.
-static __device__ __noinline__ float bsdf_pdf(const DevMaterial& m, const TexView& tv, const Shading& sd, F3 wi) {
-    switch (m.kind) {
+template <int K>
+__device__ __forceinline__ float bsdf_pdf_i(const DevMaterial& m, const TexView& tv, const Shading& sd, F3 wi) {
+    switch (K >= 0 ? K : m.kind) {
         case PGX_BSDF_DIFFUSE:
         case PGX_BSDF_ORENNAYAR:
             return cosine_pdf(to_local(sd.frame, wi));
@@ -362,7 +414,7 @@ static __device__ __noinline__ float bsdf_pdf(const DevMaterial& m, const TexVie
             return conductor_pdf(m, to_local(sd.frame, wi), to_local(sd.frame, sd.wo));
         case PGX_BSDF_DIELECTRIC: {
             float p;
-            dielectric_eval_pdf(m, zero3(), to_local(sd.frame, sd.wo), to_local(sd.frame, wi), nullptr, &p);
+            dielectric_eval_pdf_k<K>(m, zero3(), to_local(sd.frame, sd.wo), to_local(sd.frame, wi), nullptr, &p);
             return p;
         }
         case PGX_BSDF_PLASTIC: {
@@ -384,6 +436,16 @@ static __device__ __noinline__ float bsdf_pdf(const DevMaterial& m, const TexVie
     }
     (void)tv;
 }
+static __device__ __noinline__ float bsdf_pdf(const DevMaterial& m, const TexView& tv, const Shading& sd, F3 wi) {
+    return bsdf_pdf_i<-1>(m, tv, sd, wi);
+}
+template <int K>
+__device__ __forceinline__ float bsdf_pdf_k(const DevMaterial& m, const TexView& tv, const Shading& sd, F3 wi) {
+    if constexpr (K < 0)
+        return bsdf_pdf(m, tv, sd, wi);
+    else
+        return bsdf_pdf_i<K>(m, tv, sd, wi);
+}
 
 // Samplers: the path's PCG32 stream, or the reference's TestSampler
 // (Sampling.h:26-48: the first two draws are u and v, every later one 0.5).
@@ -402,17 +464,17 @@ struct FixedSampler {
 };
 
 // BSDF::sample for all kinds; draws from the sampler exactly like the reference.
-template <class Smp>
-static __device__ __noinline__ F3 bsdf_sample_s(const DevMaterial& m, const TexView& tv, const Shading& sd, Smp& rng,
-                                                F3& f, float& pdf) {
-    switch (m.kind) {
+template <int K, class Smp>
+__device__ __forceinline__ F3 bsdf_sample_i(const DevMaterial& m, const TexView& tv, const Shading& sd, Smp& rng, F3& f,
+                                            float& pdf) {
+    switch (K >= 0 ? K : m.kind) {
         case PGX_BSDF_DIFFUSE:
         case PGX_BSDF_ORENNAYAR: {
             float r1 = rng.next();
             float r2 = rng.next();
             F3 wi = to_world(sd.frame, cosine_sample(r1, r2));
-            f = bsdf_eval(m, tv, sd, wi);
-            pdf = bsdf_pdf(m, tv, sd, wi);
+            f = bsdf_eval_k<K>(m, tv, sd, wi);
+            pdf = bsdf_pdf_k<K>(m, tv, sd, wi);
             return wi;
         }
         case PGX_BSDF_MIRROR: {
@@ -436,7 +498,7 @@ static __device__ __noinline__ F3 bsdf_sample_s(const DevMaterial& m, const TexV
             }
             if (m.alpha < PGX_EPSILON) {
                 F3 wr = f3(-wol.x, -wol.y, wol.z);
-                F3 F = fresnel_conductor(wr.z, m.eta, m.k);
+                F3 F = fresnel_conductor_k<K>(wr.z, m.eta, m.k);
                 f = divs(albedo_of(tv, m, sd), fabsf(wr.z)) * F;
                 pdf = 1.f;
                 return to_world(sd.frame, wr);
@@ -446,8 +508,8 @@ static __device__ __noinline__ F3 bsdf_sample_s(const DevMaterial& m, const TexV
             F3 h = ggx_sample_h(m.alpha, r1, r2);
             F3 wil = -wol + (h * 2.f) * dot(h, wol);
             F3 wi = to_world(sd.frame, wil);
-            f = bsdf_eval(m, tv, sd, wi);
-            pdf = bsdf_pdf(m, tv, sd, wi);
+            f = bsdf_eval_k<K>(m, tv, sd, wi);
+            pdf = bsdf_pdf_k<K>(m, tv, sd, wi);
             return wi;
         }
         case PGX_BSDF_GLASS: {
@@ -534,7 +596,7 @@ static __device__ __noinline__ F3 bsdf_sample_s(const DevMaterial& m, const TexV
                 F3 w = f3(-eta * wo_h.x, -eta * wo_h.y, ct * sgn);
                 wi = to_world(sd.frame, to_world(hf, w));
             }
-            dielectric_eval_pdf(m, alb, wol, to_local(sd.frame, wi), &f, &pdf);
+            dielectric_eval_pdf_k<K>(m, alb, wol, to_local(sd.frame, wi), &f, &pdf);
             return wi;
         }
         case PGX_BSDF_PLASTIC: {
@@ -553,8 +615,8 @@ static __device__ __noinline__ F3 bsdf_sample_s(const DevMaterial& m, const TexV
                 wil = cosine_sample(r1, r2);
             }
             F3 wi = to_world(sd.frame, wil);
-            f = bsdf_eval(m, tv, sd, wi);
-            pdf = bsdf_pdf(m, tv, sd, wi);
+            f = bsdf_eval_k<K>(m, tv, sd, wi);
+            pdf = bsdf_pdf_k<K>(m, tv, sd, wi);
             return wi;
         }
         default:
@@ -564,10 +626,26 @@ static __device__ __noinline__ F3 bsdf_sample_s(const DevMaterial& m, const TexV
     }
 }
 
+template <class Smp>
+static __device__ __noinline__ F3 bsdf_sample_s(const DevMaterial& m, const TexView& tv, const Shading& sd, Smp& rng,
+                                                F3& f, float& pdf) {
+    return bsdf_sample_i<-1>(m, tv, sd, rng, f, pdf);
+}
+
 __device__ __forceinline__ F3 bsdf_sample(const DevMaterial& m, const TexView& tv, const Shading& sd, uint64_t& rng,
                                           F3& f, float& pdf) {
     PcgSampler smp{rng};
     return bsdf_sample_s(m, tv, sd, smp, f, pdf);
+}
+template <int K>
+__device__ __forceinline__ F3 bsdf_sample_k(const DevMaterial& m, const TexView& tv, const Shading& sd, uint64_t& rng,
+                                            F3& f, float& pdf) {
+    if constexpr (K < 0) {
+        return bsdf_sample(m, tv, sd, rng, f, pdf);
+    } else {
+        PcgSampler smp{rng};
+        return bsdf_sample_i<K>(m, tv, sd, smp, f, pdf);
+    }
 }
 
 // BSDF::invert (Materials.h:163-171, 287-306, 673-681): the primary sample
@@ -651,7 +729,7 @@ __device__ __forceinline__ F3 env_eval(const DevEnv& e, F3 wi) {
 }
 
 // Distribution2D::PDF (Sampling.h:203-208) via EnvironmentMap::PDF.
-static __device__ __noinline__ float env_pdf(const DevEnv& e, F3 wi) {
+__device__ __forceinline__ float env_pdf_i(const DevEnv& e, F3 wi) {
     float u = atan2f(wi.z, wi.x);
     u = (u < 0.f) ? u + PGX_2PI_F : u;
     u = u * PGX_INV_2PI_F;
@@ -668,9 +746,10 @@ static __device__ __noinline__ float env_pdf(const DevEnv& e, F3 wi) {
     }
     return p / (PGX_2PI2_F * st);
 }
+static __device__ __noinline__ float env_pdf(const DevEnv& e, F3 wi) { return env_pdf_i(e, wi); }
 
 // EnvironmentMap::sample: direction (y-up), emitted colour and solid-angle pdf.
-static __device__ __noinline__ F3 env_sample(const DevEnv& e, uint64_t& rng, F3& col, float& pdf) {
+__device__ __forceinline__ F3 env_sample_i(const DevEnv& e, uint64_t& rng, F3& col, float& pdf) {
     float ru = pgx_rng_next(rng);
     float rv = pgx_rng_next(rng);
     float pv, pu;
@@ -686,4 +765,7 @@ static __device__ __noinline__ F3 env_sample(const DevEnv& e, uint64_t& rng, F3&
     pdf = (st <= 0.f) ? 0.f : sp / (PGX_2PI2_F * st);
     col = (pdf <= 0.f) ? zero3() : env_eval(e, wi);
     return wi;
+}
+static __device__ __noinline__ F3 env_sample(const DevEnv& e, uint64_t& rng, F3& col, float& pdf) {
+    return env_sample_i(e, rng, col, pdf);
 }

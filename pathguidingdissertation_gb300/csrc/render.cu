@@ -372,10 +372,13 @@ __device__ __forceinline__ void shading_data(const SceneView& sv, const float4& 
 // RayTracer::computeDirect (Renderer.h:269-354).  Draws the light and the
 // light sample; returns true with the shadow ray and the contribution it
 // carries when the contribution can be non-zero.
-__device__ __noinline__ bool next_event(const SceneView& sv, const DevMaterial& m, const Shading& sd, uint64_t& rng, float4& so,
-                           float4& sdir, F3& contrib, const GuideView& gv, int qroot, float frac,
-                           const float4* __restrict__ mix) {
-    if (bsdf_pure_specular(m)) return false;
+// K is the material kind when the launch shades one kind (else -1); INL
+// inlines the environment sampler as well.
+template <int K, bool INL>
+__device__ __forceinline__ bool next_event_t(const SceneView& sv, const DevMaterial& m, const Shading& sd, uint64_t& rng,
+                                             float4& so, float4& sdir, F3& contrib, const GuideView& gv, int qroot,
+                                             float frac, const float4* __restrict__ mix) {
+    if (bsdf_pure_specular_k<K>(m)) return false;
     if (sv.nlights == 0) return false;
     float pmf = 1.f / (float)sv.nlights;
     unsigned nl = (unsigned)sv.nlights;
@@ -385,14 +388,14 @@ __device__ __noinline__ bool next_event(const SceneView& sv, const DevMaterial& 
     F3 target, wi, emitted;
     float pdf_light;
     if (sv.has_env_light && idx == 0) {
-        F3 dir = env_sample(sv.env, rng, emitted, pdf_light);
+        F3 dir = INL ? env_sample_i(sv.env, rng, emitted, pdf_light) : env_sample(sv.env, rng, emitted, pdf_light);
         if (pdf_light <= 0.f) return false;
         wi = normalize(dir);
         float cos_t = s_max(dot(wi, sd.sn), 0.f);
         if (cos_t <= 0.f) return false;
-        F3 f = bsdf_eval(m, sv.tex, sd, wi);
+        F3 f = bsdf_eval_k<K>(m, sv.tex, sd, wi);
         float pal = pdf_light * pmf;
-        float pab = bsdf_pdf(m, sv.tex, sd, wi);
+        float pab = bsdf_pdf_k<K>(m, sv.tex, sd, wi);
         if (qroot >= 0) pab = mixture_pdf(gv, qroot, frac, pab, wi);
         if (mix) pab = frac * mlp::packed_pdf(mix, wi) + (1.f - frac) * pab;
         float wd = power_heuristic(pal, pab);
@@ -418,8 +421,8 @@ __device__ __noinline__ bool next_event(const SceneView& sv, const DevMaterial& 
         float cos_t = s_max(dot(wi, sd.sn), 0.f);
         float cos_tp = s_max(dot(-wi, f3(L.gn)), 0.f);
         float G = (cos_t * cos_tp) / den;
-        F3 f = bsdf_eval(m, sv.tex, sd, wi);
-        float pb = bsdf_pdf(m, sv.tex, sd, wi);
+        F3 f = bsdf_eval_k<K>(m, sv.tex, sd, wi);
+        float pb = bsdf_pdf_k<K>(m, sv.tex, sd, wi);
         if (qroot >= 0) pb = mixture_pdf(gv, qroot, frac, pb, wi);
         if (mix) pb = frac * mlp::packed_pdf(mix, wi) + (1.f - frac) * pb;
         float pal = pdf_light * pmf;
@@ -438,6 +441,11 @@ __device__ __noinline__ bool next_event(const SceneView& sv, const DevMaterial& 
     so = make_float4(org.x, org.y, org.z, max_t);
     sdir = make_float4(dv.x, dv.y, dv.z, 0.f);
     return true;
+}
+__device__ __noinline__ bool next_event(const SceneView& sv, const DevMaterial& m, const Shading& sd, uint64_t& rng,
+                                        float4& so, float4& sdir, F3& contrib, const GuideView& gv, int qroot, float frac,
+                                        const float4* __restrict__ mix) {
+    return next_event_t<-1, false>(sv, m, sd, rng, so, sdir, contrib, gv, qroot, frac, mix);
 }
 
 // Light sampling for the guided-Li estimator: the reference computes NEE
@@ -639,10 +647,25 @@ __global__ void __launch_bounds__(kThreads) k_classify(SceneView sv, PathState p
     }
 }
 
-template <int MODE, bool BATCH = false>
-__global__ void __launch_bounds__(kThreads, 8) k_shade(SceneView sv0, PathState ps, FrameParams fp, int depth,
+// Resident blocks per SM the shading launches are compiled for (64
+// registers).  Measured on the interior workload: the inlined diffuse and
+// conductor kernels spill a little at this bound, and are still faster than
+// at 5-7 blocks per SM without spills or at 10-12 with more spills.
+constexpr int kShadeBlocksPerSM = 8;
+
+// CLS >= 0 shades the bin of that surface class with everything the class
+// implies known at compile time (0: misses only; 1: emitters, which end the
+// path; 2, 3, 4: diffuse, conductor, glass BSDFs inlined); CLS < 0 takes the
+// class from `cls` at run time (cls < 0: the whole queue of this depth).
+template <int MODE, bool BATCH = false, int CLS = -1>
+__global__ void __launch_bounds__(kThreads, kShadeBlocksPerSM) k_shade(SceneView sv0, PathState ps, FrameParams fp, int depth,
                                                     GuideView gv, const BatchInfo* binfo = nullptr, int cls = -1) {
-    // the whole queue of this depth (cls < 0) or one class's bin
+    constexpr int KIND = CLS == 2 ? PGX_BSDF_DIFFUSE
+                       : CLS == 3 ? PGX_BSDF_CONDUCTOR
+                       : CLS == 4 ? PGX_BSDF_GLASS
+                                  : -1;
+    constexpr bool INL = CLS >= 0 && CLS <= 4;
+    if (CLS >= 0) cls = CLS;
     const unsigned n = cls < 0 ? ps.qcount[depth] : ps.ccount[depth * kShadeClasses + cls];
     const int* __restrict__ q = cls < 0 ? ps.queue[depth & 1] : ps.cqueue + (size_t)cls * ps.capacity;
     int* __restrict__ qn = ps.queue[(depth + 1) & 1];
@@ -694,7 +717,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_shade(SceneView sv0, PathState 
             F3 r_pos = zero3(), r_nrm = zero3(), r_wi = zero3(), r_w = zero3(), r_e = zero3();
             F3 r_wo = zero3(), r_f = zero3();
             bool r_store = false;
-            if (id >= 0) {
+            if (CLS != 0 && id >= 0) {
                 Shading sd;
                 DevMaterial m;
                 F3 tri_gn;
@@ -703,7 +726,8 @@ __global__ void __launch_bounds__(kThreads, 8) k_shade(SceneView sv0, PathState 
                 r_pos = sd.x;
                 r_nrm = sd.sn;
                 r_wo = sd.wo;
-                if (m.is_light) {
+                const bool is_light = CLS < 0 ? (bool)m.is_light : CLS == 1;
+                if (is_light) {
                     F3 em = f3(m.emission[0], m.emission[1], m.emission[2]);
                     if (MODE == PGX_MODE_GUIDED_LI) {
                         r_e = em;
@@ -723,7 +747,8 @@ __global__ void __launch_bounds__(kThreads, 8) k_shade(SceneView sv0, PathState 
                     }
                 } else {
                     int qroot = -1;
-                    if (MODE == PGX_MODE_GUIDED_QUADTREE && depth < fp.guide_depth && !bsdf_pure_specular(m))
+                    const bool spec = bsdf_pure_specular_k<KIND>(m);
+                    if (MODE == PGX_MODE_GUIDED_QUADTREE && depth < fp.guide_depth && !spec)
                         qroot = guide_region_root(gv, sd.x);
                     const bool use_mix = MODE == PGX_MODE_GUIDED_MLP && depth < fp.guide_depth && mlp_guided_surface(m);
                     const float4* mix = use_mix ? ps.guide + (size_t)p * mlp::kPacked : nullptr;
@@ -731,7 +756,11 @@ __global__ void __launch_bounds__(kThreads, 8) k_shade(SceneView sv0, PathState 
                         next_event_draws(sv, m, rng);
                     } else {
                         F3 c;
-                        want_shadow = next_event(sv, m, sd, rng, so, sdir, c, gv, qroot, fp.guide_fraction, mix);
+                        if constexpr (INL)
+                            want_shadow =
+                                next_event_t<KIND, true>(sv, m, sd, rng, so, sdir, c, gv, qroot, fp.guide_fraction, mix);
+                        else
+                            want_shadow = next_event(sv, m, sd, rng, so, sdir, c, gv, qroot, fp.guide_fraction, mix);
                         sc = T * c;
                     }
                     bool alive = true;
@@ -760,7 +789,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_shade(SceneView sv0, PathState 
                         else if (MODE == PGX_MODE_GUIDED_MLP && use_mix)
                             wi = mlp_guided_sample(mix, fp.guide_fraction, m, sv.tex, sd, rng, f, pdf);
                         else
-                            wi = bsdf_sample(m, sv.tex, sd, rng, f, pdf);
+                            wi = bsdf_sample_k<KIND>(m, sv.tex, sd, rng, f, pdf);
                         float cos_t = fabsf(dot(wi, sd.sn));
                         if (MODE == PGX_MODE_GUIDED_LI) {
                             if (pdf <= 0.f || cos_t <= 0.f) {
@@ -768,7 +797,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_shade(SceneView sv0, PathState 
                             } else {
                                 r_wi = wi;
                                 r_w = divs(f * cos_t, pdf * rrp_rec);
-                                r_store = !bsdf_pure_specular(m);
+                                r_store = !spec;
                             }
                         } else {
                             if (pdf <= 0.f || cos_t <= 0.f) {
@@ -784,7 +813,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_shade(SceneView sv0, PathState 
                         }
                         if (alive) {
                             if (rec_on) {
-                                r_store = !bsdf_pure_specular(m);
+                                r_store = !spec;
                                 r_wi = wi;
                                 r_w = T;  // throughput after this vertex
                             }
@@ -793,12 +822,12 @@ __global__ void __launch_bounds__(kThreads, 8) k_shade(SceneView sv0, PathState 
                             ps.o[p] = make_float4(org.x, org.y, org.z, 0.f);
                             ps.d[p] = make_float4(wi.x, wi.y, wi.z, 0.f);
                             ps.T[p] = make_float4(T.x, T.y, T.z, pdf);
-                            ps.flags[p] = bsdf_pure_specular(m) ? 1 : 0;
+                            ps.flags[p] = spec ? 1 : 0;
                             cont = true;
                         }
                     }
                 }
-            } else {
+            } else if (CLS <= 0) {
                 // Miss: background (Renderer.h:501-527, 596-612).
                 F3 bg = env_eval(sv.env, dir);
                 if (MODE == PGX_MODE_GUIDED_LI) {
@@ -807,7 +836,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_shade(SceneView sv0, PathState 
                     add = T * bg;
                 } else if (!(lum(bg) < 1e-8f)) {
                     float pmf = 1.f / (float)sv.nlights;
-                    float pdf_light = env_pdf(sv.env, dir);
+                    float pdf_light = INL ? env_pdf_i(sv.env, dir) : env_pdf(sv.env, dir);
                     if (pmf > 0.f && pdf_light > 0.f) {
                         float pal = pmf * pdf_light;
                         float wind = power_heuristic(prev_pdf, pal);
@@ -1452,6 +1481,20 @@ __global__ void __launch_bounds__(kThreads) k_finalize_batch(PathState ps, Batch
     }
 }
 
+// Plain path tracing of one surface class's bin, with the class compiled in.
+template <bool BATCH>
+void launch_shade_class(int c, unsigned grid, cudaStream_t s, const SceneView& sv, const PathState& ps,
+                        const FrameParams& fp, int depth, const GuideView& gv, const BatchInfo* info) {
+    switch (c) {
+        case 0: k_shade<PGX_MODE_PLAIN, BATCH, 0><<<grid, kThreads, 0, s>>>(sv, ps, fp, depth, gv, info); break;
+        case 1: k_shade<PGX_MODE_PLAIN, BATCH, 1><<<grid, kThreads, 0, s>>>(sv, ps, fp, depth, gv, info); break;
+        case 2: k_shade<PGX_MODE_PLAIN, BATCH, 2><<<grid, kThreads, 0, s>>>(sv, ps, fp, depth, gv, info); break;
+        case 3: k_shade<PGX_MODE_PLAIN, BATCH, 3><<<grid, kThreads, 0, s>>>(sv, ps, fp, depth, gv, info); break;
+        case 4: k_shade<PGX_MODE_PLAIN, BATCH, 4><<<grid, kThreads, 0, s>>>(sv, ps, fp, depth, gv, info); break;
+        default: k_shade<PGX_MODE_PLAIN, BATCH, 5><<<grid, kThreads, 0, s>>>(sv, ps, fp, depth, gv, info); break;
+    }
+}
+
 inline unsigned grid_for(int64_t n) {
     int64_t b = (n + kThreads - 1) / kThreads;
     return (unsigned)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 16));
@@ -1635,7 +1678,7 @@ int enqueue_frame(pgx_ctx* ctx, RenderState* rs, const FrameParams& fp, cudaStre
                     k_shade<PGX_MODE_GUIDED_MLP><<<g, kThreads, 0, s>>>(sv, ps, fp, depth, gv, nullptr, c);
                     break;
                 default:
-                    k_shade<PGX_MODE_PLAIN><<<g, kThreads, 0, s>>>(sv, ps, fp, depth, gv, nullptr, c);
+                    launch_shade_class<false>(c, g, s, sv, ps, fp, depth, gv, nullptr);
                     break;
             }
         }
@@ -2161,7 +2204,7 @@ int batch_enqueue(pgx_batch* b, int64_t total, int depth, const pgx_batch_tuning
             k_extend<false, true><<<tg, kThreads, 0, s>>>(sv, ps, d, info);
             k_classify<<<grid_for((bw.count + kClassifyItems - 1) / kClassifyItems), kThreads, 0, s>>>(sv, ps, d);
             for (int c = 0; c < kShadeClasses; c++)
-                k_shade<PGX_MODE_PLAIN, true><<<sg, kThreads, 0, s>>>(sv, ps, fp, d, gv, info, c);
+                launch_shade_class<true>(c, sg, s, sv, ps, fp, d, gv, info);
             k_shadow<false, true><<<tg, kThreads, 0, s>>>(sv, ps, d, info);
         }
         k_finalize_batch<<<sg, kThreads, 0, s>>>(ps, bw);
