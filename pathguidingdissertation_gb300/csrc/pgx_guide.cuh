@@ -232,10 +232,12 @@ __device__ __forceinline__ float mixture_pdf(const GuideView& g, int qroot, floa
 }
 
 // Continuation direction for the guided estimator: pdf is the mixture pdf.
-static __device__ F3 guided_sample(const GuideView& g, float frac, const DevMaterial& m, const TexView& tv,
-                            const Shading& sd, uint64_t& rng, F3& f, float& pdf, int qroot) {
-    if (qroot < 0 || bsdf_pure_specular(m) || m.kind == PGX_BSDF_GLASS) {
-        return bsdf_sample(m, tv, sd, rng, f, pdf);
+// K: the material kind when the caller shades a single kind, else -1.
+template <int K = -1>
+__device__ __forceinline__ F3 guided_sample(const GuideView& g, float frac, const DevMaterial& m, const TexView& tv,
+                                            const Shading& sd, uint64_t& rng, F3& f, float& pdf, int qroot) {
+    if (qroot < 0 || bsdf_pure_specular_k<K>(m) || (K >= 0 ? K : m.kind) == PGX_BSDF_GLASS) {
+        return bsdf_sample_k<K>(m, tv, sd, rng, f, pdf);
     }
     float sel = pgx_rng_next(rng);
     F3 wi;
@@ -250,12 +252,12 @@ static __device__ F3 guided_sample(const GuideView& g, float frac, const DevMate
             quad_sample(g.qnodes, qroot, r1, r2, u, v);
         }
         wi = uv_to_dir(u, v);
-        f = bsdf_eval(m, tv, sd, wi);
+        f = bsdf_eval_k<K>(m, tv, sd, wi);
     } else {
         float bp;
-        wi = bsdf_sample(m, tv, sd, rng, f, bp);
+        wi = bsdf_sample_k<K>(m, tv, sd, rng, f, bp);
     }
-    float bp = bsdf_pdf(m, tv, sd, wi);
+    float bp = bsdf_pdf_k<K>(m, tv, sd, wi);
     pdf = mixture_pdf(g, qroot, frac, bp, wi);
     return wi;
 }

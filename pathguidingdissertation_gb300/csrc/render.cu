@@ -470,29 +470,37 @@ __device__ void next_event_draws(const SceneView& sv, const DevMaterial& m, uint
 // Continuation direction of the learned-guide estimator: one-sample MIS
 // between the network's vMF mixture (probability frac; the selection number
 // is reused as the lobe choice) and the BSDF; pdf is the mixture pdf.
-static __device__ __noinline__ F3 mlp_guided_sample(const float4* __restrict__ mix, float frac, const DevMaterial& m,
-                                                    const TexView& tv, const Shading& sd, uint64_t& rng, F3& f,
-                                                    float& pdf) {
+// K: the material kind when the caller shades a single kind, else -1.
+template <int K>
+__device__ __forceinline__ F3 mlp_guided_sample_t(const float4* __restrict__ mix, float frac, const DevMaterial& m,
+                                                  const TexView& tv, const Shading& sd, uint64_t& rng, F3& f,
+                                                  float& pdf) {
     float sel = pgx_rng_next(rng);
     F3 wi;
     if (sel < frac) {
         float u1 = pgx_rng_next(rng), u2 = pgx_rng_next(rng);
         wi = mlp::packed_sample(mix, sel / frac, u1, u2);
-        f = bsdf_eval(m, tv, sd, wi);
+        f = bsdf_eval_k<K>(m, tv, sd, wi);
     } else {
         float bp;
-        wi = bsdf_sample(m, tv, sd, rng, f, bp);
+        wi = bsdf_sample_k<K>(m, tv, sd, rng, f, bp);
         // non-specular: bsdf_sample's pdf is bsdf_pdf(wi)
         pdf = frac * mlp::packed_pdf(mix, wi) + (1.f - frac) * bp;
         return wi;
     }
-    float bp = bsdf_pdf(m, tv, sd, wi);
+    float bp = bsdf_pdf_k<K>(m, tv, sd, wi);
     pdf = frac * mlp::packed_pdf(mix, wi) + (1.f - frac) * bp;
     return wi;
 }
+static __device__ __noinline__ F3 mlp_guided_sample(const float4* __restrict__ mix, float frac, const DevMaterial& m,
+                                                    const TexView& tv, const Shading& sd, uint64_t& rng, F3& f,
+                                                    float& pdf) {
+    return mlp_guided_sample_t<-1>(mix, frac, m, tv, sd, rng, f, pdf);
+}
 
+template <int K = -1>
 __device__ __forceinline__ bool mlp_guided_surface(const DevMaterial& m) {
-    return !m.is_light && !bsdf_pure_specular(m) && m.kind != PGX_BSDF_GLASS;
+    return !m.is_light && !bsdf_pure_specular_k<K>(m) && (K >= 0 ? K : m.kind) != PGX_BSDF_GLASS;
 }
 
 // Learned guide, one depth: the network evaluated on the tensor cores for
@@ -750,7 +758,8 @@ __global__ void __launch_bounds__(kThreads, kShadeBlocksPerSM) k_shade(SceneView
                     const bool spec = bsdf_pure_specular_k<KIND>(m);
                     if (MODE == PGX_MODE_GUIDED_QUADTREE && depth < fp.guide_depth && !spec)
                         qroot = guide_region_root(gv, sd.x);
-                    const bool use_mix = MODE == PGX_MODE_GUIDED_MLP && depth < fp.guide_depth && mlp_guided_surface(m);
+                    const bool use_mix =
+                        MODE == PGX_MODE_GUIDED_MLP && depth < fp.guide_depth && mlp_guided_surface<KIND>(m);
                     const float4* mix = use_mix ? ps.guide + (size_t)p * mlp::kPacked : nullptr;
                     if (MODE == PGX_MODE_GUIDED_LI) {
                         next_event_draws(sv, m, rng);
@@ -785,7 +794,9 @@ __global__ void __launch_bounds__(kThreads, kShadeBlocksPerSM) k_shade(SceneView
                         float pdf;
                         F3 wi;
                         if (MODE == PGX_MODE_GUIDED_QUADTREE)
-                            wi = guided_sample(gv, fp.guide_fraction, m, sv.tex, sd, rng, f, pdf, qroot);
+                            wi = guided_sample<KIND>(gv, fp.guide_fraction, m, sv.tex, sd, rng, f, pdf, qroot);
+                        else if (MODE == PGX_MODE_GUIDED_MLP && use_mix && INL)
+                            wi = mlp_guided_sample_t<KIND>(mix, fp.guide_fraction, m, sv.tex, sd, rng, f, pdf);
                         else if (MODE == PGX_MODE_GUIDED_MLP && use_mix)
                             wi = mlp_guided_sample(mix, fp.guide_fraction, m, sv.tex, sd, rng, f, pdf);
                         else
@@ -1481,17 +1492,17 @@ __global__ void __launch_bounds__(kThreads) k_finalize_batch(PathState ps, Batch
     }
 }
 
-// Plain path tracing of one surface class's bin, with the class compiled in.
-template <bool BATCH>
+// One surface class's bin shaded by estimator MODE, with the class compiled in.
+template <int MODE, bool BATCH>
 void launch_shade_class(int c, unsigned grid, cudaStream_t s, const SceneView& sv, const PathState& ps,
                         const FrameParams& fp, int depth, const GuideView& gv, const BatchInfo* info) {
     switch (c) {
-        case 0: k_shade<PGX_MODE_PLAIN, BATCH, 0><<<grid, kThreads, 0, s>>>(sv, ps, fp, depth, gv, info); break;
-        case 1: k_shade<PGX_MODE_PLAIN, BATCH, 1><<<grid, kThreads, 0, s>>>(sv, ps, fp, depth, gv, info); break;
-        case 2: k_shade<PGX_MODE_PLAIN, BATCH, 2><<<grid, kThreads, 0, s>>>(sv, ps, fp, depth, gv, info); break;
-        case 3: k_shade<PGX_MODE_PLAIN, BATCH, 3><<<grid, kThreads, 0, s>>>(sv, ps, fp, depth, gv, info); break;
-        case 4: k_shade<PGX_MODE_PLAIN, BATCH, 4><<<grid, kThreads, 0, s>>>(sv, ps, fp, depth, gv, info); break;
-        default: k_shade<PGX_MODE_PLAIN, BATCH, 5><<<grid, kThreads, 0, s>>>(sv, ps, fp, depth, gv, info); break;
+        case 0: k_shade<MODE, BATCH, 0><<<grid, kThreads, 0, s>>>(sv, ps, fp, depth, gv, info); break;
+        case 1: k_shade<MODE, BATCH, 1><<<grid, kThreads, 0, s>>>(sv, ps, fp, depth, gv, info); break;
+        case 2: k_shade<MODE, BATCH, 2><<<grid, kThreads, 0, s>>>(sv, ps, fp, depth, gv, info); break;
+        case 3: k_shade<MODE, BATCH, 3><<<grid, kThreads, 0, s>>>(sv, ps, fp, depth, gv, info); break;
+        case 4: k_shade<MODE, BATCH, 4><<<grid, kThreads, 0, s>>>(sv, ps, fp, depth, gv, info); break;
+        default: k_shade<MODE, BATCH, 5><<<grid, kThreads, 0, s>>>(sv, ps, fp, depth, gv, info); break;
     }
 }
 
@@ -1669,16 +1680,16 @@ int enqueue_frame(pgx_ctx* ctx, RenderState* rs, const FrameParams& fp, cudaStre
         for (int c = 0; c < kShadeClasses; c++) {
             switch (fp.mode) {
                 case PGX_MODE_GUIDED_LI:
-                    k_shade<PGX_MODE_GUIDED_LI><<<g, kThreads, 0, s>>>(sv, ps, fp, depth, gv, nullptr, c);
+                    launch_shade_class<PGX_MODE_GUIDED_LI, false>(c, g, s, sv, ps, fp, depth, gv, nullptr);
                     break;
                 case PGX_MODE_GUIDED_QUADTREE:
-                    k_shade<PGX_MODE_GUIDED_QUADTREE><<<g, kThreads, 0, s>>>(sv, ps, fp, depth, gv, nullptr, c);
+                    launch_shade_class<PGX_MODE_GUIDED_QUADTREE, false>(c, g, s, sv, ps, fp, depth, gv, nullptr);
                     break;
                 case PGX_MODE_GUIDED_MLP:
-                    k_shade<PGX_MODE_GUIDED_MLP><<<g, kThreads, 0, s>>>(sv, ps, fp, depth, gv, nullptr, c);
+                    launch_shade_class<PGX_MODE_GUIDED_MLP, false>(c, g, s, sv, ps, fp, depth, gv, nullptr);
                     break;
                 default:
-                    launch_shade_class<false>(c, g, s, sv, ps, fp, depth, gv, nullptr);
+                    launch_shade_class<PGX_MODE_PLAIN, false>(c, g, s, sv, ps, fp, depth, gv, nullptr);
                     break;
             }
         }
@@ -2204,7 +2215,7 @@ int batch_enqueue(pgx_batch* b, int64_t total, int depth, const pgx_batch_tuning
             k_extend<false, true><<<tg, kThreads, 0, s>>>(sv, ps, d, info);
             k_classify<<<grid_for((bw.count + kClassifyItems - 1) / kClassifyItems), kThreads, 0, s>>>(sv, ps, d);
             for (int c = 0; c < kShadeClasses; c++)
-                launch_shade_class<true>(c, sg, s, sv, ps, fp, d, gv, info);
+                launch_shade_class<PGX_MODE_PLAIN, true>(c, sg, s, sv, ps, fp, d, gv, info);
             k_shadow<false, true><<<tg, kThreads, 0, s>>>(sv, ps, d, info);
         }
         k_finalize_batch<<<sg, kThreads, 0, s>>>(ps, bw);
