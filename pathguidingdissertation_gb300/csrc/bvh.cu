@@ -646,6 +646,7 @@ __global__ void k_reorder(const pgx_triangle* __restrict__ tris, const int* __re
     o.v0 = make_float4(v0.x, v0.y, v0.z, __int_as_float(id));
     o.e0 = make_float4(e0.x, e0.y, e0.z, 0.f);
     o.e1 = make_float4(e1.x, e1.y, e1.z, 0.f);
+    o.pad = make_float4(0.f, 0.f, 0.f, 0.f);
     out[p] = o;
 }
 
