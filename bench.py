@@ -212,17 +212,23 @@ def run_pgx(args) -> dict:
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     spp = args.spp_per_step
     for i in range(args.warmup):
-        ctx.render(spp, mode=mode, seed=seed, max_depth=depth, profile=True)
+        ctx.render(spp, mode=mode, seed=seed, max_depth=depth, timing=True)
+    # Node/triangle fetch counts of one step of the same workload (the counting
+    # traversal kernels; untimed).  The timed steps run the uncounted kernels.
+    ctx.render(spp, mode=mode, seed=seed, max_depth=depth, profile=True)
+    cst = ctx.render_stats()
+    visits_per_ray = cst.extend_interior_visits / max(cst.extension_rays, 1)
+    tris_per_ray = cst.extend_tri_tests / max(cst.extension_rays, 1)
     torch.cuda.synchronize()
     ranks.barrier()
     rays = paths = ext_rays = 0
     ms = ms_ext = ms_shade = 0.0
-    ext_visits = ext_tris = ext_launches = launches = 0
+    ext_launches = launches = 0
     with ClockSampler() as clk:
         for k in range(args.steps):
             flush.zero_()
             torch.cuda.synchronize()
-            ctx.render(spp, mode=mode, seed=seed, max_depth=depth, profile=True)
+            ctx.render(spp, mode=mode, seed=seed, max_depth=depth, timing=True)
             st = ctx.render_stats()
             rays += st.extension_rays + st.shadow_rays
             paths += st.paths
@@ -230,13 +236,13 @@ def run_pgx(args) -> dict:
             ms_ext += st.ms_extend
             ms_shade += st.ms_shade
             ext_rays += st.extension_rays
-            ext_visits += st.extend_interior_visits
-            ext_tris += st.extend_tri_tests
             ext_launches += st.extend_launches
             launches += st.kernel_launches
         torch.cuda.synchronize()
         ranks.barrier()
     clocks = clk.summary()
+    ext_visits = visits_per_ray * ext_rays
+    ext_tris = tris_per_ray * ext_rays
     # whole job: every replica's rays over the slowest replica's device time
     ms_max = ranks.reduce(ms, "max")
     rays_all = ranks.reduce(rays, "sum")
@@ -280,6 +286,9 @@ def run_pgx(args) -> dict:
         "traffic": traffic,
         "traffic_note": traffic_note,
         "alg_bytes_per_launch": alg_bytes / max(ext_launches, 1),
+        "nodes_per_ray": visits_per_ray,
+        "tris_per_ray": tris_per_ray,
+        "counts_note": "per extension ray, from one untimed step run with the counting traversal kernels",
         "avg_launch_ms": ms_ext / max(ext_launches, 1),
         "extend_share_of_step": ms_ext / ms if ms else None,
     }

@@ -184,12 +184,14 @@ typedef struct pgx_render_config {
                             * the last N frames of the call with the full
                             * NEE+MIS incident radiance.  The cache is rebuilt
                             * from the records when the call ends. */
-    int32_t flags;         /* PGX_RENDER_PROFILE: per-stage events/counters */
+    int32_t flags;         /* PGX_RENDER_* below                            */
     int32_t guide_depth;   /* guided modes: guide the first guide_depth
                             * bounces only (0: every bounce)               */
 } pgx_render_config;
 
 /* pgx_render_config.flags */
+/* Per-stage CUDA-event times and device counters of the node and triangle
+ * fetches (the traversal kernels then run a counting variant). */
 #define PGX_RENDER_PROFILE 1
 /* Splat with the Mitchell-Netravali filter, B = C = 1/3, radius 2
  * (MitchellNetravaliFilter, Imaging.h:153-176) instead of the box filter
@@ -198,9 +200,13 @@ typedef struct pgx_render_config {
 /* PGX_MODE_GUIDED_MLP: after every frame, one Adam step of the learned guide
  * on the radiance samples that frame's paths produced (pgx_mlp_configure). */
 #define PGX_RENDER_TRAIN_GUIDE 4
+/* Per-stage CUDA-event times only: the kernels are the ones a render without
+ * flags runs. */
+#define PGX_RENDER_TIMING 8
 
-/* Statistics of the last pgx_render call.  The per-stage times and the
- * node/triangle fetch counts are filled only with PGX_RENDER_PROFILE. */
+/* Statistics of the last pgx_render call.  The per-stage times are filled
+ * with PGX_RENDER_PROFILE or PGX_RENDER_TIMING, the node/triangle fetch counts
+ * only with PGX_RENDER_PROFILE. */
 typedef struct pgx_render_stats {
     int64_t paths;
     int64_t extension_rays;

@@ -72,6 +72,7 @@ class BvhStats(C.Structure):
 
 
 RENDER_PROFILE = 1
+RENDER_TIMING = 8
 RENDER_FILTER_MITCHELL = 2
 
 

@@ -138,7 +138,7 @@ struct FrameParams {
     int collect_lo;  // path vertices of samples [collect_lo, collect_hi) are recorded
     int collect_hi;
     float guide_fraction;
-    int profile;     // count node/triangle fetches
+    int profile;     // 1: stage events; 2: stage events and node/triangle fetch counts
     int mitchell;    // Mitchell-Netravali splat instead of the box filter
     int train;       // learned guide: emit radiance samples of recorded vertices
                      // (1: indirect light only, 2: full incident radiance)
@@ -765,12 +765,15 @@ __global__ void __launch_bounds__(kThreads, kShadeBlocksPerSM) k_shade(SceneView
                         next_event_draws(sv, m, rng);
                     } else {
                         F3 c;
-                        if constexpr (INL)
+                        if constexpr (INL) {
                             want_shadow =
                                 next_event_t<KIND, true>(sv, m, sd, rng, so, sdir, c, gv, qroot, fp.guide_fraction, mix);
-                        else
+                            // queued here so the shadow ray is not held through sampling
+                            push_shadow(ps, depth, p, so, sdir, T * c, want_shadow);
+                        } else {
                             want_shadow = next_event(sv, m, sd, rng, so, sdir, c, gv, qroot, fp.guide_fraction, mix);
-                        sc = T * c;
+                            sc = T * c;
+                        }
                     }
                     bool alive = true;
                     float rrp_rec = 1.f;
@@ -790,6 +793,10 @@ __global__ void __launch_bounds__(kThreads, kShadeBlocksPerSM) k_shade(SceneView
                     }
                     if (alive && depth == fp.max_depth) alive = false;
                     if (alive) {
+                        // The diffuse light sampling above reads only the frame's
+                        // normal: rebuilding the frame (same input, same bits) here
+                        // keeps its tangents out of registers during it.
+                        if constexpr (KIND == PGX_BSDF_DIFFUSE) sd.frame = frame_from(sd.sn);
                         F3 f;
                         float pdf;
                         F3 wi;
@@ -894,7 +901,7 @@ __global__ void __launch_bounds__(kThreads, kShadeBlocksPerSM) k_shade(SceneView
             }
             ps.rng[p] = rng;
         }
-        if (MODE != PGX_MODE_GUIDED_LI) push_shadow(ps, depth, p, so, sdir, sc, active && want_shadow);
+        if (MODE != PGX_MODE_GUIDED_LI && !INL) push_shadow(ps, depth, p, so, sdir, sc, active && want_shadow);
         unsigned slot = warp_aggregated_add(&ps.qcount[depth + 1], active && cont);
         if (active && cont) qn[slot] = p;
     }
@@ -1655,7 +1662,8 @@ int enqueue_frame(pgx_ctx* ctx, RenderState* rs, const FrameParams& fp, cudaStre
     MlpView mv = fp.mode == PGX_MODE_GUIDED_MLP ? mlp_view(ctx) : MlpView{};
     const int64_t n = (int64_t)ctx->width * ctx->height * fp.batch;
     const unsigned g = grid_for(n);
-    const bool prof = fp.profile != 0;
+    const bool prof = fp.profile != 0;  // stage events
+    const bool cnt = fp.profile > 1;    // counting traversal kernels
     int launches = 0;
     cudaMemsetAsync(ps.qcount, 0, sizeof(unsigned) * 4 * (kMaxDepthCap + 2), s);
     cudaMemsetAsync(ps.ccount, 0, sizeof(unsigned) * kShadeClasses * (kMaxDepthCap + 2), s);
@@ -1664,7 +1672,7 @@ int enqueue_frame(pgx_ctx* ctx, RenderState* rs, const FrameParams& fp, cudaStre
     for (int depth = 0; depth <= fp.max_depth; depth++) {
         if (prof) cudaEventRecord(rs->prof[4 * depth + 0], s);
         const unsigned pg = persistent_grid(n);
-        if (prof)
+        if (cnt)
             k_extend<true><<<pg, kThreads, 0, s>>>(sv, ps, depth);
         else
             k_extend<false><<<pg, kThreads, 0, s>>>(sv, ps, depth);
@@ -1696,7 +1704,7 @@ int enqueue_frame(pgx_ctx* ctx, RenderState* rs, const FrameParams& fp, cudaStre
         launches += 2 + kShadeClasses;
         if (prof) cudaEventRecord(rs->prof[4 * depth + 2], s);
         if (fp.mode != PGX_MODE_GUIDED_LI) {
-            if (prof)
+            if (cnt)
                 k_shadow<true><<<pg, kThreads, 0, s>>>(sv, ps, depth);
             else
                 k_shadow<false><<<pg, kThreads, 0, s>>>(sv, ps, depth);
@@ -1822,7 +1830,8 @@ extern "C" int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t fr
     PathState ps = path_view(rs);
     PGX_CUDA_TRY(ctx, cudaMemsetAsync(ps.stats, 0, sizeof(unsigned long long) * kStats + sizeof(unsigned) * 4, s));
     int* mlp_status = reinterpret_cast<int*>(ps.nvertices + 2);
-    const bool prof = (cfg->flags & PGX_RENDER_PROFILE) != 0;
+    const bool count = (cfg->flags & PGX_RENDER_PROFILE) != 0;
+    const bool prof = count || (cfg->flags & PGX_RENDER_TIMING) != 0;
     StageTimes times;
     int64_t launches = 0, batches = 0;
     PGX_CUDA_TRY(ctx, cudaEventRecord(rs->ev0, s));
@@ -1837,7 +1846,7 @@ extern "C" int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t fr
         fp.collect_lo = collect_lo;
         fp.collect_hi = collect_hi;
         fp.guide_fraction = cfg->guide_fraction;
-        fp.profile = prof ? 1 : 0;
+        fp.profile = count ? 2 : (prof ? 1 : 0);
         fp.mitchell = (cfg->flags & PGX_RENDER_FILTER_MITCHELL) ? 1 : 0;
         fp.train = train ? (mlp_train_direct(ctx) ? 2 : 1) : 0;
         fp.guide_depth = cfg->guide_depth > 0 ? cfg->guide_depth : kMaxDepthCap + 1;
