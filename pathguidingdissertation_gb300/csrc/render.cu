@@ -504,8 +504,9 @@ __device__ __forceinline__ bool mlp_guided_surface(const DevMaterial& m) {
 }
 
 // Learned guide, one depth: the network evaluated on the tensor cores for
-// every queued path, 128 paths per tile; paths whose hit is a guided
-// surface get their packed vMF mixture in ps.guide.  Each CTA runs
+// the paths of the depth's diffuse, conductor and other bins (classified
+// first), 128 paths per tile; paths whose hit is a guided surface get their
+// packed vMF mixture in ps.guide.  Each CTA runs
 // kInferGroups groups of 128 threads on independent tiles (they share the
 // weights in shared memory), so one group's gathers and epilogues overlap
 // another's MMAs.
@@ -546,8 +547,11 @@ __global__ void __launch_bounds__(128 * kInferGroups, 2) k_guide_infer(SceneView
     tc::fence_after_sync();
     s.tmem = tslot + (uint32_t)(g * 64);
     uint32_t phase = 0;
-    const unsigned n = ps.qcount[depth];
-    const int* __restrict__ q = ps.queue[depth & 1];
+    // Only the bins of the classes that can be guided (diffuse, conductor,
+    // other; k_classify ran first) are evaluated, back to back.
+    const unsigned* cc = ps.ccount + depth * kShadeClasses;
+    const unsigned n2 = cc[2], n3 = cc[3], n5 = cc[5];
+    const unsigned n = n2 + n3 + n5;
     const unsigned groups = gridDim.x * kInferGroups;
     for (unsigned tile = blockIdx.x * kInferGroups + g; tile * (unsigned)mlp::kRows < n; tile += groups) {
         const unsigned i = tile * mlp::kRows + s.tg;
@@ -555,7 +559,9 @@ __global__ void __launch_bounds__(128 * kInferGroups, 2) k_guide_infer(SceneView
         bool need = false;
         F3 x = zero3(), nn = zero3(), wo = zero3();
         if (i < n) {
-            p = q[i];
+            const size_t at = i < n2 ? 2 * ps.capacity + i
+                            : (i < n2 + n3 ? 3 * ps.capacity + (i - n2) : 5 * ps.capacity + (i - n2 - n3));
+            p = ps.cqueue[at];
             float4 h = ps.hit[p];
             if (__float_as_int(h.x) >= 0) {
                 Shading sd;
@@ -1677,6 +1683,7 @@ int enqueue_frame(pgx_ctx* ctx, RenderState* rs, const FrameParams& fp, cudaStre
         else
             k_extend<false><<<pg, kThreads, 0, s>>>(sv, ps, depth);
         if (prof) cudaEventRecord(rs->prof[4 * depth + 1], s);
+        k_classify<<<grid_for((n + kClassifyItems - 1) / kClassifyItems), kThreads, 0, s>>>(sv, ps, depth);
         if (fp.mode == PGX_MODE_GUIDED_MLP && depth < fp.guide_depth) {
             const int64_t tiles = (n + mlp::kRows - 1) / mlp::kRows;
             const int64_t ctas = (tiles + kInferGroups - 1) / kInferGroups;
@@ -1684,7 +1691,6 @@ int enqueue_frame(pgx_ctx* ctx, RenderState* rs, const FrameParams& fp, cudaStre
             k_guide_infer<<<ig, 128 * kInferGroups, kInferSmem, s>>>(sv, ps, depth, mv, mlp_status);
             launches++;
         }
-        k_classify<<<grid_for((n + kClassifyItems - 1) / kClassifyItems), kThreads, 0, s>>>(sv, ps, depth);
         for (int c = 0; c < kShadeClasses; c++) {
             switch (fp.mode) {
                 case PGX_MODE_GUIDED_LI:

@@ -111,7 +111,28 @@ def test_render_api_semantics(ctx):
     assert st.paths == 32 * 32 * 3 and st.extension_rays >= st.paths
 
 
-GOLDEN = __import__("pathlib").Path(__file__).resolve().parent / "golden"
+def test_render_stats_flags(ctx):
+    """PGX_RENDER_PROFILE: stage times and traversal counts; PGX_RENDER_TIMING:
+    stage times only; no flag: neither.  The image does not depend on them."""
+    desc = scenes.cornell_box(seed=2, width=48, height=48)
+    ctx.upload(desc)
+    ctx.bvh_build()
+    films = []
+    for kw in ({}, {"timing": True}, {"profile": True}):
+        ctx.clear()
+        ctx.render(2, seed=5, **kw)
+        st = ctx.render_stats()
+        films.append(ctx.film()[0])
+        timed = bool(kw)
+        assert (st.ms_extend > 0) == timed and (st.ms_shade > 0) == timed
+        assert (st.extend_interior_visits > 0) == ("profile" in kw)
+        assert (st.extend_tri_tests > 0) == ("profile" in kw)
+        assert st.ms_total > 0 and st.extension_rays >= st.paths
+    for f in films[1:]:
+        assert np.allclose(f, films[0], rtol=1e-5, atol=1e-6)
+
+
+GOLDEN =__import__("pathlib").Path(__file__).resolve().parent / "golden"
 
 
 def _fixture_desc(g):
