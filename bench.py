@@ -145,16 +145,17 @@ def measured_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def profile_traffic(kernel: str) -> tuple[float | None, str | None]:
-    """Per-launch DRAM bytes of `kernel` from the committed ncu summary."""
+def profile_traffic(kernel: str, units_per_launch: float) -> tuple[float | None, str | None]:
+    """Per-launch DRAM bytes of `kernel`: the committed ncu capture's bytes per
+    unit (extension ray) times the units of an average launch of this run."""
     p = ROOT / "profiles" / "traffic.json"
     if not p.exists():
         return None, None
     d = json.loads(p.read_text())
     e = d.get(kernel)
-    if not e:
+    if not e or "bytes_per_unit" not in e:
         return None, None
-    return float(e["bytes_per_launch"]), e.get("note")
+    return float(e["bytes_per_unit"]) * units_per_launch, e.get("note")
 
 
 def cpu_baseline_reference(desc, frames_budget_s: float = 12.0) -> dict | None:
@@ -274,7 +275,7 @@ def run_pgx(args) -> dict:
     peaks = measured_peaks()
     alg_bytes = ext_visits * 64 + ext_tris * 48
     achieved = alg_bytes / (ms_ext * 1e-3) / 1e9 if ms_ext > 0 else None
-    traffic, traffic_note = profile_traffic("k_extend")
+    traffic, traffic_note = profile_traffic("k_extend", ext_rays / max(ext_launches, 1))
     roofline = {
         "kernel": "k_extend (closest-hit traversal)",
         "bound": "hbm",
@@ -831,7 +832,7 @@ def main() -> None:
     ap.add_argument("--mode", choices=["plain", "guided_quadtree", "guided_mlp"], default="plain")
     ap.add_argument("--workload", choices=["interior", "cornell"], default="interior")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--spp-per-step", type=int, default=4,
+    ap.add_argument("--spp-per-step", type=int, default=32,
                     help="samples per pixel of one step: one pgx_render call, one wavefront")
     ap.add_argument("--study", choices=["relmse", "traversal", "adjoint", "batch"], default=None,
                     help="instead of the throughput line, run the equal-time relMSE study")

@@ -1821,9 +1821,13 @@ extern "C" int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t fr
     }
     const bool recording = collect_hi > collect_lo && !train;
     const int rec_depth = (guided_li || recording || train) ? cfg->max_depth + 1 : 0;
-    // Samples per wavefront: enough paths to fill the GPU, bounded memory
-    // (per-depth vertex records cost 80 bytes per path and depth).
-    const int64_t target_paths = rec_depth ? (int64_t)(1 << 21) : (int64_t)(1 << 22);
+    // Samples per wavefront: as many as fit in 2^25 paths (~190 bytes of state
+    // each, 6.4 GB): the depths where the queues have shrunk cost about the
+    // same per wave whatever its size, so large waves amortise them (measured
+    // on the 1280x720 interior: 1,726 Mrays/s at 4 spp per wave, 1,903 at 8,
+    // 1,998 at 16, 2,041 at 32).  Recording is bounded at 2^21 paths (per-depth
+    // vertex records cost 80 bytes per path and depth).
+    const int64_t target_paths = rec_depth ? (int64_t)(1 << 21) : (int64_t)(1 << 25);
     int batch = (int)std::max<int64_t>(1, std::min<int64_t>(frames, target_paths / std::max<int64_t>(npix, 1)));
     if (train) batch = 1;  // one Adam step after every frame
     const int64_t vcap = recording ? npix * (cfg->max_depth + 1) * (collect_hi - collect_lo) : 0;
