@@ -197,8 +197,9 @@ typedef struct pgx_render_config {
  * (MitchellNetravaliFilter, Imaging.h:153-176) instead of the box filter
  * RayTracer::init installs (Renderer.h:255). */
 #define PGX_RENDER_FILTER_MITCHELL 2
-/* PGX_MODE_GUIDED_MLP: after every frame, one Adam step of the learned guide
- * on the radiance samples that frame's paths produced (pgx_mlp_configure). */
+/* PGX_MODE_GUIDED_MLP: after every frame, the configured Adam steps of the
+ * learned guide on the radiance samples that frame's paths produced
+ * (pgx_mlp_configure). */
 #define PGX_RENDER_TRAIN_GUIDE 4
 /* Per-stage CUDA-event times only: the kernels are the ones a render without
  * flags runs. */
@@ -507,7 +508,7 @@ int pgx_batch_create(pgx_ctx* const* scenes, int32_t n, pgx_batch** out);
 int pgx_batch_destroy(pgx_batch* batch);
 /* Adds spp samples per pixel to every scene's film. */
 int pgx_batch_render(pgx_batch* batch, int32_t spp, uint64_t seed, int32_t max_depth);
-/* Times every candidate tuning (wave capacity 1M-8M paths, traversal and
+/* Times every candidate tuning (wave capacity 1M-32M paths, traversal and
  * shading grid sizes) on `spp` samples of the batch into a scratch film
  * (the scenes' films are not touched), keeps the fastest and returns it.
  * The traversal stack depth is fixed at 64 entries, as in the reference. */

@@ -1829,7 +1829,7 @@ extern "C" int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t fr
     // vertex records cost 80 bytes per path and depth).
     const int64_t target_paths = rec_depth ? (int64_t)(1 << 21) : (int64_t)(1 << 25);
     int batch = (int)std::max<int64_t>(1, std::min<int64_t>(frames, target_paths / std::max<int64_t>(npix, 1)));
-    if (train) batch = 1;  // one Adam step after every frame
+    if (train) batch = 1;  // one round of Adam steps after every frame
     const int64_t vcap = recording ? npix * (cfg->max_depth + 1) * (collect_hi - collect_lo) : 0;
     const bool mlp_mode = cfg->mode == PGX_MODE_GUIDED_MLP;
     const int64_t tcap = train ? mlp_train_batch(ctx) : 0;
@@ -2160,7 +2160,7 @@ struct pgx_batch {
     pgx_ctx* host = nullptr;        // merged arrays, stream, error text, path state
     std::vector<BatchInfo> info;    // per scene (roots and bases fixed at creation)
     DevBuf d_info, d_prefix, d_seed;
-    pgx_batch_tuning tuning{1 << 22, 8, 16};
+    pgx_batch_tuning tuning{1 << 24, 8, 16};
     pgx_batch_stats stats{};
     cudaGraphExec_t graph = nullptr;
     int g_spp = -1, g_depth = -1;
@@ -2450,7 +2450,7 @@ extern "C" int pgx_batch_autotune(pgx_batch* b, int32_t spp, int32_t max_depth, 
     uint64_t seed = 0x5eedULL;
     PGX_CUDA_TRY(h, cudaMemcpyAsync(b->d_seed.p, &seed, sizeof(uint64_t), cudaMemcpyHostToDevice, h->stream));
     const int64_t total = b->stats.paths;
-    const int64_t waves[] = {1 << 20, 1 << 21, 1 << 22, 1 << 23};
+    const int64_t waves[] = {1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24, 1 << 25};
     const int trace_bps[] = {4, 8};
     const int shade_bps[] = {8, 16};
     float best_ms = 1e30f;
