@@ -1,20 +1,24 @@
 // Wavefront path tracer: RayTracer::render (Renderer.h:648-747) with the
 // integrators pathTraceRecursive (Renderer.h:531-613, PGX_MODE_PLAIN) and
 // guidedPath/guidedPathRecursive (Renderer.h:368-528, PGX_MODE_GUIDED_LI),
-// plus the QuadTree-guided estimator (PGX_MODE_GUIDED_QUADTREE, guide.cuh)
+// plus the QuadTree-guided estimator (PGX_MODE_GUIDED_QUADTREE, pgx_guide.cuh)
 // and the learned-guide estimator (PGX_MODE_GUIDED_MLP, pgx_mlp.cuh), whose
 // network runs on the tensor cores in k_guide_infer between traversal and
 // shading at every depth.
 //
-// One path per (pixel, sample).  The recursion of the reference becomes a
-// loop over depth with queue-per-stage kernels:
-//   camgen -> [extend -> shade -> shadow] x (max_depth + 1) -> finalize
-// `shade` compacts surviving paths into the next queue with warp-aggregated
-// atomics (ballot + popc, one atomicAdd per warp) and appends next-event
-// shadow rays to a shadow queue; `shadow` runs the any-hit traversal and
-// adds the stored contribution of unoccluded rays to the path's radiance.
-// Queue lengths live on the device, so a frame needs no host round trip
-// and is replayed from a captured CUDA graph.
+// One path per (pixel, sample); a wave holds up to 2^25 of them.  The
+// recursion of the reference becomes a loop over depth with queue-per-stage
+// kernels:
+//   camgen -> [extend -> classify -> (guide_infer) -> shade x 6 classes
+//              -> shadow] x (max_depth + 1) -> finalize
+// `classify` bins the depth's paths by surface class and `shade` runs once
+// per class with that class's code compiled in; it compacts surviving paths
+// into the next queue with warp-aggregated atomics (ballot + popc, one
+// atomicAdd per warp) and appends next-event shadow rays to a shadow queue;
+// `shadow` runs the any-hit traversal and adds the stored contribution of
+// unoccluded rays to the path's radiance.  Queue lengths live on the device,
+// so a wave needs no host round trip (batches replay their waves from a
+// captured CUDA graph).
 //
 // Each path owns a PCG32 stream keyed by (seed, pixel, sample) and draws
 // from it in the reference's order (jitter, light pick, light sample, RR,
