@@ -641,7 +641,7 @@ __global__ void __launch_bounds__(kThreads) k_classify(SceneView sv, PathState p
             cls[j] = -1;
             if (p[j] >= 0) {
                 const int id = __float_as_int(ps.hit[p[j]].x);
-                cls[j] = id >= 0 ? (int)sv.tri_class[id] : 0;
+                cls[j] = id >= 0 ? min((int)sv.tri_class[id], kShadeClasses - 1) : 0;
             }
         }
         __syncthreads();  // counters cleared
