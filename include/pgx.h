@@ -517,6 +517,17 @@ int pgx_batch_set_tuning(pgx_batch* batch, const pgx_batch_tuning* tuning);
 int pgx_batch_get_stats(pgx_batch* batch, pgx_batch_stats* stats);
 const char* pgx_batch_last_error(pgx_batch* batch);
 
+/* ---- image decoding (scene ingestion) --------------------------------------
+ * Texture::load (Imaging.h:44-79) reads albedo maps with stb_image; the
+ * loader decodes PNG, HDR, BMP and TGA itself and JPEG here, on the host (no
+ * context or GPU needed).  Baseline, extended (8-bit) and progressive
+ * Huffman-coded JPEG with 1 or 3 components: 8-bit samples, rows top-down,
+ * interleaved.  With out == NULL only width, height and channels are filled.
+ * Returns PGX_ERR_INVALID_ARG for malformed or unsupported data (msg, when
+ * not NULL, gets a description of at most msg_size bytes). */
+int pgx_image_decode_jpeg(const uint8_t* data, int64_t size, int32_t* width, int32_t* height, int32_t* channels,
+                          uint8_t* out, int64_t out_size, char* msg, int32_t msg_size);
+
 #ifdef __cplusplus
 }
 #endif

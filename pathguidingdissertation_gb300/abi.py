@@ -162,6 +162,7 @@ SIGNATURES = {
     "pgx_batch_set_tuning": (C.c_int, [_P, C.POINTER(BatchTuning)]),
     "pgx_batch_get_stats": (C.c_int, [_P, C.POINTER(BatchStats)]),
     "pgx_batch_last_error": (C.c_char_p, [_P]),
+    "pgx_image_decode_jpeg": (C.c_int, [_P, _I64, _P, _P, _P, _P, _I64, _P, _I32]),
 }
 
 _lib: C.CDLL | None = None

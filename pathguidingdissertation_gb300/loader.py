@@ -203,6 +203,25 @@ def read_tga(path: str | Path) -> tuple[np.ndarray, int]:
     return np.ascontiguousarray(out), ch
 
 
+def read_jpeg(path: str | Path) -> tuple[np.ndarray, int]:
+    """8-bit samples (H, W, C) and channel count of a JPEG file, decoded by
+    libpgx's pgx_image_decode_jpeg (baseline and progressive Huffman JPEG).
+    Raises ValueError for malformed or unsupported data."""
+    from . import abi
+    data = Path(path).read_bytes()
+    lib = abi.load()
+    buf = (ctypes.c_uint8 * len(data)).from_buffer_copy(data)
+    w, h, c = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    msg = ctypes.create_string_buffer(256)
+    args = (ctypes.addressof(buf), len(data), ctypes.byref(w), ctypes.byref(h), ctypes.byref(c))
+    if lib.pgx_image_decode_jpeg(*args, None, 0, msg, 256) != abi.PGX_OK:
+        raise ValueError(f"{path}: {msg.value.decode(errors='replace')}")
+    out = np.zeros(w.value * h.value * c.value, np.uint8)
+    if lib.pgx_image_decode_jpeg(*args, out.ctypes.data, out.size, msg, 256) != abi.PGX_OK:
+        raise ValueError(f"{path}: {msg.value.decode(errors='replace')}")
+    return out.reshape(h.value, w.value, c.value), c.value
+
+
 def _white() -> np.ndarray:
     """Texture::loadDefault (Imaging.h:36-42)."""
     return np.ones((1, 1, 3), F32)
@@ -215,7 +234,10 @@ def load_texture(path: str) -> np.ndarray:
     failing does in the reference.  8-bit images are scaled by 1/255; the
     reference reads texel i at bytes [i*C, i*C+3) whatever the channel count C,
     so 1- and 2-channel images take their colour from the next bytes (bytes
-    past the end of the image read as 0 here).  JPEG is not decoded."""
+    past the end of the image read as 0 here).  JPEG is decoded by libpgx
+    (pgx_image_decode_jpeg), whose samples agree with stb_image's to within a
+    few levels (it rounds the inverse DCT, chroma upsampling and colour
+    conversion in floating point where stb_image uses fixed point)."""
     if ".hdr" in path:
         try:
             return read_hdr(path)
@@ -230,9 +252,7 @@ def load_texture(path: str) -> np.ndarray:
         elif low.endswith(".tga"):
             img, ch = read_tga(path)
         elif low.endswith((".jpg", ".jpeg")):
-            if not Path(path).exists():
-                return _white()
-            raise NotImplementedError(f"{path}: JPEG textures are not supported by this loader")
+            img, ch = read_jpeg(path)
         else:
             return _white()
     except (OSError, ValueError):
