@@ -487,7 +487,7 @@ int pgx_diff_adjoint(pgx_ctx* ctx, int32_t spp, uint64_t seed, int32_t max_depth
  * (seed, pixel, sample) of pgx_render, so a scene's image equals
  * pgx_render's for the same seed.  The waves of one call are captured in
  * one CUDA graph, replayed while spp, max_depth and the tuning stay the
- * same.  Scenes with an environment map are rejected (area lights only). */
+ * same.  Environment maps are read from the scenes' own contexts. */
 typedef struct pgx_batch pgx_batch;
 
 typedef struct pgx_batch_tuning {

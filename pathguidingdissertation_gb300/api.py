@@ -325,7 +325,7 @@ class Batch:
         h = C.c_void_p()
         rc = self.lib.pgx_batch_create(arr, len(self.contexts), C.byref(h))
         if rc != 0:
-            raise PgxError(rc, "pgx_batch_create failed (scenes need a BVH, area lights and no environment map)")
+            raise PgxError(rc, "pgx_batch_create failed (scenes need an uploaded scene and a BVH on one device)")
         self.h = h
 
     def check(self, rc: int) -> None:

@@ -157,6 +157,8 @@ struct BatchInfo {
     TravRoot root;        // the scene's tree in the merged node array
     int light_base;       // its area lights in the merged light array
     int n_lights;
+    DevEnv env;           // its environment map (the scene context's own buffers)
+    int has_env_light;    // the environment is light 0 of NEE
     DevCamera cam;
     SceneBoundsDev bounds;
     int width, height;
@@ -706,8 +708,10 @@ __global__ void __launch_bounds__(kThreads, kShadeBlocksPerSM) k_shade(SceneView
             if (active) {
                 const BatchInfo& bi = binfo[ps.scene[p]];
                 svb.lights = sv0.lights + bi.light_base;
-                svb.nlights = bi.n_lights;
+                svb.nlights = bi.n_lights + bi.has_env_light;
                 svb.n_area_lights = bi.n_lights;
+                svb.env = bi.env;
+                svb.has_env_light = bi.has_env_light;
                 svb.bounds = bi.bounds;
                 svb.width = bi.width;
                 svb.height = bi.height;
@@ -2263,7 +2267,6 @@ extern "C" int pgx_batch_create(pgx_ctx* const* scenes, int32_t n, pgx_batch** o
         pgx_ctx* c = scenes[i];
         if (!c || c->device != scenes[0]->device) return PGX_ERR_INVALID_ARG;
         if (!c->has_scene || !c->has_bvh) return PGX_ERR_STATE;
-        if (c->env.valid || c->n_area_lights == 0) return PGX_ERR_INVALID_ARG;
         recs += c->n_records;
         tris += c->ntris;
         mats += c->nmats;
@@ -2330,6 +2333,8 @@ extern "C" int pgx_batch_create(pgx_ctx* const* scenes, int32_t n, pgx_batch** o
         bi.root.ref += (c->root.count > 0) ? (int)tb : (int)rb;
         bi.light_base = (int)lb;
         bi.n_lights = c->n_area_lights;
+        bi.env = c->env;
+        bi.has_env_light = (c->env.valid && c->env.power > 0.f) ? 1 : 0;
         bi.cam = c->camera;
         bi.bounds = c->bounds;
         bi.width = c->width;

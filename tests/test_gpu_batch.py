@@ -65,10 +65,29 @@ def test_autotune_keeps_films_and_tuning_applies(pgx_lib):
         c.close()
 
 
-def test_batch_rejects_environment_scenes(pgx_lib):
-    c = Context(0)
-    c.upload(scenes.interior(seed=3, target_tris=3000, n_objects=10, width=16, height=16, env_width=16, env_height=8))
-    c.bvh_build()
-    with pytest.raises(abi.PgxError):
-        Batch([c])
-    c.close()
+def test_batch_with_environment_scenes_equals_single_renders(pgx_lib):
+    """Scenes lit by environment maps (each read from its own context) batched
+    with area-lit ones: the same images as rendering each scene alone."""
+    def interior(seed, w, h, ew, eh):
+        c = Context(0)
+        c.upload(scenes.interior(seed=seed, target_tris=3000, n_objects=10, width=w, height=h, env_width=ew,
+                                 env_height=eh))
+        c.bvh_build()
+        c.clear()
+        return c
+
+    def make():
+        return [interior(3, 24, 16, 64, 32), _ctx(SPECS[1]), interior(5, 16, 20, 32, 16)]
+
+    batch_ctx, solo = make(), make()
+    b = Batch(batch_ctx)
+    b.render(8, seed=7, max_depth=8)
+    for bc, sc in zip(batch_ctx, solo):
+        sc.render(8, mode=abi.MODE_PLAIN, seed=7, max_depth=8)
+        a, _, na = bc.film()
+        r, _, nr = sc.film()
+        assert na == nr == 8 and r.any()
+        assert _close(a.astype(np.float64), r.astype(np.float64)) < 1e-4
+    b.close()
+    for c in batch_ctx + solo:
+        c.close()
