@@ -24,7 +24,8 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from .abi import (BSDF_CONDUCTOR, BSDF_DIFFUSE, BSDF_GLASS, MATERIAL, RAY, TRIANGLE)
+from .abi import (BSDF_CONDUCTOR, BSDF_DIELECTRIC, BSDF_DIFFUSE, BSDF_GLASS, BSDF_MIRROR, BSDF_ORENNAYAR,
+                  BSDF_PLASTIC, MATERIAL, RAY, TRIANGLE)
 
 
 @dataclass
@@ -201,6 +202,33 @@ def cornell_box(seed: int = 1, width: int = 256, height: int = 256, target_tris:
     mb.quad_grid((-0.25, 1.999, -0.25), (0.5, 0, 0), (0, 0, 0.5), (0, -1, 0), 1, len(mats) - 1)
     cam = dict(from_=(0.0, 1.0, 3.8), to=(0.0, 1.0, 0.0), up=(0.0, 1.0, 0.0), fov=40.0, width=width, height=height)
     return SceneDesc(mb.triangles(), np.array(mats, MATERIAL), cam, name="cornell_box")
+
+
+def material_zoo(seed: int = 1, width: int = 64, height: int = 64, env: bool = False) -> SceneDesc:
+    """The Cornell box with a box of every further BSDF kind on its floor:
+    mirror, rough plastic, rough dielectric, Oren-Nayar, smooth and rough
+    conductor, layered diffuse (LayeredBSDF) and glass; with `env`, a sky and
+    sun environment map lights it as well."""
+    base = cornell_box(seed=seed, width=width, height=height)
+    rng = np.random.default_rng(seed + 100)
+    mb = MeshBuilder()
+    mats = list(base.materials)
+    kinds = [material(BSDF_MIRROR, albedo=(0.9, 0.9, 0.9)),
+             material(BSDF_PLASTIC, albedo=(0.2, 0.5, 0.8), roughness=0.3, int_ior=1.5, ext_ior=1.0),
+             material(BSDF_DIELECTRIC, albedo=(1, 1, 1), roughness=0.2, int_ior=1.45, ext_ior=1.0),
+             material(BSDF_ORENNAYAR, albedo=(0.7, 0.4, 0.3), sigma=0.6),
+             conductor_from_f0(0.9, 0.0),
+             conductor_from_f0(0.7, 0.35),
+             material(BSDF_DIFFUSE, albedo=(0.5, 0.7, 0.3), layered=1),
+             material(BSDF_GLASS, albedo=(1, 1, 1), int_ior=1.5, ext_ior=1.0)]
+    for i, m in enumerate(kinds):
+        mats.append(m)
+        cx, cz = -0.7 + 0.2 * i, 0.55 - 0.12 * (i % 3)
+        s = rng.uniform(0.12, 0.18)
+        mb.box((cx, s * 0.5 + 0.001, cz), (s, s, s), math.radians(rng.uniform(0.0, 90.0)), len(mats) - 1)
+    tris = np.concatenate([base.triangles, mb.triangles()])
+    envmap = sky_envmap(64, 32) if env else None
+    return SceneDesc(tris, np.array(mats, MATERIAL), base.camera, env=envmap, name="material_zoo")
 
 
 def sky_envmap(width: int = 2048, height: int = 1024, sun_dir=(0.8, 0.45, 0.25), sun_sigma_deg: float = 1.0,

@@ -48,6 +48,24 @@ def test_render_per_pixel_vs_reference(ctx, reference, mode, scene):
     _compare(film, ref_film)
 
 
+@pytest.mark.parametrize("env", [False, True], ids=["area", "area+env"])
+@pytest.mark.parametrize("mode", [abi.MODE_PLAIN, abi.MODE_GUIDED_LI])
+def test_render_every_material_kind_vs_reference(ctx, reference, mode, env):
+    """Every BSDF kind — mirror, rough plastic, rough dielectric, Oren-Nayar
+    and layered (the 'other' shading class), smooth and rough conductors,
+    glass — against the reference's integrators driven by the same streams."""
+    desc = scenes.material_zoo(seed=1, width=64, height=64, env=env)
+    ctx.upload(desc)
+    nodes, idx = reference.bvh_build(desc.triangles)
+    ctx.bvh_import(nodes, idx)
+    ctx.clear()
+    ctx.render(4, mode=mode, seed=13, max_depth=8)
+    film, _, _ = ctx.film()
+    rs = reference.scene(desc)
+    ref_film, _, _ = rs.render_pcg(mode == abi.MODE_GUIDED_LI, 13, 0, 4, threads=8)
+    _compare(film, ref_film)
+
+
 def test_guided_li_vertices_vs_reference(ctx, reference):
     desc = scenes.cornell_box(seed=1, width=48, height=48)
     ctx.upload(desc)
