@@ -432,14 +432,16 @@ def run_relmse_study(args) -> dict:
                  "adam_steps_per_frame": args.mlp_steps, "guide_depth": args.guide_depth,
                  "target": "indirect" if args.mlp_indirect else "full incident radiance"}
     else:
-        # QuadTree: train the cache over `train_iters` iterations of 1, 2, 4,
-        # ... frames (the first plain, the rest guided by the previous cache;
-        # every iteration's records rebuild the cache), all timed.
-        mode = abi.MODE_GUIDED_QUADTREE
+        # QuadTree (directions) or PSS (primary samples): train the cache over
+        # `train_iters` iterations of 1, 2, 4, ... frames (the first unguided,
+        # the rest guided by the previous cache; every iteration's records
+        # rebuild the cache, in the domain of the mode that recorded them),
+        # all timed.
+        mode = abi.MODE_GUIDED_PSS if args.guide == "pss" else abi.MODE_GUIDED_QUADTREE
         for it in range(args.train_iters):
             ctx.clear()
             n = 1 << it
-            m = abi.MODE_PLAIN if it == 0 else abi.MODE_GUIDED_QUADTREE
+            m = abi.MODE_PLAIN if (it == 0 and args.guide == "quadtree") else mode
             train_ms += render_ms(n, m, 11 + it, record_paths=n, guide_fraction=args.guide_fraction)
             train_ms += ctx.cache_stats().build_ms
             train_spp += n
@@ -841,7 +843,7 @@ def main() -> None:
     ap.add_argument("--plain-spp", type=int, default=1024)
     ap.add_argument("--train-iters", type=int, default=6)
     ap.add_argument("--guide-fraction", type=float, default=0.5)
-    ap.add_argument("--guide", choices=["mlp", "quadtree"], default="mlp")
+    ap.add_argument("--guide", choices=["mlp", "quadtree", "pss"], default="mlp")
     ap.add_argument("--metric", choices=["robust", "plain"], default="robust")
     ap.add_argument("--train-frames", type=int, default=64)
     ap.add_argument("--mlp-lr", type=float, default=5e-3)

@@ -170,7 +170,18 @@ enum pgx_render_mode {
      * every non-specular vertex the network's vMF mixture for (position,
      * shading normal, wo) is evaluated on the tensor cores and mixed with
      * the BSDF by one-sample MIS; needs pgx_mlp_init. */
-    PGX_MODE_GUIDED_MLP = 3
+    PGX_MODE_GUIDED_MLP = 3,
+    /* Extension: guiding in the BSDF's primary sample space, the design of
+     * Renderer.h:398-414 (record (position, wi, Li), invert the BSDF's
+     * sampling, sample the primary sample space): the radiance cache's
+     * regions hold quadtrees over the primary samples that the diffuse
+     * BSDFs' cosine sampler maps to the records' wi (BSDF::invert,
+     * Materials.h:163-171); at a diffuse or Oren-Nayar vertex a primary
+     * sample drawn from the region's quadtree (probability guide_fraction,
+     * else uniform) goes through BSDF::sample, and the pdf is the quadtree
+     * mixture's density at the sample times the BSDF pdf.  A render in this
+     * mode with record_paths builds the cache in this form. */
+    PGX_MODE_GUIDED_PSS = 4
 };
 
 typedef struct pgx_render_config {

@@ -35,7 +35,7 @@ RADIANCE_SAMPLE = np.dtype([("position", "<f4", 3), ("normal", "<f4", 3), ("wo",
 # BSDF kinds
 BSDF_DIFFUSE, BSDF_MIRROR, BSDF_CONDUCTOR, BSDF_GLASS, BSDF_DIELECTRIC, BSDF_ORENNAYAR, BSDF_PLASTIC = range(7)
 # render modes
-MODE_PLAIN, MODE_GUIDED_LI, MODE_GUIDED_QUADTREE, MODE_GUIDED_MLP = 0, 1, 2, 3
+MODE_PLAIN, MODE_GUIDED_LI, MODE_GUIDED_QUADTREE, MODE_GUIDED_MLP, MODE_GUIDED_PSS = 0, 1, 2, 3, 4
 
 # ---- numpy layouts of the C structs ---------------------------------------------
 VERTEX = np.dtype([("p", "<f4", 3), ("n", "<f4", 3), ("u", "<f4"), ("v", "<f4")])

@@ -55,6 +55,7 @@ struct CacheState {
     int64_t n_nodes = 0;
     int n_regions = 0;
     bool valid = false;
+    bool pss = false;  // quadtrees over the diffuse BSDF's primary samples
     double build_ms = 0.0;
 };
 
@@ -497,7 +498,8 @@ constexpr int kQtWarps = 4;
 
 __global__ void __launch_bounds__(32 * kQtWarps) k_quadtree(const int2* __restrict__ regions, int nreg,
                                                             const pgx_path_vertex* __restrict__ recs,
-                                                            int* __restrict__ qroot, QuadNode* __restrict__ qnodes) {
+                                                            int* __restrict__ qroot, QuadNode* __restrict__ qnodes,
+                                                            int pss) {
     __shared__ float s_u[kQtWarps][PGX_QT_MAX_NODES], s_v[kQtWarps][PGX_QT_MAX_NODES],
         s_s[kQtWarps][PGX_QT_MAX_NODES];
     __shared__ unsigned char s_d[kQtWarps][PGX_QT_MAX_NODES];
@@ -571,7 +573,12 @@ __global__ void __launch_bounds__(32 * kQtWarps) k_quadtree(const int2* __restri
             float w = fminf(record_lum(rr[i]), clamp);
             if (!(w > 0.f)) continue;
             float u, vv;
-            dir_to_uv(f3(rr[i].wi[0], rr[i].wi[1], rr[i].wi[2]), u, vv);
+            const F3 wi = f3(rr[i].wi[0], rr[i].wi[1], rr[i].wi[2]);
+            if (pss) {
+                if (!pss_uv(f3(rr[i].normal[0], rr[i].normal[1], rr[i].normal[2]), wi, u, vv)) continue;
+            } else {
+                dir_to_uv(wi, u, vv);
+            }
             if (u < u0 || u >= u0 + sz || vv < v0 || vv >= v0 + sz) continue;
             int c = 2 * (vv >= v0 + half ? 1 : 0) + (u >= u0 + half ? 1 : 0);
             flux[c] += w;
@@ -742,6 +749,7 @@ GuideView guide_view(const pgx_ctx* ctx) {
     g.region_qroot = cs->qroot.as<int>();
     g.qnodes = cs->qnodes.as<QuadNode>();
     g.node_region = cs->node_region.as<int>();
+    g.pss = cs->pss ? 1 : 0;
     return g;
 }
 
@@ -751,9 +759,10 @@ bool guide_ready(const pgx_ctx* ctx) {
 }
 
 // Builds the cache from n records already on the device.
-int cache_build_device(pgx_ctx* ctx, const pgx_path_vertex* d_records, int64_t n) {
+int cache_build_device(pgx_ctx* ctx, const pgx_path_vertex* d_records, int64_t n, bool pss) {
     CacheState* cs = cstate(ctx);
     cs->valid = false;
+    cs->pss = pss;
     if (n < 0 || n > (int64_t)INT32_MAX / 2) return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "cache: bad record count");
     auto t0 = std::chrono::steady_clock::now();
     cudaStream_t s = ctx->stream;
@@ -858,7 +867,7 @@ int cache_build_device(pgx_ctx* ctx, const pgx_path_vertex* d_records, int64_t n
     PGX_CUDA_TRY(ctx, cs->qroot.reserve(sizeof(int) * std::max(1, cs->n_regions)));
     PGX_CUDA_TRY(ctx, cs->qnodes.reserve(sizeof(QuadNode) * PGX_QT_MAX_NODES * (size_t)std::max(1, cs->n_regions)));
     k_quadtree<<<blocks_for(cs->n_regions, kQtWarps), 32 * kQtWarps, 0, s>>>(
-        regions, cs->n_regions, recs, cs->qroot.as<int>(), cs->qnodes.as<QuadNode>());
+        regions, cs->n_regions, recs, cs->qroot.as<int>(), cs->qnodes.as<QuadNode>(), pss ? 1 : 0);
     k_rebase_children<<<std::max(1, cs->n_regions), 128, 0, s>>>(cs->qnodes.as<QuadNode>(), cs->qroot.as<int>(),
                                                                    cs->n_regions);
     k_rebase<<<blocks_for(cs->n_regions, 128), 128, 0, s>>>(cs->qroot.as<int>(), cs->n_regions);
@@ -980,6 +989,9 @@ static int guide_query(pgx_ctx* ctx, const float* positions, const float* in, in
     if (n < 0 || (n > 0 && (!positions || !in || !pdf || (sample && !dirs))))
         return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_guide_*: bad arguments");
     if (!guide_ready(ctx)) return pgx_fail(ctx, PGX_ERR_STATE, "pgx_guide_*: no radiance cache");
+    if (cstate(ctx)->pss)
+        return pgx_fail(ctx, PGX_ERR_STATE,
+                        "pgx_guide_*: the cache was built by a PGX_MODE_GUIDED_PSS render (primary-sample trees)");
     if (n == 0) return PGX_OK;
     cudaStream_t s = ctx->stream;
     const size_t in_floats = sample ? 2 : 3;

@@ -51,11 +51,12 @@ struct GuideView {
     const int* __restrict__ region_qroot; // first QuadNode of each region (-1: no flux)
     const QuadNode* __restrict__ qnodes;
     const int* __restrict__ node_region;  // region index of region-root nodes, else -1
+    int pss;  // 1: the quadtrees are over the diffuse BSDF's primary samples, 0: over directions
 };
 
 GuideView guide_view(const pgx_ctx* ctx);
 bool guide_ready(const pgx_ctx* ctx);
-int cache_build_device(pgx_ctx* ctx, const pgx_path_vertex* d_records, int64_t n);
+int cache_build_device(pgx_ctx* ctx, const pgx_path_vertex* d_records, int64_t n, bool pss = false);
 
 __device__ __forceinline__ void dir_to_uv(F3 w, float& u, float& v) {
     float c = fminf(fmaxf(w.z, -1.f), 1.f);
@@ -225,6 +226,26 @@ __device__ __forceinline__ float guide_pdf_dir(const GuideView& g, int qroot, F3
            (1.f / (4.f * 3.14159265f));
 }
 
+// Primary sample of the diffuse BSDFs' sampler mapping to wi at a record or
+// shading point with shading normal n (the frame the shading code builds),
+// clamped into the quadtree's half-open square; false below the hemisphere.
+__device__ __forceinline__ bool pss_uv(F3 n, F3 wi, float& u, float& v) {
+    const Frame fr = frame_from(n);
+    if (dot(wi, fr.w) <= 0.f) return false;
+    cosine_invert(fr, wi, u, v);
+    u = fminf(fmaxf(u, 0.f), 0.99999994f);
+    v = fminf(fmaxf(v, 0.f), 0.99999994f);
+    return true;
+}
+
+// Density over the primary-sample square of the PSS guide at (u, v): the
+// quadtree mixed with a uniform share.
+__device__ __forceinline__ float guide_pdf_uv(const GuideView& g, int qroot, float u, float v) {
+    u = fminf(fmaxf(u, 0.f), 0.99999994f);
+    v = fminf(fmaxf(v, 0.f), 0.99999994f);
+    return (1.f - PGX_GUIDE_UNIFORM) * quad_pdf(g.qnodes, qroot, u, v) + PGX_GUIDE_UNIFORM;
+}
+
 // Solid-angle pdf of the one-sample mixture at wi.
 __device__ __forceinline__ float mixture_pdf(const GuideView& g, int qroot, float frac, float bsdf_p, F3 wi) {
     if (qroot < 0) return bsdf_p;
@@ -259,6 +280,52 @@ __device__ __forceinline__ F3 guided_sample(const GuideView& g, float frac, cons
     }
     float bp = bsdf_pdf_k<K>(m, tv, sd, wi);
     pdf = mixture_pdf(g, qroot, frac, bp, wi);
+    return wi;
+}
+
+// ---- guiding in the BSDF's primary sample space (PGX_MODE_GUIDED_PSS) ----------------
+// Surfaces guided: the diffuse BSDFs, whose cosine sampler the cache's
+// primary-sample quadtrees were built with.  K: the kind when known.
+template <int K = -1>
+__device__ __forceinline__ bool pss_surface(const DevMaterial& m) {
+    const int kind = K >= 0 ? K : m.kind;
+    return !m.is_light && (kind == PGX_BSDF_DIFFUSE || kind == PGX_BSDF_ORENNAYAR);
+}
+
+// Solid-angle pdf at wi of the mixture that draws the primary sample from
+// the guide with probability frac (else uniformly) and maps it through the
+// cosine sampler: (frac q(u, v) + 1 - frac) x the BSDF pdf, (u, v) the
+// sampler's inverse at wi.
+__device__ __forceinline__ float pss_mixture_pdf(const GuideView& g, int qroot, float frac, const Shading& sd,
+                                                 float bsdf_p, F3 wi) {
+    if (qroot < 0) return bsdf_p;
+    if (dot(wi, sd.frame.w) <= 0.f) return (1.f - frac) * bsdf_p;  // the cosine sampler never goes there
+    float u, v;
+    cosine_invert(sd.frame, wi, u, v);
+    return (frac * guide_pdf_uv(g, qroot, u, v) + (1.f - frac)) * bsdf_p;
+}
+
+// Continuation direction of the PSS-guided estimator: a primary sample from
+// the region's quadtree (probability frac; the selection number is reused
+// for the uniform share) or uniform, through BSDF::sample; pdf is the
+// mixture's solid-angle density.
+template <int K = -1>
+__device__ __forceinline__ F3 pss_guided_sample(const GuideView& g, float frac, const DevMaterial& m,
+                                                const TexView& tv, const Shading& sd, uint64_t& rng, F3& f,
+                                                float& pdf, int qroot) {
+    if (qroot < 0) return bsdf_sample_k<K>(m, tv, sd, rng, f, pdf);
+    const float sel = pgx_rng_next(rng);
+    const float r1 = pgx_rng_next(rng), r2 = pgx_rng_next(rng);
+    float u = r1, v = r2;
+    if (sel < frac && sel / frac >= PGX_GUIDE_UNIFORM) quad_sample(g.qnodes, qroot, r1, r2, u, v);
+    FixedSampler fs{u, v, 0};
+    float bp;
+    F3 wi;
+    if constexpr (K >= 0)
+        wi = bsdf_sample_i<K>(m, tv, sd, fs, f, bp);
+    else
+        wi = bsdf_sample_s(m, tv, sd, fs, f, bp);
+    pdf = (frac * guide_pdf_uv(g, qroot, u, v) + (1.f - frac)) * bp;
     return wi;
 }
 

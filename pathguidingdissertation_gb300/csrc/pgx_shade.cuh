@@ -652,18 +652,24 @@ __device__ __forceinline__ F3 bsdf_sample_k(const DevMaterial& m, const TexView&
 // (u, v) that BSDF::sample would map to wi.  Delta lobes give (0, 0); the
 // reference leaves the rough dielectric and plastic unimplemented
 // (Materials.h:541-543, 782-784), so their (u, v) stay unchanged.
+// The primary sample that the cosine-weighted hemisphere sampler of the
+// diffuse BSDFs maps to wi in frame fr (BSDF::invert, Materials.h:163-171):
+// u = cos^2 theta, v = phi / 2pi.
+__device__ __forceinline__ void cosine_invert(const Frame& fr, F3 wi, float& u, float& v) {
+    F3 wl = to_local(fr, wi);
+    float theta = acosf(wl.z);
+    float phi = spherical_phi(wl);
+    float c = cosf(theta);
+    u = c * c;
+    v = phi * PGX_INV_2PI_F;
+}
+
 static __device__ __noinline__ void bsdf_invert(const DevMaterial& m, const Shading& sd, F3 wi, float& u, float& v) {
     switch (m.kind) {
         case PGX_BSDF_DIFFUSE:
-        case PGX_BSDF_ORENNAYAR: {
-            F3 wl = to_local(sd.frame, wi);
-            float theta = acosf(wl.z);
-            float phi = spherical_phi(wl);
-            float c = cosf(theta);
-            u = c * c;
-            v = phi * PGX_INV_2PI_F;
+        case PGX_BSDF_ORENNAYAR:
+            cosine_invert(sd.frame, wi, u, v);
             break;
-        }
         case PGX_BSDF_CONDUCTOR: {
             if (m.alpha < PGX_EPSILON) {
                 u = 0.f;

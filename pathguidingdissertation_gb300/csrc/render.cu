@@ -402,7 +402,7 @@ __device__ __forceinline__ bool next_event_t(const SceneView& sv, const DevMater
         F3 f = bsdf_eval_k<K>(m, sv.tex, sd, wi);
         float pal = pdf_light * pmf;
         float pab = bsdf_pdf_k<K>(m, sv.tex, sd, wi);
-        if (qroot >= 0) pab = mixture_pdf(gv, qroot, frac, pab, wi);
+        if (qroot >= 0) pab = gv.pss ? pss_mixture_pdf(gv, qroot, frac, sd, pab, wi) : mixture_pdf(gv, qroot, frac, pab, wi);
         if (mix) pab = frac * mlp::packed_pdf(mix, wi) + (1.f - frac) * pab;
         float wd = power_heuristic(pal, pab);
         contrib = divs(((emitted * f) * cos_t) * wd, pal);
@@ -429,7 +429,7 @@ __device__ __forceinline__ bool next_event_t(const SceneView& sv, const DevMater
         float G = (cos_t * cos_tp) / den;
         F3 f = bsdf_eval_k<K>(m, sv.tex, sd, wi);
         float pb = bsdf_pdf_k<K>(m, sv.tex, sd, wi);
-        if (qroot >= 0) pb = mixture_pdf(gv, qroot, frac, pb, wi);
+        if (qroot >= 0) pb = gv.pss ? pss_mixture_pdf(gv, qroot, frac, sd, pb, wi) : mixture_pdf(gv, qroot, frac, pb, wi);
         if (mix) pb = frac * mlp::packed_pdf(mix, wi) + (1.f - frac) * pb;
         float pal = pdf_light * pmf;
         float pab = (pb * cos_tp) / den;
@@ -770,7 +770,9 @@ __global__ void __launch_bounds__(kThreads, kShadeBlocksPerSM) k_shade(SceneView
                 } else {
                     int qroot = -1;
                     const bool spec = bsdf_pure_specular_k<KIND>(m);
-                    if (MODE == PGX_MODE_GUIDED_QUADTREE && depth < fp.guide_depth && !spec)
+                    if (MODE == PGX_MODE_GUIDED_QUADTREE && depth < fp.guide_depth && !spec && !gv.pss)
+                        qroot = guide_region_root(gv, sd.x);
+                    if (MODE == PGX_MODE_GUIDED_PSS && depth < fp.guide_depth && gv.pss && pss_surface<KIND>(m))
                         qroot = guide_region_root(gv, sd.x);
                     const bool use_mix =
                         MODE == PGX_MODE_GUIDED_MLP && depth < fp.guide_depth && mlp_guided_surface<KIND>(m);
@@ -816,6 +818,8 @@ __global__ void __launch_bounds__(kThreads, kShadeBlocksPerSM) k_shade(SceneView
                         F3 wi;
                         if (MODE == PGX_MODE_GUIDED_QUADTREE)
                             wi = guided_sample<KIND>(gv, fp.guide_fraction, m, sv.tex, sd, rng, f, pdf, qroot);
+                        else if (MODE == PGX_MODE_GUIDED_PSS)
+                            wi = pss_guided_sample<KIND>(gv, fp.guide_fraction, m, sv.tex, sd, rng, f, pdf, qroot);
                         else if (MODE == PGX_MODE_GUIDED_MLP && use_mix && INL)
                             wi = mlp_guided_sample_t<KIND>(mix, fp.guide_fraction, m, sv.tex, sd, rng, f, pdf);
                         else if (MODE == PGX_MODE_GUIDED_MLP && use_mix)
@@ -1707,6 +1711,9 @@ int enqueue_frame(pgx_ctx* ctx, RenderState* rs, const FrameParams& fp, cudaStre
                 case PGX_MODE_GUIDED_QUADTREE:
                     launch_shade_class<PGX_MODE_GUIDED_QUADTREE, false>(c, g, s, sv, ps, fp, depth, gv, nullptr);
                     break;
+                case PGX_MODE_GUIDED_PSS:
+                    launch_shade_class<PGX_MODE_GUIDED_PSS, false>(c, g, s, sv, ps, fp, depth, gv, nullptr);
+                    break;
                 case PGX_MODE_GUIDED_MLP:
                     launch_shade_class<PGX_MODE_GUIDED_MLP, false>(c, g, s, sv, ps, fp, depth, gv, nullptr);
                     break;
@@ -1787,7 +1794,7 @@ extern "C" int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t fr
     if (!ctx) return PGX_ERR_INVALID_ARG;
     ctx->err.clear();
     if (!cfg || frames < 0) return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_render: bad arguments");
-    if (cfg->mode < PGX_MODE_PLAIN || cfg->mode > PGX_MODE_GUIDED_MLP)
+    if (cfg->mode < PGX_MODE_PLAIN || cfg->mode > PGX_MODE_GUIDED_PSS)
         return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_render: unknown mode %d", cfg->mode);
     if (cfg->max_depth < 0 || cfg->max_depth > kMaxDepthCap)
         return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_render: max_depth must be in [0, %d]", kMaxDepthCap);
@@ -1795,6 +1802,9 @@ extern "C" int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t fr
     if (!ctx->has_bvh) return pgx_fail(ctx, PGX_ERR_STATE, "pgx_render: no BVH");
     if (cfg->mode == PGX_MODE_GUIDED_QUADTREE && !guide_ready(ctx))
         return pgx_fail(ctx, PGX_ERR_STATE, "pgx_render: guided mode needs a radiance cache (pgx_cache_build)");
+    if (cfg->mode == PGX_MODE_GUIDED_QUADTREE && guide_view(ctx).pss)
+        return pgx_fail(ctx, PGX_ERR_STATE,
+                        "pgx_render: the radiance cache holds primary-sample trees (built by a PGX_MODE_GUIDED_PSS render)");
     if (cfg->mode == PGX_MODE_GUIDED_MLP && !mlp_view(ctx).valid)
         return pgx_fail(ctx, PGX_ERR_STATE, "pgx_render: learned-guide mode needs pgx_mlp_init");
     if ((cfg->flags & PGX_RENDER_TRAIN_GUIDE) && cfg->mode != PGX_MODE_GUIDED_MLP)
@@ -1920,7 +1930,8 @@ extern "C" int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t fr
     if (recording) {
         rs->nvertices_last = std::min<int64_t>(nv, rs->vcapacity);
         rst.path_vertices = rs->nvertices_last;
-        PGX_TRY(cache_build_device(ctx, rs->vertices.as<pgx_path_vertex>(), rs->nvertices_last));
+        PGX_TRY(cache_build_device(ctx, rs->vertices.as<pgx_path_vertex>(), rs->nvertices_last,
+                                   cfg->mode == PGX_MODE_GUIDED_PSS));
     }
     return PGX_OK;
 }

@@ -228,3 +228,64 @@ def test_guided_estimator_unbiased(ctx, scene, training):
     # Whole image: the difference of the two means against its standard error.
     z_total = abs(ma.sum() - mb.sum()) / np.sqrt(va.sum() + vb.sum())
     assert z_total < 4.0, z_total
+
+
+@pytest.mark.parametrize("scene", ["cornell", "interior"])
+def test_pss_guided_estimator_unbiased(ctx, scene):
+    """PGX_MODE_GUIDED_PSS: the cache is trained by renders in the mode itself
+    (the first unguided, the next guided by the first's primary-sample
+    trees); the guided image then agrees with plain path tracing per tile."""
+    if scene == "cornell":
+        desc = scenes.cornell_box(seed=1, width=48, height=48)
+    else:
+        desc = scenes.interior(seed=3, target_tris=20000, n_objects=40, width=48, height=27, env_width=256,
+                               env_height=128)
+    ctx.upload(desc)
+    ctx.bvh_build()
+    ctx.clear()
+    ctx.render(2, mode=abi.MODE_GUIDED_PSS, seed=77, max_depth=8, record_paths=2)
+    assert ctx.cache_stats().records > 0
+    ctx.clear()
+    ctx.render(4, mode=abi.MODE_GUIDED_PSS, seed=78, max_depth=8, record_paths=4, guide_fraction=0.5)
+    ctx.clear()
+    spp = 1024
+    ctx.render(spp, mode=abi.MODE_PLAIN, seed=5, max_depth=8)
+    a, a2, _ = ctx.film(squares=True)
+    ctx.clear()
+    ctx.render(spp, mode=abi.MODE_GUIDED_PSS, seed=6, max_depth=8, guide_fraction=0.5)
+    b, b2, _ = ctx.film(squares=True)
+    assert not np.array_equal(a, b)
+    t = 8
+    H, W = a.shape[:2]
+
+    def tiles(x):
+        return x[: H // t * t, : W // t * t].reshape(H // t, t, W // t, t, 3).sum(axis=(1, 3))
+
+    n = spp * t * t
+    ma, mb = tiles(a) / n, tiles(b) / n
+    va = np.maximum(tiles(a2) / n - ma * ma, 0) / n
+    vb = np.maximum(tiles(b2) / n - mb * mb, 0) / n
+    z = np.abs(ma - mb) / np.sqrt(va + vb + 1e-12)
+    assert np.mean(z < 4.0) > 0.97, np.sort(z.ravel())[-5:]
+    z_total = abs(ma.sum() - mb.sum()) / np.sqrt(va.sum() + vb.sum())
+    assert z_total < 4.0, z_total
+
+
+def test_pss_cache_refuses_direction_use(ctx):
+    """A cache built by a PSS render holds primary-sample trees: the
+    direction-space queries and the QuadTree mode refuse it."""
+    desc = scenes.cornell_box(seed=1, width=32, height=32)
+    ctx.upload(desc)
+    ctx.bvh_build()
+    ctx.clear()
+    ctx.render(2, mode=abi.MODE_GUIDED_PSS, seed=7, max_depth=8, record_paths=2)
+    _, recs = ctx.cache_export()
+    x = recs["position"][:4].astype(np.float32)
+    d = np.tile(np.array([[0.0, 1.0, 0.0]], np.float32), (4, 1))
+    with pytest.raises(abi.PgxError):
+        ctx.guide_pdf(x, d)
+    with pytest.raises(abi.PgxError):
+        ctx.render(1, mode=abi.MODE_GUIDED_QUADTREE, seed=7, max_depth=8)
+    # a plain recording rebuilds it in direction space
+    ctx.render(2, mode=abi.MODE_PLAIN, seed=7, max_depth=8, record_paths=2)
+    assert ctx.guide_pdf(x, d).shape == (4,)
