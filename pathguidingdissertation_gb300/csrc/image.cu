@@ -49,6 +49,7 @@ struct Huffman {
             valptr[len] = k;
             mincode[len] = code;
             for (int i = 0; i < counts[len - 1]; i++, k++, code++) {
+                if (code >= (1 << len)) fail("invalid Huffman table");  // over-subscribed lengths
                 if (len <= 9) {
                     const int shift = 9 - len;
                     for (int f = code << shift; f < ((code + 1) << shift); f++) {
@@ -217,7 +218,7 @@ struct Decoder {
         }
         mcux = (width + 8 * hmax - 1) / (8 * hmax);
         mcuy = (height + 8 * vmax - 1) / (8 * vmax);
-        if ((int64_t)mcux * mcuy * hmax * vmax * nc > (int64_t)1 << 26) fail("image too large");
+        if ((int64_t)mcux * mcuy * hmax * vmax * nc > (int64_t)1 << 23) fail("image too large");
         for (Component& c : comp) {
             c.bw = ((width * c.h + hmax - 1) / hmax + 7) / 8;
             c.bh = ((height * c.v + vmax - 1) / vmax + 7) / 8;
