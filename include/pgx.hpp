@@ -13,6 +13,7 @@
 // status codes; the reference printed and carried on or exited).
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <stdexcept>

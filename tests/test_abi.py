@@ -23,6 +23,23 @@ def test_header_declares_entry_points():
     assert "pgx_create" in names and "pgx_render" in names and "pgx_trace_closest" in names
 
 
+def test_headers_compile_standalone(tmp_path):
+    """pgx.h is valid C11 (for C FFI users) and pgx.hpp valid C++17, each
+    included on its own."""
+    import shutil
+    import subprocess
+    cc, cxx = shutil.which("gcc"), shutil.which("g++")
+    if not cc or not cxx:
+        import pytest
+        pytest.skip("no host compiler")
+    (tmp_path / "a.c").write_text('#include "pgx.h"\nint main(void) { return PGX_OK; }\n')
+    (tmp_path / "b.cpp").write_text('#include "pgx.hpp"\nint main() { pgx::RayTracer rt; (void)rt; return 0; }\n')
+    for comp, std, src in ((cc, "-std=c11", "a.c"), (cxx, "-std=c++17", "b.cpp")):
+        r = subprocess.run([comp, std, "-Wall", "-Wextra", "-pedantic", "-Werror", "-fsyntax-only", "-I", str(INCLUDE),
+                            str(tmp_path / src)], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+
+
 def test_library_exports_all_declared(pgx_lib):
     missing = [n for n in declared_functions() if not hasattr(pgx_lib, n)]
     assert not missing, missing
