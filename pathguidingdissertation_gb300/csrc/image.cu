@@ -411,10 +411,13 @@ struct Decoder {
                 for (int bx = 0; bx < c.pbw; bx++) {
                     const int16_t* blk = c.coef.data() + ((size_t)by * c.pbw + bx) * 64;
                     double f[64], tmp[64];
-                    bool ac = false;
+                    bool ac = false, row_nz[8] = {};
                     for (int i = 0; i < 64; i++) {
                         f[i] = (double)blk[i] * q[i];
-                        if (i && blk[i]) ac = true;
+                        if (blk[i]) {
+                            row_nz[i >> 3] = true;
+                            if (i) ac = true;
+                        }
                     }
                     uint8_t* out = c.plane.data() + (size_t)by * 8 * stride + bx * 8;
                     if (!ac) {
@@ -423,16 +426,20 @@ struct Decoder {
                         for (int y = 0; y < 8; y++) std::memset(out + (size_t)y * stride, v, 8);
                         continue;
                     }
-                    for (int v = 0; v < 8; v++)  // rows: f(v, u) -> tmp(v, x)
+                    // rows: f(v, u) -> tmp(v, x); rows of zero coefficients stay zero
+                    for (int v = 0; v < 8; v++) {
+                        if (!row_nz[v]) continue;
                         for (int x = 0; x < 8; x++) {
                             double s = 0.0;
                             for (int u = 0; u < 8; u++) s += cosv[x][u] * f[v * 8 + u];
                             tmp[v * 8 + x] = s;
                         }
+                    }
                     for (int y = 0; y < 8; y++)
                         for (int x = 0; x < 8; x++) {
                             double s = 0.0;
-                            for (int v = 0; v < 8; v++) s += cosv[y][v] * tmp[v * 8 + x];
+                            for (int v = 0; v < 8; v++)
+                                if (row_nz[v]) s += cosv[y][v] * tmp[v * 8 + x];
                             s += 128.0;
                             out[(size_t)y * stride + x] = (uint8_t)std::min(255.0, std::max(0.0, std::floor(s + 0.5)));
                         }
@@ -475,9 +482,21 @@ struct Decoder {
         // RGB-coded data: an Adobe marker with transform 0, or components named R, G, B
         const bool rgb = adobe_transform == 0 ||
                          (!jfif && adobe_transform < 0 && comp[0].id == 'R' && comp[1].id == 'G' && comp[2].id == 'B');
+        const bool full = comp[0].h == hmax && comp[0].v == vmax && comp[1].h == hmax && comp[1].v == vmax &&
+                          comp[2].h == hmax && comp[2].v == vmax;
         for (int y = 0; y < height; y++)
             for (int x = 0; x < width; x++) {
-                const int Y = sample(comp[0], x, y), cb = sample(comp[1], x, y), cr = sample(comp[2], x, y);
+                int Y, cb, cr;
+                if (full) {  // every component at full resolution: no resampling
+                    const size_t i = (size_t)y * comp[0].pbw * 8 + x;
+                    Y = comp[0].plane[i];
+                    cb = comp[1].plane[(size_t)y * comp[1].pbw * 8 + x];
+                    cr = comp[2].plane[(size_t)y * comp[2].pbw * 8 + x];
+                } else {
+                    Y = sample(comp[0], x, y);
+                    cb = sample(comp[1], x, y);
+                    cr = sample(comp[2], x, y);
+                }
                 uint8_t* o = out + ((size_t)y * width + x) * 3;
                 if (rgb) {
                     o[0] = (uint8_t)Y;
