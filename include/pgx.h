@@ -322,7 +322,10 @@ int pgx_trace_any(pgx_ctx* ctx, const pgx_ray* rays, int64_t n, uint8_t* visible
  * the life of the process.  Larger batches are rejected with
  * PGX_ERR_INVALID_ARG (split them).  Hits are identical to pgx_trace_closest.
  * The first call on a device looks up the array's device address (set-up);
- * make that first call before any stream capture starts.  All
+ * make that first call before any stream capture starts.  The address is kept
+ * for the life of the process and belongs to the device's primary context:
+ * a process that resets the device (cudaDeviceReset) must not call this
+ * entry point afterwards.  All
  * calls, from every context on a device, share the one array: calls that
  * overlap on the GPU (another thread, another context) race on it and must
  * be serialised by the caller. */
@@ -404,6 +407,36 @@ int pgx_cache_knn(pgx_ctx* ctx, const float* queries, int64_t nq, int32_t k,
  * uniform share.  positions, dirs: n*3 floats. */
 int pgx_guide_pdf(pgx_ctx* ctx, const float* positions, const float* dirs, int64_t n, float* pdf);
 int pgx_guide_sample(pgx_ctx* ctx, const float* positions, const float* u2, int64_t n, float* dirs, float* pdf);
+
+/* One region of the QuadTree guide: the point-BVH subtree (root node `node`)
+ * whose record count first drops to 1,024 (the whole cache when it holds at
+ * most 1,024 records), owning records [first, first + count) of the exported
+ * record order; its quadtree starts at quad node `qroot` (-1: no flux). */
+typedef struct pgx_guide_region {
+    int32_t first;
+    int32_t count;
+    int32_t node;
+    int32_t qroot;
+} pgx_guide_region;
+
+/* QuadTree cell (extension; the reference's QuadTree.h:24-174 holds points,
+ * not flux): the flux of its four children (index 2*y + x over the cell's
+ * halves in (u, v)) and their quad node indices (-1: leaf). */
+typedef struct pgx_quad_node {
+    float flux[4];
+    int32_t child[4];
+} pgx_quad_node;
+
+#define PGX_GUIDE_MAX_QUAD_NODES 256 /* per region */
+/* Copies the guide out for inspection: nregions regions and, when qnodes is
+ * not NULL, nregions * PGX_GUIDE_MAX_QUAD_NODES quad nodes (region r's block
+ * starts at r * PGX_GUIDE_MAX_QUAD_NODES; child indices and qroot are
+ * absolute; cells not reachable from a region's root are undefined).  Call
+ * with regions == NULL to get the count.  `pss` gets 1 when the trees are
+ * over the diffuse sampler's primary samples (a PGX_MODE_GUIDED_PSS cache),
+ * 0 for directions. */
+int pgx_guide_export(pgx_ctx* ctx, pgx_guide_region* regions, int32_t* nregions, pgx_quad_node* qnodes,
+                     int32_t* pss);
 
 /* ---- learned guide (extension; the reference has no learned component) ----
  * A 6-layer MLP (inputs: position encoded with 12 sin/cos frequencies per

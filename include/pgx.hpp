@@ -1,5 +1,5 @@
 // pgx.hpp — C++ façade over the C ABI in pgx.h, keeping the reference's class
-// names and call pattern (PathGuidingDissertation/main.cpp:408-468):
+// names and call pattern (PathGuidingDissertation/main.cpp:147-199):
 //
 //   pgx::Scene scene;                  // Scene (Scene.h:76-176)
 //   scene.init(triangles, materials, envmap, camera);

@@ -7,11 +7,17 @@ Two products, both loaded with ctypes by tests and by bench.py's CPU leg:
   reference's rounding.
 * ``oracle/_ref/liborcref.so`` (parity flags) and ``oracle/_ref/liborcref_fast.so``
   (``-O3``, timing) — the reference renderer itself, compiled headless.
-  When the reference checkout is present (``$PGX_REFERENCE_DIR`` or the
-  default mount) its headers are staged into ``oracle/_ref/src`` with the
-  platform header replaced by ``oracle/ref_shim``; on a machine without the
-  checkout the staged copy, if any, is compiled.  Nothing is written outside
-  ``oracle/_ref`` and ``oracle/_build``.
+  When the reference checkout is present its headers are staged into
+  ``oracle/_ref/src`` with the platform header replaced by ``oracle/ref_shim``;
+  on a machine without the checkout the staged copy, if any, is compiled.
+  The reference's complete scenes (every mesh present) are staged into
+  ``oracle/_ref/scenes`` so that tests can render them where the checkout is
+  absent.  Nothing is written outside ``oracle/_ref`` and ``oracle/_build``.
+
+The checkout is ``$PGX_REFERENCE_DIR`` (the project root holding
+``PathGuidingDissertation/`` and ``Scenes/``; a path to the source directory
+itself is accepted too), by default the directory ``reference`` beside this
+repository.
 """
 from __future__ import annotations
 
@@ -25,7 +31,11 @@ HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 REF_OUT = HERE / "_ref"
 REF_SRC = REF_OUT / "src"
-DEFAULT_REFERENCE = "/root/reference/PathGuidingDissertation"
+REF_SCENES = REF_OUT / "scenes"
+# Reference scenes whose meshes are all present (the others name mesh files
+# that are missing from the checkout, on which loadScene exits).
+COMPLETE_SCENES = ["cornell-box", "veach-mis", "veach-bidir", "MaterialsScene", "staircase2", "living-room",
+                   "dining-room"]
 REF_HEADERS = [
     "MyMath.h", "Sampling.h", "Imaging.h", "Geometry.h", "Materials.h",
     "Lights.h", "Scene.h", "Renderer.h", "SceneLoader.h", "QuadTree.h", "Metrics.h",
@@ -59,10 +69,43 @@ def build_oracle(force: bool = False) -> Path:
     return out
 
 
+def reference_root() -> Path:
+    """The reference checkout's root (may not exist on this machine)."""
+    env = os.environ.get("PGX_REFERENCE_DIR")
+    if env:
+        p = Path(env)
+        return p.parent if (p / "Renderer.h").exists() else p
+    return HERE.parent.parent / "reference"
+
+
+def reference_sources() -> Path:
+    return reference_root() / "PathGuidingDissertation"
+
+
+def scenes_dir() -> Path:
+    """The reference's scenes: the staged copy when present, else the checkout's."""
+    return REF_SCENES if REF_SCENES.is_dir() else reference_root() / "Scenes"
+
+
+def stage_scenes() -> None:
+    """Copy the complete reference scenes into oracle/_ref/scenes."""
+    src = reference_root() / "Scenes"
+    if not src.is_dir():
+        return
+    for name in COMPLETE_SCENES:
+        s, d = src / name, REF_SCENES / name
+        if not s.is_dir():
+            continue
+        d.mkdir(parents=True, exist_ok=True)
+        for f in s.iterdir():
+            if f.is_file() and (not (d / f.name).exists() or (d / f.name).stat().st_size != f.stat().st_size):
+                shutil.copy2(f, d / f.name)
+
+
 def stage_reference(reference_dir: str | None = None) -> bool:
     """Copy the reference headers into oracle/_ref/src (returns False when
     neither the checkout nor a staged copy exists)."""
-    ref = Path(reference_dir or os.environ.get("PGX_REFERENCE_DIR", DEFAULT_REFERENCE))
+    ref = Path(reference_dir) if reference_dir else reference_sources()
     if ref.is_dir():
         REF_SRC.mkdir(parents=True, exist_ok=True)
         for h in REF_HEADERS:
@@ -143,6 +186,7 @@ def _stale_platform(d: Path) -> bool:
 def build(force: bool = False) -> None:
     build_oracle(force or _stale_platform(BUILD))
     build_reference(force or _stale_platform(REF_OUT))
+    stage_scenes()
 
 
 if __name__ == "__main__":

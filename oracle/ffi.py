@@ -147,8 +147,9 @@ class Oracle:
 
 
 def reference_available() -> bool:
+    from . import build as _b  # noqa: PLC0415
     return (HERE / "_ref" / "liborcref.so").exists() or (HERE / "_ref" / "src" / "Renderer.h").exists() or \
-        Path(os.environ.get("PGX_REFERENCE_DIR", "/root/reference/PathGuidingDissertation")).is_dir()
+        (_b.reference_sources() / "Renderer.h").exists()
 
 
 class Reference:
@@ -189,6 +190,8 @@ class Reference:
         L.orcref_render_native.argtypes = [_P, _I32, _P, C.POINTER(_I32), C.POINTER(_I64)]
         L.orcref_clear.restype = None
         L.orcref_clear.argtypes = [_P]
+        L.orcref_camera_rays.restype = None
+        L.orcref_camera_rays.argtypes = [_P, _P, _P, _I64, _P, _P]
         L.orcref_pointbvh.restype = _I64
         L.orcref_pointbvh.argtypes = [_P, _I64, _P, _P]
         L.orcref_set_filter.restype = None
@@ -354,6 +357,15 @@ class RefScene:
 
     def clear(self):
         self.ref.lib.orcref_clear(self.h)
+
+    def camera_rays(self, px: np.ndarray, py: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+        """Camera::generateRay at film positions (px, py): origins, directions."""
+        px = np.ascontiguousarray(px, np.float32)
+        py = np.ascontiguousarray(py, np.float32)
+        o = np.zeros((len(px), 3), np.float32)
+        d = np.zeros((len(px), 3), np.float32)
+        self.ref.lib.orcref_camera_rays(self.h, _p(px), _p(py), len(px), _p(o), _p(d))
+        return o, d
 
 
 class RefWorld:

@@ -370,6 +370,17 @@ double orcref_render_native(void* h, int32_t frames, float* film_rgb, int32_t* s
 
 void orcref_clear(void* h) { static_cast<RefScene*>(h)->rt.clear(); }
 
+// Camera::generateRay (Scene.h:45-57) at n film positions (px, py): ray
+// origin to o3 (n x 3) and normalised direction to d3 (n x 3).
+void orcref_camera_rays(void* h, const float* px, const float* py, int64_t n, float* o3, float* d3) {
+    RefScene* rs = static_cast<RefScene*>(h);
+    for (int64_t i = 0; i < n; i++) {
+        Ray r = rs->scene->camera.generateRay(px[i], py[i]);
+        o3[3 * i] = r.o.x; o3[3 * i + 1] = r.o.y; o3[3 * i + 2] = r.o.z;
+        d3[3 * i] = r.dir.x; d3[3 * i + 1] = r.dir.y; d3[3 * i + 2] = r.dir.z;
+    }
+}
+
 // PointBVHNode::buildPointBVHNode (Renderer.h:189-211) on given records;
 // exports the tree in preorder (root first) and the records in node order.
 int64_t orcref_pointbvh(const pgx_path_vertex* recs, int64_t n, pgx_cache_node* nodes, pgx_path_vertex* out) {

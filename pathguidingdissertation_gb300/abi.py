@@ -51,6 +51,9 @@ BVH_NODE = np.dtype([("bmin", "<f4", 3), ("bmax", "<f4", 3), ("left_first", "<i4
 PATH_VERTEX = np.dtype([("position", "<f4", 3), ("normal", "<f4", 3), ("wi", "<f4", 3), ("Li", "<f4", 3)])
 CACHE_NODE = np.dtype([("bmin", "<f4", 3), ("bmax", "<f4", 3), ("left", "<i4"), ("right", "<i4"),
                        ("offset", "<i4"), ("used", "<i4")])
+GUIDE_REGION = np.dtype([("first", "<i4"), ("count", "<i4"), ("node", "<i4"), ("qroot", "<i4")])
+QUAD_NODE = np.dtype([("flux", "<f4", 4), ("child", "<i4", 4)])
+GUIDE_MAX_QUAD_NODES = 256
 
 assert VERTEX.itemsize == 32 and TRIANGLE.itemsize == 100 and MATERIAL.itemsize == 76
 assert RAY.itemsize == 32 and HIT.itemsize == 16 and BVH_NODE.itemsize == 32
@@ -143,6 +146,7 @@ SIGNATURES = {
     "pgx_cache_knn": (C.c_int, [_P, _P, _I64, _I32, _P, _P]),
     "pgx_guide_pdf": (C.c_int, [_P, _P, _P, _I64, _P]),
     "pgx_guide_sample": (C.c_int, [_P, _P, _P, _I64, _P, _P]),
+    "pgx_guide_export": (C.c_int, [_P, _P, C.POINTER(_I32), _P, C.POINTER(_I32)]),
     "pgx_mlp_init": (C.c_int, [_P, C.c_uint64, _P, _P]),
     "pgx_mlp_get_params": (C.c_int, [_P, _P]),
     "pgx_mlp_set_params": (C.c_int, [_P, _P]),

@@ -223,6 +223,16 @@ class Context:
         self.check(self.lib.pgx_guide_sample(self.h, ptr(p), ptr(u), len(p), ptr(dirs), ptr(pdf)))
         return dirs, pdf
 
+    def guide_export(self) -> tuple[np.ndarray, np.ndarray, bool]:
+        """The QuadTree guide's regions and quad nodes (pgx_guide_export)."""
+        nreg, pss = C.c_int32(), C.c_int32()
+        self.check(self.lib.pgx_guide_export(self.h, None, C.byref(nreg), None, C.byref(pss)))
+        regions = np.zeros(nreg.value, abi.GUIDE_REGION)
+        qnodes = np.zeros(nreg.value * abi.GUIDE_MAX_QUAD_NODES, abi.QUAD_NODE)
+        if nreg.value:
+            self.check(self.lib.pgx_guide_export(self.h, ptr(regions), C.byref(nreg), ptr(qnodes), C.byref(pss)))
+        return regions, qnodes, bool(pss.value)
+
     # ---- learned guide ----
     def mlp_init(self, seed: int = 1, bmin=None, bmax=None) -> None:
         lo = None if bmin is None else np.ascontiguousarray(bmin, np.float32)

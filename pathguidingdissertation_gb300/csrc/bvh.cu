@@ -763,7 +763,7 @@ int bvh_build_gpu(pgx_ctx* ctx) {
     BuildMisc hm{};
     for (int k = 0; k < 12; k++) hm.root_acc[k] = ((k % 6) < 3) ? INT_MAX : INT_MIN;
     PGX_CUDA_TRY(ctx, cudaMemcpyAsync(misc, &hm, sizeof(hm), cudaMemcpyHostToDevice, s));
-    k_root_reduce<<<std::min<unsigned>(blocks_for(n, 256), 4 * 152), 256, 0, s>>>(cent, tmin, tmax, n, misc);
+    k_root_reduce<<<std::min<unsigned>(blocks_for(n, 256), 4 * pgx_num_sms()), 256, 0, s>>>(cent, tmin, tmax, n, misc);
     k_root_init<<<1, 32, 0, s>>>(nodes, items, misc, n, small);
     PGX_CUDA_TRY(ctx, cudaGetLastError());
 
@@ -777,7 +777,7 @@ int bvh_build_gpu(pgx_ctx* ctx) {
         PGX_CUDA_TRY(ctx, cudaMemsetAsync(&misc->nitems_next, 0, sizeof(int), s));
         k_chunks<<<blocks_for(nitems, 128), 128, 0, s>>>(items, nitems, chunks, misc);
         k_bins_reset<<<blocks_for((int64_t)nitems * kBinInts, 256), 256, 0, s>>>(bins, nitems);
-        unsigned grid = (unsigned)std::min<int64_t>(n / kChunk + nitems, 8 * 152);
+        unsigned grid = (unsigned)std::min<int64_t>(n / kChunk + nitems, 8 * pgx_num_sms());
         k_bin<<<grid, kThreads, 0, s>>>(items, chunks, misc, idx, cent, tmin, tmax, bins);
         k_split<<<blocks_for(nitems, 64), 64, 0, s>>>(items, nitems, bins, nodes);
         k_partition<<<grid, kThreads, 0, s>>>(items, chunks, misc, idx, idx2, cent, tmin, tmax);

@@ -816,7 +816,7 @@ int cache_build_device(pgx_ctx* ctx, const pgx_path_vertex* d_records, int64_t n
     k_pos<<<blocks_for(n, 256), 256, 0, s>>>(cs->recs_in.as<pgx_path_vertex>(), n, pos, idx);
     int hacc[8] = {INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN, 0, 0};
     PGX_CUDA_TRY(ctx, cudaMemcpyAsync(acc, hacc, sizeof(hacc), cudaMemcpyHostToDevice, s));
-    k_root_bounds<<<std::min<unsigned>(blocks_for(n, 256), 4 * 152), 256, 0, s>>>(pos, n, acc);
+    k_root_bounds<<<std::min<unsigned>(blocks_for(n, 256), 4 * pgx_num_sms()), 256, 0, s>>>(pos, n, acc);
     k_root<<<1, 32, 0, s>>>(pos, n, misc, nodes, items, small, acc);
     PGX_CUDA_TRY(ctx, cudaMemsetAsync(hist, 0, sizeof(int) * 256 * item_cap, s));
     PGX_CUDA_TRY(ctx, cudaGetLastError());
@@ -829,7 +829,7 @@ int cache_build_device(pgx_ctx* ctx, const pgx_path_vertex* d_records, int64_t n
         PGX_CUDA_TRY(ctx, cudaMemsetAsync(&misc->nchunks, 0, sizeof(int), s));
         PGX_CUDA_TRY(ctx, cudaMemsetAsync(&misc->nitems_next, 0, sizeof(int), s));
         k_pchunks<<<blocks_for(nitems, 128), 128, 0, s>>>(items, nitems, nodes, chunks, misc);
-        unsigned grid = (unsigned)std::min<int64_t>(n / kChunk + nitems, 8 * 152);
+        unsigned grid = (unsigned)std::min<int64_t>(n / kChunk + nitems, 8 * pgx_num_sms());
         for (int b = 3; b >= 0; b--) {
             k_phist<<<grid, kThreads, 0, s>>>(items, chunks, misc, idx, pos, hist, b);
             k_pselect<<<blocks_for(nitems, 64), 64, 0, s>>>(items, nitems, hist, b);
@@ -1018,4 +1018,35 @@ extern "C" int pgx_guide_pdf(pgx_ctx* ctx, const float* positions, const float* 
 extern "C" int pgx_guide_sample(pgx_ctx* ctx, const float* positions, const float* u2, int64_t n, float* dirs,
                                 float* pdf) {
     return guide_query(ctx, positions, u2, n, 1, dirs, pdf);
+}
+
+extern "C" int pgx_guide_export(pgx_ctx* ctx, pgx_guide_region* regions, int32_t* nregions, pgx_quad_node* qnodes,
+                                int32_t* pss) {
+    if (!ctx || !nregions) return PGX_ERR_INVALID_ARG;
+    ctx->err.clear();
+    CacheState* cs = static_cast<CacheState*>(ctx->cache_state);
+    if (!cs || !cs->valid) return pgx_fail(ctx, PGX_ERR_STATE, "pgx_guide_export: no cache");
+    static_assert(sizeof(pgx_quad_node) == sizeof(QuadNode), "quad node layouts differ");
+    static_assert(PGX_QT_MAX_NODES == PGX_GUIDE_MAX_QUAD_NODES, "quad node capacity differs");
+    const int nreg = cs->n_records > 0 ? cs->n_regions : 0;
+    *nregions = nreg;
+    if (pss) *pss = cs->pss ? 1 : 0;
+    if (!regions || nreg == 0) return PGX_OK;
+    cudaStream_t s = ctx->stream;
+    std::vector<int2> rg((size_t)nreg);
+    std::vector<int> qr((size_t)nreg);
+    std::vector<int> nr((size_t)cs->n_nodes);
+    PGX_CUDA_TRY(ctx, cudaMemcpyAsync(rg.data(), cs->regions.p, sizeof(int2) * nreg, cudaMemcpyDeviceToHost, s));
+    PGX_CUDA_TRY(ctx, cudaMemcpyAsync(qr.data(), cs->qroot.p, sizeof(int) * nreg, cudaMemcpyDeviceToHost, s));
+    if (cs->n_nodes > 0)
+        PGX_CUDA_TRY(ctx, cudaMemcpyAsync(nr.data(), cs->node_region.p, sizeof(int) * nr.size(),
+                                          cudaMemcpyDeviceToHost, s));
+    if (qnodes)
+        PGX_CUDA_TRY(ctx, cudaMemcpyAsync(qnodes, cs->qnodes.p, sizeof(QuadNode) * PGX_QT_MAX_NODES * (size_t)nreg,
+                                          cudaMemcpyDeviceToHost, s));
+    PGX_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    for (int r = 0; r < nreg; r++) regions[r] = pgx_guide_region{rg[(size_t)r].x, rg[(size_t)r].y, -1, qr[(size_t)r]};
+    for (size_t i = 0; i < nr.size(); i++)
+        if (nr[i] >= 0 && nr[i] < nreg) regions[nr[i]].node = (int32_t)i;
+    return PGX_OK;
 }

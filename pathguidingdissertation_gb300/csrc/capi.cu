@@ -1,4 +1,5 @@
 // Context management, error reporting and the BVH entry points of the C ABI.
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <functional>
@@ -25,6 +26,20 @@ extern "C" const char* pgx_version(void) { return "pgx 0.1 (sm_103a)"; }
 extern "C" const char* pgx_last_error(const pgx_ctx* ctx) {
     if (!ctx) return g_create_error.c_str();
     return ctx->err.c_str();
+}
+
+int pgx_num_sms() {
+    static std::atomic<int> cache[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
+    if (dev >= 0 && dev < 64) {
+        int v = cache[dev].load(std::memory_order_relaxed);
+        if (v > 0) return v;
+    }
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 1;
+    if (dev >= 0 && dev < 64) cache[dev].store(v, std::memory_order_relaxed);
+    return v;
 }
 
 extern "C" int pgx_create(int32_t device, pgx_ctx** out) {

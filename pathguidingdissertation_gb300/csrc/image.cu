@@ -330,6 +330,7 @@ struct Decoder {
     // One scan (B.2.3): returns the position after its entropy-coded data.
     const uint8_t* scan(const uint8_t* q, int len, const uint8_t* seg_end) {
         if (!frame_seen) fail("scan before frame header");
+        if (len < 1) fail("invalid scan header");
         const int ns = q[0];
         if (ns < 1 || ns > 4 || len < 4 + 2 * ns) fail("invalid scan header");
         std::vector<Component*> sc;

@@ -191,6 +191,11 @@ int pgx_fail(pgx_ctx* ctx, int code, const char* fmt, ...);
         if (s_ != PGX_OK) return s_;  \
     } while (0)
 
+// Streaming multiprocessors of the current device (queried once per device
+// ordinal and cached); grids of persistent and grid-stride kernels are sized
+// in multiples of it.
+int pgx_num_sms();
+
 // Internal entry points implemented across the .cu files.
 int bvh_build_gpu(pgx_ctx* ctx);
 int bvh_import_ref(pgx_ctx* ctx, const pgx_bvh_node* nodes, int64_t nnodes, const int32_t* idx);

@@ -343,7 +343,7 @@ __global__ void __launch_bounds__(kThreads, kPersistentBlocksPerSM) k_shadow(Sce
 
 inline unsigned persistent_grid(int64_t n) {
     int64_t b = (n + kThreads - 1) / kThreads;
-    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(b, 152 * kPersistentBlocksPerSM));
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)pgx_num_sms() * kPersistentBlocksPerSM));
 }
 
 // Scene::calculateShadingData (Scene.h:152-176).
@@ -849,7 +849,10 @@ __global__ void __launch_bounds__(kThreads, kShadeBlocksPerSM) k_shade(SceneView
                         }
                         if (alive) {
                             if (rec_on) {
-                                r_store = !spec;
+                                // Primary-sample guides are built over the
+                                // cosine sampler's inverse: record only the
+                                // surfaces that sample through it.
+                                r_store = !spec && (MODE != PGX_MODE_GUIDED_PSS || pss_surface<KIND>(m));
                                 r_wi = wi;
                                 r_w = T;  // throughput after this vertex
                             }
@@ -1533,7 +1536,7 @@ void launch_shade_class(int c, unsigned grid, cudaStream_t s, const SceneView& s
 
 inline unsigned grid_for(int64_t n) {
     int64_t b = (n + kThreads - 1) / kThreads;
-    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 16));
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)pgx_num_sms() * 16));
 }
 
 RenderState* state_of(pgx_ctx* ctx) {
@@ -1699,7 +1702,7 @@ int enqueue_frame(pgx_ctx* ctx, RenderState* rs, const FrameParams& fp, cudaStre
         if (fp.mode == PGX_MODE_GUIDED_MLP && depth < fp.guide_depth) {
             const int64_t tiles = (n + mlp::kRows - 1) / mlp::kRows;
             const int64_t ctas = (tiles + kInferGroups - 1) / kInferGroups;
-            const unsigned ig = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ctas, 152 * 2));
+            const unsigned ig = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ctas, (int64_t)pgx_num_sms() * 2));
             k_guide_infer<<<ig, 128 * kInferGroups, kInferSmem, s>>>(sv, ps, depth, mv, mlp_status);
             launches++;
         }

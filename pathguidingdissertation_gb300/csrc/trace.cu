@@ -50,7 +50,7 @@ __global__ void __launch_bounds__(kTraceThreads, kPersistentBlocksPerSM)
 
 unsigned persistent_grid(int64_t n) {
     int64_t blocks = (n + kTraceThreads - 1) / kTraceThreads;
-    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(blocks, 152 * kPersistentBlocksPerSM));
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)pgx_num_sms() * kPersistentBlocksPerSM));
 }
 
 // Camera::generateRay with exact arithmetic.

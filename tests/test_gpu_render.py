@@ -86,27 +86,75 @@ def test_guided_li_vertices_vs_reference(ctx, reference):
     assert np.mean(np.abs(a[:n] - b[:n]) < 1e-3) > 0.97
 
 
-def test_render_statistical_vs_native_reference(ctx, reference):
-    """Per-16x16-tile means within 3 sigma of the reference's own render()."""
-    desc = scenes.cornell_box(seed=1, width=64, height=64)
+def _stat_scene(name):
+    if name == "cornell":
+        return scenes.cornell_box(seed=1, width=64, height=64)
+    # 128 x 128: 64 tiles of 16 x 16.  The sky is kept and the sun lobe is
+    # clipped away (texels at most 8): with the sun, the guided-Li estimator
+    # (BSDF sampling only) is so heavy-tailed at 64 spp that two renders of
+    # the reference itself with different seeds differ by 76 % per tile
+    # (median), and no tile test can tell anything.
+    d = scenes.interior(seed=3, target_tris=20000, n_objects=40, width=128, height=128, env_width=256,
+                        env_height=128)
+    d.env = np.minimum(d.env, np.float32(8.0))
+    return d
+
+
+@pytest.mark.parametrize("mode", [abi.MODE_PLAIN, abi.MODE_GUIDED_LI], ids=["plain", "guided_li"])
+@pytest.mark.parametrize("scene", ["cornell", "interior"])
+def test_render_statistical_vs_native_reference(ctx, reference, mode, scene):
+    """Per-16x16-tile means within 3 sigma of the reference's own
+    RayTracer::render (its tile scheduler, MTRandom samplers and film; the
+    plain or the GUIDED_PATH build), on the box (16 tiles) and on a small
+    interior with an environment map (64 tiles)."""
+    desc = _stat_scene(scene)
     frames = 64
     ctx.upload(desc)
     ctx.bvh_build()
     ctx.clear()
-    ctx.render(frames, mode=abi.MODE_GUIDED_LI, seed=3, max_depth=8)
+    ctx.render(frames, mode=mode, seed=3, max_depth=8)
     film, film2, spp = ctx.film(squares=True)
-    ref = type(reference)(variant="fast")
+    ref = type(reference)(variant="plain_fast" if mode == abi.MODE_PLAIN else "fast")
     rs = ref.scene(desc, threads=8)
     rfilm, rspp, _, _ = rs.render_native(frames)
+    rs.close()
     assert rspp == frames and spp == frames
     t = 16
-    H, W = 64, 64
+    W, H = desc.camera["width"], desc.camera["height"]
     g = film.reshape(H // t, t, W // t, t, 3).sum(axis=(1, 3)) / (spp * t * t)
     g2 = film2.reshape(H // t, t, W // t, t, 3).sum(axis=(1, 3)) / (spp * t * t)
     r = rfilm.reshape(H // t, t, W // t, t, 3).sum(axis=(1, 3)) / (rspp * t * t)
     var = np.maximum(g2 - g * g, 1e-12) / (spp * t * t)
     z = np.abs(g - r) / np.sqrt(2 * var)
-    assert np.mean(z < 3.0) > 0.95, z.max()
+    assert (H // t) * (W // t) >= (16 if scene == "cornell" else 64)
+    assert np.mean(z < 3.0) > 0.95, (np.mean(z < 3.0), z.max())
+
+
+def test_relmse_vs_converged_matches_reference(ctx, reference):
+    """The plain configuration (the 36-triangle box, 256 x 256, 16 spp, depth
+    8): the relative MSE of pgx's render against a 65,536-spp converged image
+    is within 5 % of the relative MSE of the reference's own
+    RayTracer::render (plain build, its own samplers) at the same spp."""
+    from pathguidingdissertation_gb300 import metrics
+    desc = scenes.cornell_box(seed=1, width=256, height=256)
+    ctx.upload(desc)
+    ctx.bvh_build()
+    ctx.clear()
+    ctx.render(65536, mode=abi.MODE_PLAIN, seed=1000, max_depth=8)
+    conv, _, n = ctx.film()
+    conv = conv / n
+    ctx.clear()
+    ctx.render(16, mode=abi.MODE_PLAIN, seed=7, max_depth=8)
+    mine, _, n = ctx.film()
+    mine = mine / n
+    ref = type(reference)(variant="plain_fast")
+    rs = ref.scene(desc, threads=8)
+    rfilm, rspp, _, _ = rs.render_native(16)
+    rs.close()
+    theirs = rfilm / rspp
+    a = metrics.relmse(mine, conv)
+    b = metrics.relmse(theirs, conv)
+    assert abs(a / b - 1.0) < 0.05, (a, b)
 
 
 def test_render_api_semantics(ctx):

@@ -1,0 +1,127 @@
+"""The QuadTree guide's CPU restatement (oracle/guide_oracle.py) checked
+against its own mathematics, CPU only: the tree's density integrates to 1
+over the unit square, refinement follows the 1 % flux rule and the caps,
+sampling follows the density, and the cosine sampler's inverse round-trips
+through the reference's sampler formula (Materials.h:163-171)."""
+from __future__ import annotations
+
+import numpy as np
+
+from oracle import guide_oracle as go
+
+PV = np.dtype([("position", "<f4", 3), ("normal", "<f4", 3), ("wi", "<f4", 3), ("Li", "<f4", 3)])
+
+
+def lobes_records(n, seed, lobes=6, spread=0.05, bright=None):
+    rng = np.random.default_rng(seed)
+    r = np.zeros(n, PV)
+    r["position"] = rng.uniform(-1, 1, (n, 3))
+    r["normal"] = rng.normal(size=(n, 3))
+    centres = rng.normal(size=(lobes, 3))
+    centres /= np.linalg.norm(centres, axis=1, keepdims=True)
+    k = rng.integers(0, lobes, n)
+    d = centres[k] + spread * rng.normal(size=(n, 3))
+    r["wi"] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    r["Li"] = np.exp(rng.normal(0, 1, (n, 1))) * np.ones((1, 3)) if bright is None else bright
+    return r
+
+
+def test_luminance_filters_invalid():
+    li = np.array([[1, 1, 1], [0, 0, 0], [-1, 0, 0], [np.nan, 0, 0], [np.inf, 0, 0]], np.float32)
+    w = go.luminance(li)
+    assert w[0] > 0 and np.all(w[1:] == 0)
+
+
+def _leaves(tree):
+    """(u0, v0, size, probability mass) of every leaf cell of a tree."""
+    out = []
+    stack = [(0, 0.0, 0.0, 1.0, 1.0)]
+    while stack:
+        node, u0, v0, size, mass = stack.pop()
+        flux, child = tree[node]
+        total = sum(flux)
+        for c in range(4):
+            cu, cv, h = u0 + 0.5 * size * (c & 1), v0 + 0.5 * size * (c >> 1), 0.5 * size
+            m = mass * flux[c] / total
+            if child[c] >= 0:
+                stack.append((child[c], cu, cv, h, m))
+            else:
+                out.append((cu, cv, h, m))
+    return out
+
+
+def test_tree_density_integrates_to_one():
+    """The leaves' masses sum to 1 and quad_pdf at each leaf's centre is its
+    mass over its area."""
+    tree = go.build_quadtree(lobes_records(900, 1))
+    leaves = _leaves(tree)
+    assert abs(sum(m for *_, m in leaves) - 1.0) < 1e-12
+    for u0, v0, h, m in leaves:
+        assert abs(go.quad_pdf(tree, u0 + 0.5 * h, v0 + 0.5 * h) * h * h - m) <= 1e-12 + 1e-9 * m
+
+
+def test_refinement_rule_and_caps():
+    recs = lobes_records(1000, 2, lobes=40, spread=1e-6)
+    tree = go.build_quadtree(recs)
+    assert len(tree) == go.MAX_NODES  # forty tight lobes exhaust the node budget
+    w = np.minimum(go.luminance(recs["Li"]), go.CLAMP_MEDIAN * go.median_bisection(go.luminance(recs["Li"])))
+    total = float(w.astype(np.float64).sum())
+    depth = {0: 0}
+    for i, (flux, child) in enumerate(tree):
+        for c in range(4):
+            if child[c] >= 0:
+                assert flux[c] > 0.01 * total
+                depth[child[c]] = depth[i] + 1
+    assert max(depth.values()) <= go.MAX_DEPTH - 1
+    single = go.build_quadtree(lobes_records(500, 3, lobes=1, spread=0.0))
+    assert len(single) == go.MAX_DEPTH  # one direction: a chain down to the depth cap
+
+
+def test_sampling_follows_density():
+    tree = go.build_quadtree(lobes_records(800, 4, lobes=3, spread=0.2))
+    rng = np.random.default_rng(0)
+    n = 40000
+    uv = np.array([go.quad_sample(tree, *rng.random(2)) for _ in range(n)])
+    bins = 8
+    h, _, _ = np.histogram2d(uv[:, 0], uv[:, 1], bins=bins, range=[[0, 1], [0, 1]])
+    expect = np.zeros((bins, bins))
+    for u0, v0, sz, m in _leaves(tree):
+        # a leaf larger than a bin spreads its mass evenly over the bins it covers
+        k = max(1, int(round(sz * bins)))
+        i0, j0 = int(u0 * bins + 1e-9), int(v0 * bins + 1e-9)
+        expect[i0:i0 + k, j0:j0 + k] += m / (k * k)
+    expect *= n
+    m = expect > 20
+    chi2 = float((((h - expect) ** 2) / np.maximum(expect, 1e-9))[m].sum())
+    assert chi2 < 3 * m.sum(), chi2
+    for r in rng.random((200, 2)):
+        u, v = go.quad_sample(tree, *r)
+        assert go.quad_pdf(tree, u, v) > 0
+
+
+def test_pss_uv_inverts_the_cosine_sampler():
+    """u = cos^2 theta, v = phi / 2 pi inverts the sampler theta =
+    acos(sqrt(u)), phi = 2 pi v of DiffuseBSDF::sample (Materials.h:147-160)."""
+    rng = np.random.default_rng(1)
+    n = rng.normal(size=(500, 3)).astype(np.float32)
+    uv = rng.uniform(0.02, 0.98, (500, 2))
+    fu, fv, fw = go._frame(n)
+    th = np.arccos(np.sqrt(uv[:, 0]))
+    ph = 2 * np.pi * uv[:, 1]
+    loc = np.stack([np.cos(ph) * np.sin(th), np.sin(ph) * np.sin(th), np.cos(th)], 1)
+    wi = (fu * loc[:, :1] + fv * loc[:, 1:2] + fw * loc[:, 2:]).astype(np.float32)
+    u, v, ok = go.pss_uv(n, wi)
+    assert ok.all()
+    assert np.abs(u - uv[:, 0]).max() < 1e-4 and np.abs(v - uv[:, 1]).max() < 1e-4
+
+
+def test_regions_from_a_median_split_tree():
+    nodes = np.zeros(7, [("bmin", "<f4", 3), ("bmax", "<f4", 3), ("left", "<i4"), ("right", "<i4"),
+                         ("offset", "<i4"), ("used", "<i4")])
+    # root 3000 -> 1500 + 1500 -> (750, 750) + (750, 750)
+    spec = [(1, 2, 0, 3000), (3, 4, 0, 1500), (5, 6, 1500, 1500), (-1, -1, 0, 750), (-1, -1, 750, 750),
+            (-1, -1, 1500, 750), (-1, -1, 2250, 750)]
+    for i, (l, r, o, u) in enumerate(spec):
+        nodes[i]["left"], nodes[i]["right"], nodes[i]["offset"], nodes[i]["used"] = l, r, o, u
+    assert go.regions_from_bvh(nodes, 3000) == [(0, 750, 3), (750, 750, 4), (1500, 750, 5), (2250, 750, 6)]
+    assert go.regions_from_bvh(nodes[:1], 800) == [(0, 800, 0)]

@@ -5,7 +5,6 @@ headless; plus the writer's round trip.  CPU only."""
 from __future__ import annotations
 
 import json
-import os
 from pathlib import Path
 
 import numpy as np
@@ -14,7 +13,10 @@ import pytest
 from pathguidingdissertation_gb300 import loader, scenes
 from pathguidingdissertation_gb300.abi import BSDF_CONDUCTOR, BSDF_DIFFUSE, BSDF_GLASS, BSDF_PLASTIC
 
-REF_SCENES = Path(os.environ.get("PGX_REFERENCE_SCENES", "/root/reference/Scenes"))
+from oracle import build as _oracle_build
+
+# The checkout's scene folder (every scene, for the image-format tests).
+REF_SCENES = _oracle_build.reference_root() / "Scenes"
 # The reference scenes whose meshes are all present and whose textures are
 # PNG or HDR (the others lack mesh files, on which loadScene exits).
 COMPLETE = ["cornell-box", "veach-mis", "veach-bidir", "MaterialsScene"]
