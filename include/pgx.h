@@ -572,6 +572,37 @@ const char* pgx_batch_last_error(pgx_batch* batch);
 int pgx_image_decode_jpeg(const uint8_t* data, int64_t size, int32_t* width, int32_t* height, int32_t* channels,
                           uint8_t* out, int64_t out_size, char* msg, int32_t msg_size);
 
+/* ---- scene files (the reference's format) ------------------------------------
+ * `loadScene(dir)` (SceneLoader.h:222-269) on the host: `dir`/scene.json
+ * (GEMScene::load, GEMLoader.h:853-882), the .gem meshes it names
+ * (GEMModelLoader::load, GEMLoader.h:430-457) and their textures
+ * (Texture::load, Imaging.h:44-79: PNG, JPEG, BMP, TGA; Radiance HDR for the
+ * environment map), assembled with loadInstance's rules
+ * (SceneLoader.h:104-220): one material per instance, float32 world
+ * transforms, zero-area triangles dropped, distinct texture files shared.  A
+ * texture that cannot be read becomes 1x1 white, as in the reference.
+ * pgx_scene_read returns the upload arrays (owned by the result; release
+ * with pgx_scene_data_free); on failure (missing scene.json or mesh, a
+ * malformed file) it returns PGX_ERR_INVALID_ARG and a message in msg.  The
+ * reference prints and continues or exits instead. */
+typedef struct pgx_scene_data {
+    pgx_triangle* triangles;
+    int64_t ntris;
+    pgx_material* materials;
+    int32_t nmats;
+    pgx_texture* textures; /* albedo textures, first use first */
+    int32_t ntextures;
+    int32_t has_env;
+    pgx_texture env;       /* the environment map when has_env */
+    pgx_camera camera;
+    void* internal;        /* owner of the arrays */
+} pgx_scene_data;
+int pgx_scene_read(const char* dir, pgx_scene_data** out, char* msg, int32_t msg_size);
+void pgx_scene_data_free(pgx_scene_data* data);
+/* pgx_scene_read followed by pgx_scene_upload: the whole of `loadScene`
+ * (without the BVH build, which is pgx_bvh_build, `Scene::build`). */
+int pgx_scene_load(pgx_ctx* ctx, const char* dir);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,11 +1,11 @@
 // pgx.hpp — C++ façade over the C ABI in pgx.h, keeping the reference's class
 // names and call pattern (PathGuidingDissertation/main.cpp:147-199):
 //
-//   pgx::Scene scene;                  // Scene (Scene.h:76-176)
-//   scene.init(triangles, materials, envmap, camera);
-//   scene.build();                     // Scene::build: BVH on the GPU, lights
+//   pgx::Scene* scene = pgx::loadScene("Scenes/cornell-box");  // SceneLoader.h:222
+//   // or: pgx::Scene scene; scene.init(triangles, materials, envmap, camera);
+//   //     scene.build();             // Scene::build: BVH on the GPU, lights
 //   pgx::RayTracer rt;                 // RayTracer (Renderer.h:236-752)
-//   rt.init(&scene);
+//   rt.init(scene);
 //   while (rt.getSPP() < spp) rt.render();
 //   rt.saveHDR("GI.hdr");
 //
@@ -69,6 +69,22 @@ class Scene {
                                            (int32_t)textures.size(), envmap, &camera));
     }
 
+    // Reads a scene directory in the reference's format (scene.json, .gem
+    // meshes, textures; SceneLoader.h:104-269) and uploads it (Scene::init).
+    void load(const std::string& dir) {
+        pgx_scene_data* d = nullptr;
+        char msg[512];
+        int rc = pgx_scene_read(dir.c_str(), &d, msg, (int32_t)sizeof(msg));
+        if (rc != PGX_OK) throw Error(rc, std::string("pgx: loadScene: ") + msg);
+        triangles_.assign(d->triangles, d->triangles + d->ntris);
+        camera_ = d->camera;
+        rc = pgx_scene_upload(ctx_.get(), d->triangles, d->ntris, d->materials, d->nmats,
+                              d->ntextures ? d->textures : nullptr, d->ntextures, d->has_env ? &d->env : nullptr,
+                              &d->camera);
+        pgx_scene_data_free(d);
+        check(ctx_.get(), rc);
+    }
+
     // Scene::build (Scene.h:84-101): binned-SAH BVH, built on the GPU.
     void build() { check(ctx_.get(), pgx_bvh_build(ctx_.get())); }
 
@@ -107,6 +123,20 @@ class Scene {
     std::vector<pgx_triangle> triangles_;
     pgx_camera camera_{};
 };
+
+// `loadScene(dir)` (SceneLoader.h:222-269): the scene read, uploaded and
+// built (BVH and light list), ready for RayTracer::init.
+inline Scene* loadScene(const std::string& dir, int device = 0) {
+    Scene* scene = new Scene(device);
+    try {
+        scene->load(dir);
+        scene->build();
+    } catch (...) {
+        delete scene;
+        throw;
+    }
+    return scene;
+}
 
 // Reference `RayTracer`: progressive film, one sample per pixel per render().
 class RayTracer {

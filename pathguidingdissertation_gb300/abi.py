@@ -69,6 +69,13 @@ class Camera(C.Structure):
                 ("fov_degrees", C.c_float), ("width", C.c_int32), ("height", C.c_int32), ("flip_x", C.c_int32)]
 
 
+class SceneData(C.Structure):
+    """pgx_scene_data (include/pgx.h)."""
+    _fields_ = [("triangles", C.c_void_p), ("ntris", C.c_int64), ("materials", C.c_void_p), ("nmats", C.c_int32),
+                ("textures", C.c_void_p), ("ntextures", C.c_int32), ("has_env", C.c_int32), ("env", Texture),
+                ("camera", Camera), ("internal", C.c_void_p)]
+
+
 class BvhStats(C.Structure):
     _fields_ = [("nodes", C.c_int64), ("leaves", C.c_int64), ("max_depth", C.c_int32),
                 ("max_leaf_size", C.c_int32), ("sah_cost", C.c_double), ("build_ms", C.c_double)]
@@ -167,6 +174,9 @@ SIGNATURES = {
     "pgx_batch_get_stats": (C.c_int, [_P, C.POINTER(BatchStats)]),
     "pgx_batch_last_error": (C.c_char_p, [_P]),
     "pgx_image_decode_jpeg": (C.c_int, [_P, _I64, _P, _P, _P, _P, _I64, _P, _I32]),
+    "pgx_scene_read": (C.c_int, [C.c_char_p, C.POINTER(C.POINTER(SceneData)), _P, _I32]),
+    "pgx_scene_data_free": (None, [C.POINTER(SceneData)]),
+    "pgx_scene_load": (C.c_int, [_P, C.c_char_p]),
 }
 
 _lib: C.CDLL | None = None

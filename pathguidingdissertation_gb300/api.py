@@ -9,6 +9,7 @@ reference's names and semantics (Scene.h:76-176, Renderer.h:236-752):
 from __future__ import annotations
 
 import ctypes as C
+from pathlib import Path
 
 import numpy as np
 
@@ -67,6 +68,14 @@ class Context:
                                              C.byref(env) if env is not None else None, C.byref(cam)))
         self.scene = scene
         del env_keep, texs
+
+    def load_scene(self, scene_dir: str) -> SceneDesc:
+        """pgx_scene_load: the reference's scene directory read by the native
+        loader and uploaded; returns the same arrays as a SceneDesc."""
+        desc = read_scene(scene_dir)
+        self.check(self.lib.pgx_scene_load(self.h, str(scene_dir).encode()))
+        self.scene = desc
+        return desc
 
     def bvh_build(self) -> None:
         self.check(self.lib.pgx_bvh_build(self.h))
@@ -369,6 +378,39 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def read_scene(scene_dir: str) -> SceneDesc:
+    """`loadScene` by the native reader (pgx_scene_read), copied into a
+    SceneDesc.  Raises PgxError for a missing or malformed scene."""
+    lib = abi.load()
+    out = C.POINTER(abi.SceneData)()
+    msg = C.create_string_buffer(512)
+    rc = lib.pgx_scene_read(str(scene_dir).encode(), C.byref(out), msg, 512)
+    if rc != abi.PGX_OK:
+        raise PgxError(rc, msg.value.decode(errors="replace"))
+    try:
+        d = out.contents
+
+        def arr(p, n, dtype):
+            if n == 0:
+                return np.zeros(0, dtype)
+            buf = (C.c_uint8 * (n * dtype.itemsize)).from_address(p)
+            return np.frombuffer(buf, dtype, n).copy()
+
+        def tex(t):
+            return arr(t.rgb, t.width * t.height * 3, np.dtype(np.float32)).reshape(t.height, t.width, 3)
+
+        tris = arr(d.triangles, d.ntris, abi.TRIANGLE)
+        mats = arr(d.materials, d.nmats, abi.MATERIAL)
+        texs = [tex(abi.Texture.from_address(d.textures + i * C.sizeof(abi.Texture))) for i in range(d.ntextures)]
+        env = tex(d.env) if d.has_env else None
+        c = d.camera
+        cam = dict(from_=tuple(c.from_), to=tuple(c.to), up=tuple(c.up), fov=c.fov_degrees, width=c.width,
+                   height=c.height, flip_x=c.flip_x)
+    finally:
+        lib.pgx_scene_data_free(out)
+    return SceneDesc(tris, mats, cam, env=env, textures=texs, name=Path(str(scene_dir).rstrip("/")).name)
 
 
 def camera_struct(c: dict) -> abi.Camera:

@@ -9,10 +9,10 @@ import pytest
 ROOT = Path(__file__).resolve().parents[1]
 
 
-def _build_example(tmp_path, pgx_lib):
-    exe = tmp_path / "render_box"
+def _build_example(tmp_path, pgx_lib, name="render_box"):
+    exe = tmp_path / name
     lib_dir = ROOT / "pathguidingdissertation_gb300"
-    cmd = ["g++", "-std=c++17", "-O2", "-I", str(ROOT / "include"), str(ROOT / "tests" / "cpp" / "render_box.cpp"),
+    cmd = ["g++", "-std=c++17", "-O2", "-I", str(ROOT / "include"), str(ROOT / "tests" / "cpp" / f"{name}.cpp"),
            "-L", str(lib_dir), "-lpgx", f"-Wl,-rpath,{lib_dir}", "-o", str(exe)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
@@ -21,6 +21,7 @@ def _build_example(tmp_path, pgx_lib):
 
 def test_cpp_facade_compiles(tmp_path, pgx_lib):
     assert _build_example(tmp_path, pgx_lib).exists()
+    assert _build_example(tmp_path, pgx_lib, "load_scene").exists()
 
 
 @pytest.mark.gpu
@@ -31,3 +32,36 @@ def test_cpp_facade_renders(tmp_path, pgx_lib):
     assert r.returncode == 0, r.stdout + r.stderr
     assert "spp=8" in r.stdout and "expected error" in r.stdout
     assert out.stat().st_size > 64 * 64 * 4
+
+
+@pytest.mark.gpu
+def test_cpp_load_scene_renders_reference_scene(tmp_path, pgx_lib):
+    """pgx::loadScene on the reference's cornell-box directory (the C++
+    host path of SceneLoader.h:222-269), rendered by pgx::RayTracer; the
+    image equals the one rendered through the Python API from the same
+    native reader (same seeds and samples)."""
+    import numpy as np
+
+    from oracle import build as ob
+    from pathguidingdissertation_gb300 import abi
+    from pathguidingdissertation_gb300.api import Context
+    scene = ob.scenes_dir() / "cornell-box"
+    if not scene.is_dir():
+        pytest.skip("reference scenes not staged")
+    exe = _build_example(tmp_path, pgx_lib, "load_scene")
+    out = tmp_path / "cb.hdr"
+    r = subprocess.run([str(exe), str(scene), "8", str(out)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "expected error" in r.stdout
+    fields = dict(kv.split("=") for kv in r.stdout.splitlines()[0].split())
+    with Context(0) as ctx:
+        desc = ctx.load_scene(str(scene))
+        ctx.bvh_build()
+        ctx.clear()
+        ctx.render(8, mode=abi.MODE_PLAIN, seed=1, max_depth=8)
+        film, _, spp = ctx.film()
+    assert int(fields["triangles"]) == len(desc.triangles)
+    assert (int(fields["width"]), int(fields["height"])) == (desc.camera["width"], desc.camera["height"])
+    assert int(fields["spp"]) == spp == 8
+    mean = float(film.astype(np.float64).mean() / spp)
+    assert mean > 0 and abs(float(fields["mean"]) - mean) <= 1e-5 * mean + 1e-7

@@ -263,3 +263,70 @@ def test_property_parsing_rules():
     assert loader._as_float("0.1", 0.0) == float(np.float32(0.1))
     assert loader._as_int("0.5", 3) == 0 and loader._as_int("x", 3) == 3 and loader._as_int("12.000000", 0) == 12
     assert loader._prop_str(1280.0) == "1280.000000"
+
+
+@pytest.mark.parametrize("name", COMPLETE + COMPLETE_JPEG)
+def test_native_reader_matches_python_loader(pgx_lib, name):
+    """pgx_scene_read (C++, csrc/scene_load.cu) gives byte-identical upload
+    arrays to the Python reader on every complete reference scene (both
+    decode JPEG with the same pgx_image_decode_jpeg)."""
+    from pathguidingdissertation_gb300.api import read_scene
+    d = _oracle_build.scenes_dir() / name
+    if not d.is_dir():
+        pytest.skip("reference scenes not available")
+    a = loader.load_scene(d)
+    b = read_scene(str(d))
+    assert a.triangles.tobytes() == b.triangles.tobytes()
+    assert a.materials.tobytes() == b.materials.tobytes()
+    assert len(a.textures) == len(b.textures)
+    for x, y in zip(a.textures, b.textures):
+        assert x.shape == y.shape and x.tobytes() == y.tobytes()
+    assert (a.env is None) == (b.env is None)
+    if a.env is not None:
+        assert a.env.tobytes() == b.env.tobytes()
+    for k in ("from_", "to", "up"):
+        assert np.float32(a.camera[k]).tobytes() == np.float32(b.camera[k]).tobytes()
+    assert np.float32(a.camera["fov"]) == np.float32(b.camera["fov"])
+    assert (a.camera["width"], a.camera["height"], a.camera["flip_x"]) == \
+        (b.camera["width"], b.camera["height"], b.camera["flip_x"])
+
+
+def test_native_reader_corner_rules(pgx_lib, tmp_path):
+    """The loader's corner rules through the native reader: sorted keys,
+    last duplicate wins, stof/stoi prefixes and defaults, vector words,
+    unknown BSDFs skipped, dielectric below roughness 1e-3 becoming glass,
+    a coating dropping the emission, unreadable textures as white, and the
+    same arrays as the Python reader."""
+    from pathguidingdissertation_gb300.api import read_scene
+    d = tmp_path / "s"
+    d.mkdir()
+    verts = np.zeros((4, 11), np.float32)
+    verts[:, :3] = [[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0]]
+    verts[:, 3:6] = [0, 0, 1]
+    verts[:, 9:] = [[0, 0], [1, 0], [1, 1], [0, 1]]
+    loader.write_gem(d / "quad.gem", [(verts, np.array([0, 1, 2, 0, 2, 3, 0, 0, 0], np.uint32))])
+    loader._write_png(d / "a.png", np.array([[[10, 200, 30], [0, 0, 255]]], np.uint8))
+    (d / "bad.png").write_bytes(b"not a png")
+    js = """{"width": "64x", "height": "  48", "fov": "55.5deg", "from": "0 0  3", "to": "0 0", "up": "0 1 0 9",
+      "flipX": true, "width": "32",
+      "instances": [
+        {"filename": "quad.gem", "bsdf": "diffuse", "reflectance": "a.png",
+         "world": [2, 0, 0, 1, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1]},
+        {"filename": "quad.gem", "bsdf": "dielectric", "roughness": "0.0005", "intIOR": 1.7,
+         "reflectance": "bad.png"},
+        {"filename": "quad.gem", "bsdf": "velvet"},
+        {"filename": "quad.gem", "bsdf": "conductor", "eta": "0.2 0.9", "k": "3 x 1", "roughness": "",
+         "emission": "5 5 5", "coatingThickness": "2", "reflectance": "a.png"}
+      ]}"""
+    (d / "scene.json").write_text(js)
+    a = loader.load_scene(d)
+    b = read_scene(str(d))
+    assert a.triangles.tobytes() == b.triangles.tobytes()
+    assert a.materials.tobytes() == b.materials.tobytes()
+    assert [t.tobytes() for t in a.textures] == [t.tobytes() for t in b.textures]
+    assert b.camera["width"] == 32 and b.camera["height"] == 48 and b.camera["flip_x"] == 1
+    assert len(b.materials) == 3 and b.materials["kind"][1] == BSDF_GLASS
+    assert b.materials["layered"][2] == 1 and np.all(b.materials["emission"][2] == 0)
+    assert b.textures[1].shape == (1, 1, 3) and np.all(b.textures[1] == 1)
+    with pytest.raises(Exception):
+        read_scene(str(tmp_path / "missing"))
