@@ -178,6 +178,47 @@ def cpu_baseline_reference(desc, frames_budget_s: float = 12.0) -> dict | None:
                       f"{rays} rays in {secs:.2f} s"}
 
 
+def prepare_mode(ctx, mode: int, depth: int) -> None:
+    """Untimed set-up of a guided estimator: the radiance cache from a 1-spp
+    guided-Li pass (QuadTree), or the learned guide trained online on 16
+    frames."""
+    from pathguidingdissertation_gb300 import abi
+    ctx.clear()  # the guided-Li pass records its vertices only while SPP < 16 (Renderer.h:720-746)
+    if mode == abi.MODE_GUIDED_QUADTREE:
+        ctx.render(1, mode=abi.MODE_GUIDED_LI, seed=99, max_depth=depth, record_paths=True)
+    if mode == abi.MODE_GUIDED_MLP:
+        ctx.mlp_init(3)
+        ctx.mlp_configure(lr=5e-3, decay=0.998, batch=1 << 18, steps=4)
+        ctx.render(16, mode=mode, seed=99, max_depth=depth, train_guide=True)
+
+
+def side_mode_rate(ctx, mode: int, depth: int, spp: int, steps: int, seed: int, flush, ranks) -> dict:
+    """Mrays/s and Mpaths/s of one more estimator on the bench's workload."""
+    import torch
+    prepare_mode(ctx, mode, depth)
+    ctx.clear()
+    ctx.render(spp, mode=mode, seed=seed, max_depth=depth, timing=True)  # warm-up
+    torch.cuda.synchronize()
+    ranks.barrier()
+    rays = paths = 0
+    ms = 0.0
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ctx.render(spp, mode=mode, seed=seed, max_depth=depth, timing=True)
+        st = ctx.render_stats()
+        rays += st.extension_rays + st.shadow_rays
+        paths += st.paths
+        ms += st.ms_total
+    torch.cuda.synchronize()
+    ranks.barrier()
+    ms_max = ranks.reduce(ms, "max")
+    return {"mrays_per_s": ranks.reduce(rays, "sum") / (ms_max * 1e-3) / 1e6,
+            "mpaths_per_s": ranks.reduce(paths, "sum") / (ms_max * 1e-3) / 1e6,
+            "ms_per_step": ms_max / steps, "steps": steps, "max_depth": depth,
+            "rays_per_path": rays / max(paths, 1)}
+
+
 def run_pgx(args) -> dict:
     import torch
 
@@ -201,14 +242,7 @@ def run_pgx(args) -> dict:
     ctx = Context(ranks.local)
     ctx.upload(desc)
     ctx.bvh_build()
-    if mode == abi.MODE_GUIDED_QUADTREE:
-        # Radiance cache from a 1-spp guided-Li pass (the reference's records).
-        ctx.render(1, mode=abi.MODE_GUIDED_LI, seed=99, max_depth=depth, record_paths=True)
-    if mode == abi.MODE_GUIDED_MLP:
-        # The learned guide, trained online on 16 frames (not timed).
-        ctx.mlp_init(3)
-        ctx.mlp_configure(lr=5e-3, decay=0.998, batch=1 << 18, steps=4)
-        ctx.render(16, mode=mode, seed=99, max_depth=depth, train_guide=True)
+    prepare_mode(ctx, mode, depth)
     ctx.clear()
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     spp = args.spp_per_step
@@ -249,6 +283,20 @@ def run_pgx(args) -> dict:
     rays_all = ranks.reduce(rays, "sum")
     paths_all = ranks.reduce(paths, "sum")
     value = rays_all / (ms_max * 1e-3) / 1e6
+
+    # The other half of the metric: throughput of the guided estimators on the
+    # same workload (each after its own untimed set-up: the radiance cache from
+    # a 1-spp guided-Li pass, or 16 frames of online training), and plain path
+    # tracing at the reference arm's fixed depth 8 for an equal-depth anchor.
+    # Same L2 flush and device timing as the steps above, fewer steps.
+    side = {}
+    if not args.no_side_modes:
+        for name, m, d in (("guided_quadtree", abi.MODE_GUIDED_QUADTREE, depth),
+                           ("guided_mlp", abi.MODE_GUIDED_MLP, depth), ("plain_depth8", abi.MODE_PLAIN, 8)):
+            if m == mode and d == depth:
+                continue
+            side[name] = side_mode_rate(ctx, m, d, spp, max(1, min(args.steps, 4)), seed, flush, ranks)
+        ctx.clear()
 
     # End to end through the C ABI: camera from host, render, film to pinned host memory.
     H, W = desc.camera["height"], desc.camera["width"]
@@ -337,6 +385,7 @@ def run_pgx(args) -> dict:
         "gpu_launches": launches,
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": C.sizeof(abi.Camera),
                 "d2h_bytes_per_step": H * W * 3 * 4},
+        "modes": side,
         "roofline": roofline,
         "roofline_shade": roofline_shade,
         "cpu_baseline": cpu,
@@ -353,10 +402,8 @@ def relmse(img: np.ndarray, ref: np.ndarray, eps: float = 1e-2) -> float:
 def relmse_robust(img: np.ndarray, ref: np.ndarray, eps: float = 1e-2, drop: float = 1e-3) -> float:
     """relMSE with the largest 0.1 % of per-pixel errors left out (a few
     fireflies from the sun lobe otherwise decide the mean)."""
-    d = img.astype(np.float64) - ref
-    e = np.sort((d * d / (ref * ref + eps)).mean(axis=2).ravel())
-    k = max(1, int(len(e) * drop))
-    return float(e[:-k].mean())
+    from pathguidingdissertation_gb300 import metrics
+    return metrics.relmse_robust(img, ref, eps, drop)
 
 
 def rrmse_reference_metric(img: np.ndarray, ref: np.ndarray) -> float:
@@ -413,6 +460,7 @@ def run_relmse_study(args) -> dict:
     plain_ms = render_ms(args.plain_spp, abi.MODE_PLAIN, 7)
     plain_img = image()
     plain_err = metric(plain_img, ref)
+    other = relmse if metric is relmse_robust else relmse_robust
 
     ctx.clear()
     train_ms = 0.0
@@ -456,8 +504,9 @@ def run_relmse_study(args) -> dict:
         guided_ms += render_ms(chunk, mode, 17 + total, guide_fraction=args.guide_fraction,
                                guide_depth=args.guide_depth)
         total += chunk
-        err = metric(image(), ref)
-        curve.append((total, train_ms + guided_ms, err))
+        img = image()
+        err = metric(img, ref)
+        curve.append((total, train_ms + guided_ms, err, other(img, ref)))
         if reached_ms is None and err <= plain_err:
             reached_ms = train_ms + guided_ms
         if train_ms + guided_ms >= 2.0 * plain_ms and reached_ms is not None:
@@ -466,9 +515,12 @@ def run_relmse_study(args) -> dict:
             break
     # Guided error at the plain render's wall time (linear between points).
     eq_err = None
-    for (s0, t0, e0), (s1, t1, e1) in zip(curve, curve[1:]):
+    for (s0, t0, e0, _), (s1, t1, e1, _) in zip(curve, curve[1:]):
         if t0 <= plain_ms <= t1:
             eq_err = e0 + (e1 - e0) * (plain_ms - t0) / max(t1 - t0, 1e-9)
+    # the same ratio under the other metric (robust <-> plain relMSE)
+    plain_other = other(plain_img, ref)
+    reached_other = next((t for _, t, _, e in curve if e <= plain_other), None)
     guided_img = image()
     ctx.close()
     return {
@@ -477,14 +529,15 @@ def run_relmse_study(args) -> dict:
                                                 else ""),
         "workload": f"{args.workload} {w}x{h}, depth {depth}",
         "reference": {"spp": args.ref_spp, "ms": ref_ms},
-        "plain": {"spp": args.plain_spp, "ms": plain_ms, "relmse": plain_err,
+        "plain": {"spp": args.plain_spp, "ms": plain_ms, "relmse": plain_err, "relmse_other_metric": plain_other,
                   "rrmse_metrics_h": rrmse_reference_metric(plain_img, ref)},
         "guided": dict(extra, guide=args.guide, train_spp=train_spp, train_ms=train_ms,
                        guide_fraction=args.guide_fraction, spp_rendered=total,
                        ms_to_plain_error=reached_ms, relmse_at_plain_time=eq_err,
                        rrmse_metrics_h_final=rrmse_reference_metric(guided_img, ref),
-                       curve=[{"spp": a, "ms": b, "relmse": c} for a, b, c in curve]),
+                       curve=[{"spp": a, "ms": b, "relmse": c, "relmse_other_metric": d} for a, b, c, d in curve]),
         "time_ratio_guided_over_plain": (reached_ms / plain_ms) if reached_ms else None,
+        "time_ratio_other_metric": (reached_other / plain_ms) if reached_other else None,
     }
 
 
@@ -834,6 +887,7 @@ def main() -> None:
     ap.add_argument("--mode", choices=["plain", "guided_quadtree", "guided_mlp"], default="plain")
     ap.add_argument("--workload", choices=["interior", "cornell"], default="interior")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-side-modes", action="store_true", help="skip the guided and depth-8 side measurements")
     ap.add_argument("--spp-per-step", type=int, default=32,
                     help="samples per pixel of one step: one pgx_render call, one wavefront")
     ap.add_argument("--study", choices=["relmse", "traversal", "adjoint", "batch"], default=None,

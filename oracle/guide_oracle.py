@@ -113,6 +113,29 @@ def pss_uv(normal: np.ndarray, wi: np.ndarray) -> tuple[np.ndarray, np.ndarray, 
     return np.clip(u, F(0), ONE_MINUS), np.clip(v, F(0), ONE_MINUS), ok
 
 
+def subtree_ranges(nodes: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """(first record, record count) of every node's subtree, from the leaves'
+    ranges (records are in leaf order, so a subtree's records are contiguous)."""
+    n = len(nodes)
+    first = np.zeros(n, np.int64)
+    count = np.zeros(n, np.int64)
+    order, stack = [], [0]
+    while stack:
+        i = stack.pop()
+        order.append(i)
+        if nodes[i]["left"] >= 0:
+            stack += [int(nodes[i]["left"]), int(nodes[i]["right"])]
+    for i in reversed(order):
+        nd = nodes[i]
+        if nd["left"] < 0:
+            first[i], count[i] = int(nd["offset"]), int(nd["used"])
+        else:
+            a, b = int(nd["left"]), int(nd["right"])
+            first[i] = min(first[a], first[b])
+            count[i] = count[a] + count[b]
+    return first, count
+
+
 def regions_from_bvh(nodes: np.ndarray, n_records: int) -> list[tuple[int, int, int]]:
     """(first, count, node) of every region, in record order: the subtrees
     whose record count first drops to REGION_MAX (the root when the cache
@@ -121,17 +144,16 @@ def regions_from_bvh(nodes: np.ndarray, n_records: int) -> list[tuple[int, int, 
         return []
     if n_records <= REGION_MAX:
         return [(0, n_records, 0)]
+    first, count = subtree_ranges(nodes)
     out = []
     stack = [0]
     while stack:
         i = stack.pop()
-        nd = nodes[i]
-        if nd["left"] < 0:
+        if nodes[i]["left"] < 0:
             continue  # a leaf of a region above the bound cannot exist (leaves hold <= 8)
-        for c in (int(nd["left"]), int(nd["right"])):
-            ch = nodes[c]
-            if ch["used"] <= REGION_MAX:
-                out.append((int(ch["offset"]), int(ch["used"]), c))
+        for c in (int(nodes[i]["left"]), int(nodes[i]["right"])):
+            if count[c] <= REGION_MAX:
+                out.append((int(first[c]), int(count[c]), c))
             else:
                 stack.append(c)
     return sorted(out)

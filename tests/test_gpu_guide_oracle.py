@@ -112,12 +112,12 @@ def test_quadtrees_match_oracle(ctx, n, seed):
 def test_primary_sample_quadtrees_match_oracle(ctx):
     """Trees over the diffuse sampler's primary samples, built from the
     records of a PGX_MODE_GUIDED_PSS render of the small interior."""
-    desc = scenes.interior(seed=3, target_tris=20000, n_objects=40, width=64, height=36, env_width=256,
+    desc = scenes.interior(seed=3, target_tris=20000, n_objects=40, width=128, height=72, env_width=256,
                            env_height=128)
     ctx.upload(desc)
     ctx.bvh_build()
     ctx.clear()
-    ctx.render(4, mode=abi.MODE_GUIDED_PSS, seed=5, max_depth=8, record_paths=4)
+    ctx.render(8, mode=abi.MODE_GUIDED_PSS, seed=5, max_depth=8, record_paths=8)
     nodes, out = ctx.cache_export()
     regions, qnodes, pss = ctx.guide_export()
     assert pss and len(out) > 2 * go.REGION_MAX

@@ -119,7 +119,8 @@ def test_regions_from_a_median_split_tree():
     nodes = np.zeros(7, [("bmin", "<f4", 3), ("bmax", "<f4", 3), ("left", "<i4"), ("right", "<i4"),
                          ("offset", "<i4"), ("used", "<i4")])
     # root 3000 -> 1500 + 1500 -> (750, 750) + (750, 750)
-    spec = [(1, 2, 0, 3000), (3, 4, 0, 1500), (5, 6, 1500, 1500), (-1, -1, 0, 750), (-1, -1, 750, 750),
+    # interior nodes carry no range of their own (as exported): it comes from the leaves
+    spec = [(1, 2, 0, 0), (3, 4, 0, 0), (5, 6, 0, 0), (-1, -1, 0, 750), (-1, -1, 750, 750),
             (-1, -1, 1500, 750), (-1, -1, 2250, 750)]
     for i, (l, r, o, u) in enumerate(spec):
         nodes[i]["left"], nodes[i]["right"], nodes[i]["offset"], nodes[i]["used"] = l, r, o, u
