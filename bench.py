@@ -522,6 +522,11 @@ def run_relmse_study(args) -> dict:
     plain_other = other(plain_img, ref)
     reached_other = next((t for _, t, _, e in curve if e <= plain_other), None)
     guided_img = image()
+    if args.save_images:
+        d = Path(args.save_images)
+        d.mkdir(parents=True, exist_ok=True)
+        np.save(d / f"plain_{args.plain_spp}spp.npy", plain_img.astype(np.float32))
+        np.save(d / f"guided_{args.guide}.npy", guided_img.astype(np.float32))
     ctx.close()
     return {
         "study": f"equal-time relMSE, {args.guide}-guided vs plain GPU path tracing",
@@ -587,10 +592,17 @@ def run_adjoint_study(args) -> dict:
     used = np.unique(desc.triangles["material"])
     nz_env = np.flatnonzero(np.abs(g_env).ravel() > 0)
     for k in kinds:
+        step = h
         if k == 0:
+            # The image is linear in every texel (sampling is detached), so the
+            # loss is quadratic in it and the central difference is exact at
+            # any step; the step is 1e-3 relative to the texel so that bright
+            # texels (the sun lobe reaches 5e4) move the float32 path
+            # radiance by more than its rounding.
             idx = int(rng.choice(nz_env))
-            e1 = env0.copy().ravel(); e1[idx] += h
-            e2 = env0.copy().ravel(); e2[idx] -= h
+            step = h * max(1.0, abs(float(env0.ravel()[idx])))
+            e1 = env0.copy().ravel(); e1[idx] += step
+            e2 = env0.copy().ravel(); e2[idx] -= step
             lp = (dict(env=e1.reshape(env0.shape)), dict(env=e2.reshape(env0.shape)))
             g = float(g_env.ravel()[idx]); name = f"env[{idx}]"
         elif k == 1:
@@ -608,7 +620,7 @@ def run_adjoint_study(args) -> dict:
         for kw in lp:
             ctx.diff_set_params(**kw)
             vals.append(float(np.sum((ctx.diff_render(spp, seed, depth) - target) ** 2)))
-        res.append((name, (vals[0] - vals[1]) / (2 * h), g))
+        res.append((name, (vals[0] - vals[1]) / (2 * step), g))
     fd_s = time.perf_counter() - t0
     ctx.diff_set_params()
     ctx.close()
@@ -619,7 +631,8 @@ def run_adjoint_study(args) -> dict:
     significant = np.abs(fd) > 1e-3 * scale
     paths = 512 * 512 * spp
     return {
-        "study": "adjoint gradients vs central finite differences (h = 1e-3), fBm heightfield",
+        "study": "adjoint gradients vs central finite differences, fBm heightfield",
+        "fd_step": "1e-3 for albedo offsets and roughness; 1e-3 x max(1, texel) for environment texels",
         "workload": f"terrain {desc.ntris} tris, {nm} materials, env 512x256, 512x512, depth {depth}",
         "loss": loss, "spp": spp, "target_spp": 256,
         "primal_s": primal_s, "adjoint_s": adjoint_s, "target_s": target_s,
@@ -904,6 +917,7 @@ def main() -> None:
     ap.add_argument("--mlp-decay", type=float, default=0.998)
     ap.add_argument("--mlp-steps", type=int, default=4)
     ap.add_argument("--ref-cache", default=None, help="npy file keeping the converged image between study runs")
+    ap.add_argument("--save-images", default=None, help="directory for the study's final plain and guided images")
     ap.add_argument("--guide-depth", type=int, default=0, help="guide the first N bounces only (0: all)")
     ap.add_argument("--mlp-indirect", action="store_true", help="train the learned guide on indirect light only")
     ap.add_argument("--trav-rays", type=int, default=10_000_000)

@@ -1114,9 +1114,8 @@ __global__ void __launch_bounds__(kThreads) k_finalize(SceneView sv, PathState p
 }
 
 // ---- differentiable rendering ---------------------------------------------------------
-// Plain path tracing with NEE + MIS (the estimator of k_shade<PLAIN>) as one
-// thread per pixel looping over its samples, in two flavours sharing
-// diff_path:
+// Plain path tracing with NEE + MIS (the estimator of k_shade<PLAIN>), in
+// two flavours sharing diff_path:
 //  * primal: sampling decisions (directions, pdfs, MIS weights, Russian
 //    roulette, the environment's sampling tables) use the uploaded scene,
 //    while radiance is evaluated with the "evaluation" parameters -- the
@@ -1125,16 +1124,19 @@ __global__ void __launch_bounds__(kThreads) k_finalize(SceneView sv, PathState p
 //    kernel adds the 4 neighbours' partial sums in a fixed order, so the
 //    image is deterministic and a finite difference between two parameter
 //    sets differs only through the samples a parameter touches;
-//  * adjoint: with evaluation = uploaded parameters, each sample is traced
-//    twice from its seed.  The first pass gives its radiance L; the second
-//    replays the path and at every vertex j accumulates
-//      d/dtheta of the terms added there (NEE: albedo, roughness, the
+//  * adjoint: with evaluation = uploaded parameters, one thread per sample
+//    traces the path once from its seed; every vertex j keeps (in the
+//    thread's registers and local memory, never in global memory) what its
+//    terms need, and once the path's radiance L is known the thread adds
+//      d/dtheta of the terms added at j (NEE: albedo, roughness, the
 //      environment texels under the light direction; escaped rays: the
 //      texels under the ray), and
 //      (L - L_up_to_j) * d log beta_j / dtheta for the continuation weight
 //      beta_j = f(wi) |cos| / pdf(wi) (path replay backpropagation, Vicini
-//      et al. 2021), with pdf detached,
-//    each weighted by dLoss/dImage at the sample's pixel / spp.
+//      et al. 2021, whose second replay pass the per-vertex records
+//      replace), with pdf detached,
+//    each weighted by dLoss/dImage at the sample's pixel / spp, into double
+//    accumulators (material terms per block in shared memory).
 struct DiffView {
     const DevMaterial* __restrict__ mats_e;  // evaluation materials
     DevEnv env_e;                            // evaluation environment (sampling tables of sv.env)
@@ -1142,9 +1144,9 @@ struct DiffView {
     uint64_t seed;
     double* partial;          // primal: [npix][4][3]
     const float* dimg;        // adjoint: dLoss/dImage [npix][3]
-    float* g_env;             // [env W*H*3]
-    float* g_alb;             // [nmats*3]
-    float* g_rough;           // [nmats]
+    double* g_env;            // [env W*H*3]
+    double* g_alb;            // [nmats*3]
+    double* g_rough;          // [nmats]
     int nmats;
 };
 
@@ -1182,7 +1184,7 @@ __device__ float conductor_dlogf_drough(const DevMaterial& m, F3 wil, F3 wol) {
 
 // Adds g (rgb) times the bilinear weights of the environment lookup of wi
 // (env_eval's texel choice) to the texel gradients.
-__device__ void env_scatter(const DevEnv& e, F3 wi, F3 g, float* grad) {
+__device__ void env_scatter(const DevEnv& e, F3 wi, F3 g, double* grad) {
     if (!e.valid || !grad) return;
     float u = atan2f(wi.z, wi.x);
     u = (u < 0.f) ? u + PGX_2PI_F : u;
@@ -1202,35 +1204,60 @@ __device__ void env_scatter(const DevEnv& e, F3 wi, F3 g, float* grad) {
     long long idx[4] = {(long long)y * W + x, (long long)y * W + x1, (long long)y1 * W + x, (long long)y1 * W + x1};
     for (int k = 0; k < 4; k++) {
         if (w[k] == 0.f) continue;
-        atomicAdd(grad + 3 * idx[k] + 0, g.x * w[k]);
-        atomicAdd(grad + 3 * idx[k] + 1, g.y * w[k]);
-        atomicAdd(grad + 3 * idx[k] + 2, g.z * w[k]);
+        atomicAdd(grad + 3 * idx[k] + 0, (double)(g.x * w[k]));
+        atomicAdd(grad + 3 * idx[k] + 1, (double)(g.y * w[k]));
+        atomicAdd(grad + 3 * idx[k] + 2, (double)(g.z * w[k]));
     }
 }
 
 struct DiffAcc {
-    float* alb;    // shared memory [nmats*3] or global
-    float* rough;  // [nmats]
+    double* alb;    // shared memory [nmats*3] or global
+    double* rough;  // [nmats]
 };
 
 __device__ __forceinline__ void add_alb(const DiffAcc& acc, int mat, F3 g) {
-    atomicAdd(acc.alb + 3 * mat + 0, g.x);
-    atomicAdd(acc.alb + 3 * mat + 1, g.y);
-    atomicAdd(acc.alb + 3 * mat + 2, g.z);
+    atomicAdd(acc.alb + 3 * mat + 0, (double)g.x);
+    atomicAdd(acc.alb + 3 * mat + 1, (double)g.y);
+    atomicAdd(acc.alb + 3 * mat + 2, (double)g.z);
 }
+
+// What the gradient of one path vertex needs once the path's radiance is
+// known: the NEE contribution and its log-derivative factors, the radiance
+// collected up to the vertex (the continuation's term is delta x (L_total -
+// L_snap) x d log beta / d theta), and the environment lookup of an
+// environment light sample.
+struct DiffVertex {
+    F3 ia;        // 1 / albedo (per channel) when the material is albedo-linear, else 0
+    F3 C;         // NEE contribution T * emitted * weight (0 without one)
+    F3 tcw;       // environment NEE: T * radiance weight of the sample
+    F3 wi;        // environment NEE direction
+    F3 l_snap;    // radiance collected up to and including this vertex's NEE
+    float dr_nee, dr_cont;
+    int mat;
+    int flags;    // 1: NEE term, 2: environment NEE, 4: continuation term
+};
 
 __device__ __forceinline__ F3 safe_div3(F3 a, F3 b) {
     return f3(a.x / fmaxf(b.x, 1e-6f), a.y / fmaxf(b.y, 1e-6f), a.z / fmaxf(b.z, 1e-6f));
 }
 
-// One path from its seed.  GRAD: L_total is the first pass's radiance and
-// delta the adjoint of the sample's value.  Returns the path's radiance.
+// One path from its seed.  Returns the path's radiance.  GRAD: delta is the
+// adjoint of the sample's value; each vertex keeps what its gradient terms
+// need (DiffVertex) and the terms are emitted after the last vertex, when
+// the path's total radiance is known and the sample is known to be kept by
+// the film (finite) — one traversal per sample (path replay
+// backpropagation, Vicini et al. 2021, with the replay's second pass folded
+// into per-vertex records held by the thread).
 template <bool GRAD>
-__device__ F3 diff_path(const SceneView& sv, const DiffView& dv, uint64_t rng, F3 o, F3 dir, F3 L_total, F3 delta,
+__device__ F3 diff_path(const SceneView& sv, const DiffView& dv, uint64_t rng, F3 o, F3 dir, F3 delta,
                         const DiffAcc& acc) {
     F3 T = f3(1.f, 1.f, 1.f), Ts = T, L = zero3();
     bool prev_spec = false;
     float prev_pdf = 0.f;
+    DiffVertex vtx[GRAD ? kMaxDepthCap + 1 : 1];
+    int nvtx = 0;
+    F3 esc_dir = zero3(), esc_w = zero3();  // escaped ray: direction, T x MIS weight
+    bool escaped = false;
     for (int depth = 0; depth <= dv.max_depth; depth++) {
         int id;
         float t, hu, hv;
@@ -1254,7 +1281,11 @@ __device__ F3 diff_path(const SceneView& sv, const DiffView& dv, uint64_t rng, F
             }
             if (w > 0.f) {
                 L = L + (T * bg) * w;
-                if (GRAD) env_scatter(dv.env_e, dir, (delta * T) * w, dv.g_env);
+                if (GRAD) {
+                    escaped = true;
+                    esc_dir = dir;
+                    esc_w = T * w;
+                }
             }
             break;
         }
@@ -1265,6 +1296,13 @@ __device__ F3 diff_path(const SceneView& sv, const DiffView& dv, uint64_t rng, F
         shading_data(sv, make_float4(o.x, o.y, o.z, 0.f), make_float4(dir.x, dir.y, dir.z, 0.f),
                      make_float4(__int_as_float(id), t, hu, hv), sd, ms, tri_gn, tri_area);
         const DevMaterial me = dv.mats_e[sd.mat];
+        DiffVertex* V = GRAD ? &vtx[nvtx] : nullptr;
+        if (GRAD) {
+            nvtx++;
+            V->flags = 0;
+            V->mat = sd.mat;
+            V->ia = albedo_linear(me) ? safe_div3(f3(1.f, 1.f, 1.f), albedo_of(sv.tex, me, sd)) : zero3();
+        }
         if (ms.is_light) {
             F3 em = f3(ms.emission[0], ms.emission[1], ms.emission[2]);
             if (depth == 0 || prev_spec) {
@@ -1350,11 +1388,14 @@ __device__ F3 diff_path(const SceneView& sv, const DiffView& dv, uint64_t rng, F
                         F3 C = T * contrib;
                         L = L + C;
                         if (GRAD) {
-                            F3 g = delta * C;
-                            if (albedo_linear(me)) add_alb(acc, sd.mat, safe_div3(g, albedo_of(sv.tex, me, sd)));
-                            float dr = conductor_dlogf_drough(me, to_local(sd.frame, wi), to_local(sd.frame, sd.wo));
-                            if (dr != 0.f) atomicAdd(acc.rough + sd.mat, (g.x + g.y + g.z) * dr);
-                            if (env_light) env_scatter(dv.env_e, wi, delta * (T * cw), dv.g_env);
+                            V->flags |= 1;
+                            V->C = C;
+                            V->dr_nee = conductor_dlogf_drough(me, to_local(sd.frame, wi), to_local(sd.frame, sd.wo));
+                            if (env_light) {
+                                V->flags |= 2;
+                                V->wi = wi;
+                                V->tcw = T * cw;
+                            }
                         }
                     }
                 }
@@ -1389,12 +1430,9 @@ __device__ F3 diff_path(const SceneView& sv, const DiffView& dv, uint64_t rng, F
             fe = bsdf_eval(me, sv.tex, sd, wi);
         }
         if (GRAD) {
-            F3 g = delta * (L_total - L);  // radiance collected after this vertex
-            if (albedo_linear(me)) add_alb(acc, sd.mat, safe_div3(g, albedo_of(sv.tex, me, sd)));
-            if (!spec) {
-                float dr = conductor_dlogf_drough(me, to_local(sd.frame, wi), to_local(sd.frame, sd.wo));
-                if (dr != 0.f) atomicAdd(acc.rough + sd.mat, (g.x + g.y + g.z) * dr);
-            }
+            V->flags |= 4;
+            V->l_snap = L;
+            V->dr_cont = spec ? 0.f : conductor_dlogf_drough(me, to_local(sd.frame, wi), to_local(sd.frame, sd.wo));
         }
         T = divs(T * fe * cos_t, pdf);
         Ts = divs(Ts * fs * cos_t, pdf);
@@ -1407,6 +1445,24 @@ __device__ F3 diff_path(const SceneView& sv, const DiffView& dv, uint64_t rng, F
         dir = wi;
         prev_spec = spec;
         prev_pdf = pdf;
+    }
+    if (GRAD && valid(L)) {  // the film drops non-finite samples: no gradient from them
+        for (int j = 0; j < nvtx; j++) {
+            const DiffVertex& v = vtx[j];
+            const bool alb = v.ia.x != 0.f || v.ia.y != 0.f || v.ia.z != 0.f;
+            if (v.flags & 1) {
+                F3 g = delta * v.C;
+                if (alb) add_alb(acc, v.mat, g * v.ia);
+                if (v.dr_nee != 0.f) atomicAdd(acc.rough + v.mat, (double)((g.x + g.y + g.z) * v.dr_nee));
+                if (v.flags & 2) env_scatter(dv.env_e, v.wi, delta * v.tcw, dv.g_env);
+            }
+            if (v.flags & 4) {
+                F3 g = delta * (L - v.l_snap);  // radiance collected after this vertex
+                if (alb) add_alb(acc, v.mat, g * v.ia);
+                if (v.dr_cont != 0.f) atomicAdd(acc.rough + v.mat, (double)((g.x + g.y + g.z) * v.dr_cont));
+            }
+        }
+        if (escaped) env_scatter(dv.env_e, esc_dir, delta * esc_w, dv.g_env);
     }
     return L;
 }
@@ -1437,7 +1493,7 @@ __global__ void __launch_bounds__(kThreads) k_diff_primal(SceneView sv, DiffView
             uint64_t rng;
             F3 dir;
             int k = diff_camera(sv, dv, pixel, s, rng, dir);
-            F3 c = diff_path<false>(sv, dv, rng, origin, dir, zero3(), zero3(), none);
+            F3 c = diff_path<false>(sv, dv, rng, origin, dir, zero3(), none);
             if (k < 0 || !valid(c)) continue;
             acc[k][0] += (double)c.x;
             acc[k][1] += (double)c.y;
@@ -1468,11 +1524,11 @@ __global__ void k_diff_gather(const double* __restrict__ partial, int W, int H, 
 }
 
 __global__ void __launch_bounds__(kThreads) k_diff_adjoint(SceneView sv, DiffView dv) {
-    extern __shared__ float sacc[];  // [nmats*3 + nmats] when it fits
-    const bool shared_acc = dv.nmats * 4 * (int)sizeof(float) <= 32 * 1024;
+    extern __shared__ double sacc[];  // [nmats*3 + nmats] when it fits
+    const bool shared_acc = dv.nmats * 4 * (int)sizeof(double) <= 32 * 1024;
     DiffAcc acc;
     if (shared_acc) {
-        for (int i = threadIdx.x; i < dv.nmats * 4; i += blockDim.x) sacc[i] = 0.f;
+        for (int i = threadIdx.x; i < dv.nmats * 4; i += blockDim.x) sacc[i] = 0.0;
         __syncthreads();
         acc.alb = sacc;
         acc.rough = sacc + dv.nmats * 3;
@@ -1481,30 +1537,31 @@ __global__ void __launch_bounds__(kThreads) k_diff_adjoint(SceneView sv, DiffVie
         acc.rough = dv.g_rough;
     }
     const int64_t npix = (int64_t)sv.width * sv.height;
+    const int64_t items = npix * dv.spp;
     const F3 origin = f3(sv.cam.origin[0], sv.cam.origin[1], sv.cam.origin[2]);
     const float inv_spp = 1.f / (float)dv.spp;
-    for (int64_t pixel = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; pixel < npix;
-         pixel += (int64_t)gridDim.x * blockDim.x) {
+    // One sample per thread: neighbouring threads take neighbouring pixels
+    // of the same sample index (coherent camera rays).
+    for (int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; item < items;
+         item += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t pixel = item % npix;
+        const int s = (int)(item / npix);
         int x = (int)(pixel % sv.width), y = (int)(pixel / sv.width);
-        for (int s = 0; s < dv.spp; s++) {
-            uint64_t rng;
-            F3 dir;
-            int k = diff_camera(sv, dv, pixel, s, rng, dir);
-            if (k < 0) continue;
-            int64_t tp = (int64_t)(y + k / 2) * sv.width + (x + k % 2);
-            F3 delta = f3(dv.dimg[3 * tp], dv.dimg[3 * tp + 1], dv.dimg[3 * tp + 2]) * inv_spp;
-            if (delta.x == 0.f && delta.y == 0.f && delta.z == 0.f) continue;
-            F3 L = diff_path<false>(sv, dv, rng, origin, dir, zero3(), zero3(), acc);
-            if (!valid(L)) continue;  // the film drops these samples
-            diff_path<true>(sv, dv, rng, origin, dir, L, delta, acc);
-        }
+        uint64_t rng;
+        F3 dir;
+        int k = diff_camera(sv, dv, pixel, s, rng, dir);
+        if (k < 0) continue;
+        int64_t tp = (int64_t)(y + k / 2) * sv.width + (x + k % 2);
+        F3 delta = f3(dv.dimg[3 * tp], dv.dimg[3 * tp + 1], dv.dimg[3 * tp + 2]) * inv_spp;
+        if (delta.x == 0.f && delta.y == 0.f && delta.z == 0.f) continue;
+        diff_path<true>(sv, dv, rng, origin, dir, delta, acc);
     }
     if (shared_acc) {
         __syncthreads();
         for (int i = threadIdx.x; i < dv.nmats * 3; i += blockDim.x)
-            if (sacc[i] != 0.f) atomicAdd(dv.g_alb + i, sacc[i]);
+            if (sacc[i] != 0.0) atomicAdd(dv.g_alb + i, sacc[i]);
         for (int i = threadIdx.x; i < dv.nmats; i += blockDim.x)
-            if (sacc[dv.nmats * 3 + i] != 0.f) atomicAdd(dv.g_rough + i, sacc[dv.nmats * 3 + i]);
+            if (sacc[dv.nmats * 3 + i] != 0.0) atomicAdd(dv.g_rough + i, sacc[dv.nmats * 3 + i]);
     }
 }
 
@@ -2109,29 +2166,35 @@ extern "C" int pgx_diff_adjoint(pgx_ctx* ctx, int32_t spp, uint64_t seed, int32_
     const size_t ef = env_floats(ctx), nm = (size_t)ctx->nmats;
     cudaStream_t s = ctx->stream;
     PGX_CUDA_TRY(ctx, rs->d_dimg.reserve(sizeof(float) * 3 * npix));
-    PGX_CUDA_TRY(ctx, rs->d_genv.reserve(sizeof(float) * std::max<size_t>(ef, 1)));
-    PGX_CUDA_TRY(ctx, rs->d_galb.reserve(sizeof(float) * std::max<size_t>(3 * nm, 1)));
-    PGX_CUDA_TRY(ctx, rs->d_grough.reserve(sizeof(float) * std::max<size_t>(nm, 1)));
+    // Gradients are accumulated in double (millions of atomic additions
+    // into the popular texels) and returned as float.
+    PGX_CUDA_TRY(ctx, rs->d_genv.reserve(sizeof(double) * std::max<size_t>(ef, 1)));
+    PGX_CUDA_TRY(ctx, rs->d_galb.reserve(sizeof(double) * std::max<size_t>(3 * nm, 1)));
+    PGX_CUDA_TRY(ctx, rs->d_grough.reserve(sizeof(double) * std::max<size_t>(nm, 1)));
     PGX_CUDA_TRY(ctx, cudaMemcpyAsync(rs->d_dimg.p, dloss_dimage, sizeof(float) * 3 * npix, cudaMemcpyHostToDevice, s));
-    PGX_CUDA_TRY(ctx, cudaMemsetAsync(rs->d_genv.p, 0, sizeof(float) * std::max<size_t>(ef, 1), s));
-    PGX_CUDA_TRY(ctx, cudaMemsetAsync(rs->d_galb.p, 0, sizeof(float) * std::max<size_t>(3 * nm, 1), s));
-    PGX_CUDA_TRY(ctx, cudaMemsetAsync(rs->d_grough.p, 0, sizeof(float) * std::max<size_t>(nm, 1), s));
+    PGX_CUDA_TRY(ctx, cudaMemsetAsync(rs->d_genv.p, 0, sizeof(double) * std::max<size_t>(ef, 1), s));
+    PGX_CUDA_TRY(ctx, cudaMemsetAsync(rs->d_galb.p, 0, sizeof(double) * std::max<size_t>(3 * nm, 1), s));
+    PGX_CUDA_TRY(ctx, cudaMemsetAsync(rs->d_grough.p, 0, sizeof(double) * std::max<size_t>(nm, 1), s));
     DiffView dv = diff_view(ctx, rs, spp, seed, max_depth);
     dv.dimg = rs->d_dimg.as<float>();
-    dv.g_env = ef ? rs->d_genv.as<float>() : nullptr;
-    dv.g_alb = rs->d_galb.as<float>();
-    dv.g_rough = rs->d_grough.as<float>();
-    const size_t sm = nm * 4 * sizeof(float) <= 32 * 1024 ? nm * 4 * sizeof(float) : 0;
+    dv.g_env = ef ? rs->d_genv.as<double>() : nullptr;
+    dv.g_alb = rs->d_galb.as<double>();
+    dv.g_rough = rs->d_grough.as<double>();
+    const size_t sm = nm * 4 * sizeof(double) <= 32 * 1024 ? nm * 4 * sizeof(double) : 0;
     SceneView sv = scene_view(ctx);
-    k_diff_adjoint<<<grid_for(npix), kThreads, sm, s>>>(sv, dv);
+    k_diff_adjoint<<<grid_for(npix * (int64_t)spp), kThreads, sm, s>>>(sv, dv);
     PGX_CUDA_TRY(ctx, cudaGetLastError());
-    if (grad_env && ef)
-        PGX_CUDA_TRY(ctx, cudaMemcpyAsync(grad_env, rs->d_genv.p, sizeof(float) * ef, cudaMemcpyDeviceToHost, s));
-    if (grad_albedo && nm)
-        PGX_CUDA_TRY(ctx, cudaMemcpyAsync(grad_albedo, rs->d_galb.p, sizeof(float) * 3 * nm, cudaMemcpyDeviceToHost, s));
-    if (grad_roughness && nm)
-        PGX_CUDA_TRY(ctx, cudaMemcpyAsync(grad_roughness, rs->d_grough.p, sizeof(float) * nm, cudaMemcpyDeviceToHost, s));
+    std::vector<double> he(grad_env && ef ? ef : 0), ha(grad_albedo ? 3 * nm : 0), hr(grad_roughness ? nm : 0);
+    if (!he.empty())
+        PGX_CUDA_TRY(ctx, cudaMemcpyAsync(he.data(), rs->d_genv.p, sizeof(double) * ef, cudaMemcpyDeviceToHost, s));
+    if (!ha.empty())
+        PGX_CUDA_TRY(ctx, cudaMemcpyAsync(ha.data(), rs->d_galb.p, sizeof(double) * 3 * nm, cudaMemcpyDeviceToHost, s));
+    if (!hr.empty())
+        PGX_CUDA_TRY(ctx, cudaMemcpyAsync(hr.data(), rs->d_grough.p, sizeof(double) * nm, cudaMemcpyDeviceToHost, s));
     PGX_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    for (size_t i = 0; i < he.size(); i++) grad_env[i] = (float)he[i];
+    for (size_t i = 0; i < ha.size(); i++) grad_albedo[i] = (float)ha[i];
+    for (size_t i = 0; i < hr.size(); i++) grad_roughness[i] = (float)hr[i];
     return PGX_OK;
 }
 
