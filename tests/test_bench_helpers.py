@@ -20,11 +20,12 @@ def test_profile_traffic_scales_with_the_launch():
     rays of an average launch."""
     d = json.loads((ROOT / "profiles" / "traffic.json").read_text())
     per_ray = float(d["k_extend"]["bytes_per_unit"])
-    t, note = bench.profile_traffic("k_extend", 1.0e6)
-    assert t == per_ray * 1.0e6 and note
-    t2, _ = bench.profile_traffic("k_extend", 2.0e6)
+    t, note, issue = bench.profile_traffic("k_extend", 1.0e6)
+    assert t == per_ray * 1.0e6 and note and ".md" not in note
+    assert len(issue["threads_per_executed_instruction"]) == len(issue["smsp_issue_active_pct"])
+    t2, _, _ = bench.profile_traffic("k_extend", 2.0e6)
     assert t2 == 2 * t
-    assert bench.profile_traffic("no_such_kernel", 1.0) == (None, None)
+    assert bench.profile_traffic("no_such_kernel", 1.0) == (None, None, None)
 
 
 def test_relmse_metrics():
