@@ -353,7 +353,15 @@ __device__ __forceinline__ void trace_persistent(const BvhView& bvh, unsigned n,
         }
         if (__all_sync(kFull, ray < 0)) break;  // every lane idle and the queue is drained
         for (int s = 0; s < kMaxSteps; s++) {
-            if (ray >= 0) {
+            // Branch vote: lanes at a leaf (triangle tests) and lanes at an
+            // interior node (two slab tests) take different code; when a warp
+            // holds both, only the larger group steps this time and the other
+            // waits one step.  A ray's own sequence of nodes and triangles is
+            // unchanged (it only pauses), so results stay bit-identical.
+            const unsigned act = __ballot_sync(kFull, ray >= 0);
+            const unsigned leaf = __ballot_sync(kFull, ray >= 0 && L.cnt > 0);
+            const bool leaf_turn = 2 * __popc(leaf) >= __popc(act);
+            if (ray >= 0 && (L.cnt > 0) == leaf_turn) {
                 if (lane_step<ANY, COUNT>(bvh, L, stack, n_interior, n_tris)) {
                     status_or |= (unsigned)L.status;
                     store((unsigned)ray, L);
