@@ -478,19 +478,28 @@ def run_relmse_study(args) -> dict:
     train_ms = 0.0
     train_spp = 0
     extra = {}
+    waves = args.guide == "mlp" and args.mlp_schedule == "waves"
     if args.guide == "mlp":
-        # Learned guide: online training on the first `train_frames` frames
-        # (one Adam step per frame, batch 2^18), which stay in the image.
         ctx.mlp_init(3)
         ctx.mlp_configure(lr=args.mlp_lr, decay=args.mlp_decay, batch=1 << 18, steps=args.mlp_steps,
                           direct=not args.mlp_indirect)
         mode = abi.MODE_GUIDED_MLP
-        train_ms = render_ms(args.train_frames, mode, 13, guide_fraction=args.guide_fraction, train_guide=True,
-                             guide_depth=args.guide_depth)
-        train_spp = args.train_frames
-        extra = {"train_frames": args.train_frames, "lr": args.mlp_lr, "lr_decay": args.mlp_decay,
-                 "adam_steps_per_frame": args.mlp_steps, "guide_depth": args.guide_depth,
-                 "target": "indirect" if args.mlp_indirect else "full incident radiance"}
+        extra = {"schedule": args.mlp_schedule, "lr": args.mlp_lr, "lr_decay": args.mlp_decay,
+                 "guide_depth": args.guide_depth, "target": "indirect" if args.mlp_indirect else "full incident radiance"}
+        if waves:
+            # Learned guide trained on the render's own wavefronts: calls of
+            # 1, 1, 2, 2, 4, 4, ... frames up to the chunk size, then chunks;
+            # after every call `mlp_steps` Adam steps on samples of its first
+            # 2^21 paths, while the frame count is below train_frames.  All of
+            # it is timed and stays in the image.
+            extra.update(adam_steps_per_wave=args.mlp_steps, train_until_spp=args.train_frames)
+        else:
+            # Learned guide: online training on the first `train_frames` frames
+            # (`mlp_steps` Adam steps per frame, batch 2^18), which stay in the image.
+            train_ms = render_ms(args.train_frames, mode, 13, guide_fraction=args.guide_fraction, train_guide=True,
+                                 guide_depth=args.guide_depth)
+            train_spp = args.train_frames
+            extra.update(train_frames=args.train_frames, adam_steps_per_frame=args.mlp_steps)
     else:
         # QuadTree (directions) or PSS (primary samples): train the cache over
         # `train_iters` iterations of 1, 2, 4, ... frames (the first unguided,
@@ -512,10 +521,20 @@ def run_relmse_study(args) -> dict:
     reached_ms = None
     chunk = max(1, args.plain_spp // 32)
     total = train_spp if args.guide == "mlp" else 0
+    ramp = [1, 1, 2, 2, 4, 4, 8, 8, 16, 16]
+    calls = 0
     while total < 4 * args.plain_spp:
-        guided_ms += render_ms(chunk, mode, 17 + total, guide_fraction=args.guide_fraction,
-                               guide_depth=args.guide_depth)
-        total += chunk
+        if waves:
+            n = min(ramp[calls], chunk) if calls < len(ramp) else chunk
+            train = total < args.train_frames
+            guided_ms += render_ms(n, mode, 17 + total, guide_fraction=args.guide_fraction,
+                                   guide_depth=args.guide_depth, train_guide=train, train_waves=train)
+            calls += 1
+            total += n
+        else:
+            guided_ms += render_ms(chunk, mode, 17 + total, guide_fraction=args.guide_fraction,
+                                   guide_depth=args.guide_depth)
+            total += chunk
         img = image()
         err = metric(img, ref)
         curve.append((total, train_ms + guided_ms, err, other(img, ref)))
@@ -597,6 +616,7 @@ def run_adjoint_study(args) -> dict:
     g_env, g_alb, g_rough = ctx.diff_adjoint(dimg, spp, seed, depth)
     adjoint_s = time.perf_counter() - t0
     h = 1e-3
+    env_step = 0.1
     n_fd = args.fd_params
     kinds = rng.choice(3, n_fd, p=[0.5, 0.25, 0.25])
     res = []
@@ -608,11 +628,12 @@ def run_adjoint_study(args) -> dict:
         if k == 0:
             # The image is linear in every texel (sampling is detached), so the
             # loss is quadratic in it and the central difference is exact at
-            # any step; the step is 1e-3 relative to the texel so that bright
-            # texels (the sun lobe reaches 5e4) move the float32 path
-            # radiance by more than its rounding.
+            # any step, up to the float32 rounding of each path's radiance: a
+            # texel moved by 1e-3 changes a path that also carries the sun
+            # (5e4) by less than that rounding.  The step is therefore 0.1 x
+            # max(1, texel).
             idx = int(rng.choice(nz_env))
-            step = h * max(1.0, abs(float(env0.ravel()[idx])))
+            step = env_step * max(1.0, abs(float(env0.ravel()[idx])))
             e1 = env0.copy().ravel(); e1[idx] += step
             e2 = env0.copy().ravel(); e2[idx] -= step
             lp = (dict(env=e1.reshape(env0.shape)), dict(env=e2.reshape(env0.shape)))
@@ -644,7 +665,8 @@ def run_adjoint_study(args) -> dict:
     paths = 512 * 512 * spp
     return {
         "study": "adjoint gradients vs central finite differences, fBm heightfield",
-        "fd_step": "1e-3 for albedo offsets and roughness; 1e-3 x max(1, texel) for environment texels",
+        "fd_step": "1e-3 for albedo offsets and roughness; 0.1 x max(1, texel) for environment texels (exact: the "
+                   "loss is quadratic in a texel)",
         "workload": f"terrain {desc.ntris} tris, {nm} materials, env 512x256, 512x512, depth {depth}",
         "loss": loss, "spp": spp, "target_spp": 256,
         "primal_s": primal_s, "adjoint_s": adjoint_s, "target_s": target_s,
@@ -925,6 +947,8 @@ def main() -> None:
     ap.add_argument("--guide", choices=["mlp", "quadtree", "pss"], default="mlp")
     ap.add_argument("--metric", choices=["robust", "plain"], default="robust")
     ap.add_argument("--train-frames", type=int, default=64)
+    ap.add_argument("--mlp-schedule", choices=["frames", "waves"], default="frames",
+                    help="learned guide: train on one-sample frames first, or on the render's own wavefronts")
     ap.add_argument("--mlp-lr", type=float, default=5e-3)
     ap.add_argument("--mlp-decay", type=float, default=0.998)
     ap.add_argument("--mlp-steps", type=int, default=4)
