@@ -478,28 +478,19 @@ def run_relmse_study(args) -> dict:
     train_ms = 0.0
     train_spp = 0
     extra = {}
-    waves = args.guide == "mlp" and args.mlp_schedule == "waves"
     if args.guide == "mlp":
+        # Learned guide: online training on the first `train_frames` frames
+        # (`mlp_steps` Adam steps per frame, batch 2^18), which stay in the image.
         ctx.mlp_init(3)
         ctx.mlp_configure(lr=args.mlp_lr, decay=args.mlp_decay, batch=1 << 18, steps=args.mlp_steps,
                           direct=not args.mlp_indirect)
         mode = abi.MODE_GUIDED_MLP
-        extra = {"schedule": args.mlp_schedule, "lr": args.mlp_lr, "lr_decay": args.mlp_decay,
-                 "guide_depth": args.guide_depth, "target": "indirect" if args.mlp_indirect else "full incident radiance"}
-        if waves:
-            # Learned guide trained on the render's own wavefronts: calls of
-            # 1, 1, 2, 2, 4, 4, ... frames up to the chunk size, then chunks;
-            # after every call `mlp_steps` Adam steps on samples of its first
-            # 2^21 paths, while the frame count is below train_frames.  All of
-            # it is timed and stays in the image.
-            extra.update(adam_steps_per_wave=args.mlp_steps, train_until_spp=args.train_frames)
-        else:
-            # Learned guide: online training on the first `train_frames` frames
-            # (`mlp_steps` Adam steps per frame, batch 2^18), which stay in the image.
-            train_ms = render_ms(args.train_frames, mode, 13, guide_fraction=args.guide_fraction, train_guide=True,
-                                 guide_depth=args.guide_depth)
-            train_spp = args.train_frames
-            extra.update(train_frames=args.train_frames, adam_steps_per_frame=args.mlp_steps)
+        train_ms = render_ms(args.train_frames, mode, 13, guide_fraction=args.guide_fraction, train_guide=True,
+                             guide_depth=args.guide_depth)
+        train_spp = args.train_frames
+        extra = {"train_frames": args.train_frames, "lr": args.mlp_lr, "lr_decay": args.mlp_decay,
+                 "adam_steps_per_frame": args.mlp_steps, "guide_depth": args.guide_depth,
+                 "target": "indirect" if args.mlp_indirect else "full incident radiance"}
     else:
         # QuadTree (directions) or PSS (primary samples): train the cache over
         # `train_iters` iterations of 1, 2, 4, ... frames (the first unguided,
@@ -521,20 +512,10 @@ def run_relmse_study(args) -> dict:
     reached_ms = None
     chunk = max(1, args.plain_spp // 32)
     total = train_spp if args.guide == "mlp" else 0
-    ramp = [1, 1, 2, 2, 4, 4, 8, 8, 16, 16]
-    calls = 0
     while total < 4 * args.plain_spp:
-        if waves:
-            n = min(ramp[calls], chunk) if calls < len(ramp) else chunk
-            train = total < args.train_frames
-            guided_ms += render_ms(n, mode, 17 + total, guide_fraction=args.guide_fraction,
-                                   guide_depth=args.guide_depth, train_guide=train, train_waves=train)
-            calls += 1
-            total += n
-        else:
-            guided_ms += render_ms(chunk, mode, 17 + total, guide_fraction=args.guide_fraction,
-                                   guide_depth=args.guide_depth)
-            total += chunk
+        guided_ms += render_ms(chunk, mode, 17 + total, guide_fraction=args.guide_fraction,
+                               guide_depth=args.guide_depth)
+        total += chunk
         img = image()
         err = metric(img, ref)
         curve.append((total, train_ms + guided_ms, err, other(img, ref)))
@@ -629,9 +610,9 @@ def run_adjoint_study(args) -> dict:
             # The image is linear in every texel (sampling is detached), so the
             # loss is quadratic in it and the central difference is exact at
             # any step, up to the float32 rounding of each path's radiance: a
-            # texel moved by 1e-3 changes a path that also carries the sun
-            # (5e4) by less than that rounding.  The step is therefore 0.1 x
-            # max(1, texel).
+            # dim texel moved by 1e-3 changes a path that also carries the
+            # sun lobe by little more than that rounding.  The step is
+            # therefore 0.1 x max(1, texel).
             idx = int(rng.choice(nz_env))
             step = env_step * max(1.0, abs(float(env0.ravel()[idx])))
             e1 = env0.copy().ravel(); e1[idx] += step
@@ -640,33 +621,53 @@ def run_adjoint_study(args) -> dict:
             g = float(g_env.ravel()[idx]); name = f"env[{idx}]"
         elif k == 1:
             m, c = int(rng.choice(used)), int(rng.integers(3))
-            a = np.zeros((nm, 3), np.float32); a[m, c] = h
-            lp = (dict(albedo_offset=a), dict(albedo_offset=-a))
+
+            def lp_at(hh, m=m, c=c):
+                a = np.zeros((nm, 3), np.float32); a[m, c] = hh
+                return dict(albedo_offset=a), dict(albedo_offset=-a)
             g = float(g_alb[m, c]); name = f"albedo[{m},{c}]"
         else:
             m = int(rng.choice(used))
-            r1 = rough0.copy(); r1[m] += h
-            r2 = rough0.copy(); r2[m] -= h
-            lp = (dict(roughness=r1), dict(roughness=r2))
+
+            def lp_at(hh, m=m):
+                r1 = rough0.copy(); r1[m] += hh
+                r2 = rough0.copy(); r2[m] -= hh
+                return dict(roughness=r1), dict(roughness=r2)
             g = float(g_rough[m]); name = f"roughness[{m}]"
-        vals = []
-        for kw in lp:
-            ctx.diff_set_params(**kw)
-            vals.append(float(np.sum((ctx.diff_render(spp, seed, depth) - target) ** 2)))
-        res.append((name, (vals[0] - vals[1]) / (2 * step), g))
+
+        def central(pair, st):
+            vals = []
+            for kw in pair:
+                ctx.diff_set_params(**kw)
+                vals.append(float(np.sum((ctx.diff_render(spp, seed, depth) - target) ** 2)))
+            return (vals[0] - vals[1]) / (2 * st)
+
+        if k == 0:
+            res.append((name, central(lp, step), g, None))
+        else:
+            # Albedo and roughness enter the image nonlinearly (GGX D and G
+            # in roughness; products of albedos along a path), so the
+            # central difference carries an h^2 truncation term; Richardson
+            # extrapolation of the differences at h and h/2 cancels it.
+            d1 = central(lp_at(h), h)
+            d2 = central(lp_at(h / 2), h / 2)
+            res.append((name, (4.0 * d2 - d1) / 3.0, g, d1))
     fd_s = time.perf_counter() - t0
     ctx.diff_set_params()
     ctx.close()
     fd = np.array([r[1] for r in res])
     ad = np.array([r[2] for r in res])
     rel = np.abs(ad - fd) / np.maximum(np.abs(fd), 1e-30)
+    # the plain h = 1e-3 central difference for albedo and roughness, beside
+    raw = np.array([r[3] if r[3] is not None else r[1] for r in res])
+    rel_raw = np.abs(ad - raw) / np.maximum(np.abs(raw), 1e-30)
     scale = np.abs(fd).max()
     significant = np.abs(fd) > 1e-3 * scale
     paths = 512 * 512 * spp
     return {
         "study": "adjoint gradients vs central finite differences, fBm heightfield",
-        "fd_step": "1e-3 for albedo offsets and roughness; 0.1 x max(1, texel) for environment texels (exact: the "
-                   "loss is quadratic in a texel)",
+        "fd_step": "albedo offsets and roughness: central differences at h = 1e-3 and 5e-4 combined by Richardson "
+                   "extrapolation; environment texels: 0.1 x max(1, texel) (exact: the loss is quadratic in a texel)",
         "workload": f"terrain {desc.ntris} tris, {nm} materials, env 512x256, 512x512, depth {depth}",
         "loss": loss, "spp": spp, "target_spp": 256,
         "primal_s": primal_s, "adjoint_s": adjoint_s, "target_s": target_s,
@@ -677,7 +678,8 @@ def run_adjoint_study(args) -> dict:
         "frac_within_1e-3_rel": float(np.mean(rel <= 1e-3)),
         "frac_significant_within_1e-3_rel": float(np.mean(rel[significant] <= 1e-3)),
         "n_significant": int(significant.sum()),
-        "worst": sorted(res, key=lambda r: -abs(r[2] - r[1]) / max(abs(r[1]), 1e-30))[:5],
+        "frac_significant_within_1e-3_rel_plain_h": float(np.mean(rel_raw[significant] <= 1e-3)),
+        "worst": [r[:3] for r in sorted(res, key=lambda r: -abs(r[2] - r[1]) / max(abs(r[1]), 1e-30))[:5]],
     }
 
 
@@ -947,8 +949,6 @@ def main() -> None:
     ap.add_argument("--guide", choices=["mlp", "quadtree", "pss"], default="mlp")
     ap.add_argument("--metric", choices=["robust", "plain"], default="robust")
     ap.add_argument("--train-frames", type=int, default=64)
-    ap.add_argument("--mlp-schedule", choices=["frames", "waves"], default="frames",
-                    help="learned guide: train on one-sample frames first, or on the render's own wavefronts")
     ap.add_argument("--mlp-lr", type=float, default=5e-3)
     ap.add_argument("--mlp-decay", type=float, default=0.998)
     ap.add_argument("--mlp-steps", type=int, default=4)

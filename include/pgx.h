@@ -215,12 +215,6 @@ typedef struct pgx_render_config {
 /* Per-stage CUDA-event times only: the kernels are the ones a render without
  * flags runs. */
 #define PGX_RENDER_TIMING 8
-/* With PGX_RENDER_TRAIN_GUIDE: train after every wavefront instead of every
- * frame.  The frames of the call render in waves of up to 2^25 paths (as a
- * render without training does) and the radiance samples of a wave come from
- * its first 2^21 paths (its first samples of every pixel); the caller sets
- * how often the guide learns by how many frames it passes per call. */
-#define PGX_RENDER_TRAIN_WAVES 16
 
 /* Statistics of the last pgx_render call.  The per-stage times are filled
  * with PGX_RENDER_PROFILE or PGX_RENDER_TIMING, the node/triangle fetch counts

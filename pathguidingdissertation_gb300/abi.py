@@ -28,7 +28,6 @@ NOALLOC_MAX_RAYS = 65536  # PGX_NOALLOC_MAX_RAYS
 MLP_PARAMS = 24424   # PGX_MLP_PARAMS
 MLP_OUTPUTS = 40     # PGX_MLP_OUTPUTS
 RENDER_TRAIN_GUIDE = 4
-RENDER_TRAIN_WAVES = 16
 # pgx_radiance_sample: position, normal, wo, wi, weight
 RADIANCE_SAMPLE = np.dtype([("position", "<f4", 3), ("normal", "<f4", 3), ("wo", "<f4", 3), ("wi", "<f4", 3),
                             ("weight", "<f4")])

@@ -137,15 +137,11 @@ class Context:
 
     def render(self, frames: int = 1, mode: int = abi.MODE_PLAIN, seed: int = 1, max_depth: int = 8,
                guide_fraction: float = 0.5, record_paths: int | bool = 0, profile: bool = False,
-               mitchell: bool = False, train_guide: bool = False, guide_depth: int = 0, timing: bool = False,
-               train_waves: bool = False) -> None:
+               mitchell: bool = False, train_guide: bool = False, guide_depth: int = 0, timing: bool = False) -> None:
         """profile: per-stage times and traversal counters (counting kernels);
-        timing: per-stage times only (the kernels of an unflagged render);
-        train_guide: online training of the learned guide after every frame,
-        or after every wavefront with train_waves."""
+        timing: per-stage times only (the kernels of an unflagged render)."""
         flags = (abi.RENDER_PROFILE if profile else 0) | (abi.RENDER_FILTER_MITCHELL if mitchell else 0) | \
-            (abi.RENDER_TRAIN_GUIDE if train_guide else 0) | (abi.RENDER_TIMING if timing else 0) | \
-            (abi.RENDER_TRAIN_WAVES if train_waves else 0)
+            (abi.RENDER_TRAIN_GUIDE if train_guide else 0) | (abi.RENDER_TIMING if timing else 0)
         cfg = abi.RenderConfig(mode, max_depth, seed, guide_fraction, int(record_paths), flags, guide_depth)
         self.check(self.lib.pgx_render(self.h, C.byref(cfg), frames))
 

@@ -81,7 +81,6 @@ struct PathState {
     pgx_path_vertex* vertices;
     unsigned* nvertices;
     int64_t capacity;
-    int64_t rcap;      // paths [0, rcap) of a wave keep per-depth records (all of them except when training only)
     int64_t vcapacity;
     // learned guide: per-path mixture (10 float4), training records
     float4* guide;
@@ -99,12 +98,11 @@ struct RenderState {
     DevBuf counters, vertices, cqueue, ccount;
     DevBuf guide, rec_wo, rec_f, train, scene;
     int64_t capacity = 0;
-    int64_t rcap = 0;      // paths with per-depth records (record arrays hold rec_depth x rcap entries)
     int rec_depth = 0;
     int64_t guide_capacity = 0;
     int train_depth = 0;
     int64_t tcapacity = 0;
-    double train_last = 0.0;  // radiance samples per recorded path in the previous wave
+    int64_t train_last = 0;   // samples the previous batch produced
     int64_t vcapacity = 0;
     int64_t nvertices_last = 0;
     // captured frame graph
@@ -691,6 +689,7 @@ __global__ void __launch_bounds__(kThreads, kShadeBlocksPerSM) k_shade(SceneView
     const unsigned n = cls < 0 ? ps.qcount[depth] : ps.ccount[depth * kShadeClasses + cls];
     const int* __restrict__ q = cls < 0 ? ps.queue[depth & 1] : ps.cqueue + (size_t)cls * ps.capacity;
     int* __restrict__ qn = ps.queue[(depth + 1) & 1];
+    const int64_t cap = ps.capacity;
     // Uniform trip count per warp so the warp-aggregated appends see whole warps.
     const unsigned stride = gridDim.x * blockDim.x;
     const unsigned first = blockIdx.x * blockDim.x + threadIdx.x;
@@ -724,7 +723,7 @@ __global__ void __launch_bounds__(kThreads, kShadeBlocksPerSM) k_shade(SceneView
         // baseline from which k_finalize recovers that vertex's incident Li.
         const int sample_of_p = fp.spp0 + (int)(p / ((int64_t)sv.width * sv.height));
         const bool rec_on = MODE != PGX_MODE_GUIDED_LI && active && sample_of_p >= fp.collect_lo &&
-                            sample_of_p < fp.collect_hi && p < ps.rcap;
+                            sample_of_p < fp.collect_hi;
         // (written below, after this vertex's emission is known)
         if (active) {
             float4 o = ps.o[p], d = ps.d[p], h = ps.hit[p], Tw = ps.T[p];
@@ -885,7 +884,7 @@ __global__ void __launch_bounds__(kThreads, kShadeBlocksPerSM) k_shade(SceneView
                 }
             }
             if (MODE == PGX_MODE_GUIDED_LI) {
-                size_t ri = (size_t)depth * ps.rcap + p;
+                size_t ri = (size_t)depth * cap + p;
                 ps.rec_pos[ri] = make_float4(r_pos.x, r_pos.y, r_pos.z, r_store ? 1.f : 0.f);
                 ps.rec_nrm[ri] = make_float4(r_nrm.x, r_nrm.y, r_nrm.z, 0.f);
                 ps.rec_wi[ri] = make_float4(r_wi.x, r_wi.y, r_wi.z, 0.f);
@@ -902,12 +901,12 @@ __global__ void __launch_bounds__(kThreads, kShadeBlocksPerSM) k_shade(SceneView
                     // emission on (snapshot before it); the indirect-only
                     // target of the learned guide starts after it.
                     if (snap)
-                        ps.rec_e[(size_t)(depth - 1) * ps.rcap + p] =
+                        ps.rec_e[(size_t)(depth - 1) * cap + p] =
                             fp.train == 1 ? make_float4(l.x + add.x, l.y + add.y, l.z + add.z, 0.f) : l;
                     if (adds) ps.L[p] = make_float4(l.x + add.x, l.y + add.y, l.z + add.z, 0.f);
                 }
                 if (rec_on) {
-                    size_t ri = (size_t)depth * ps.rcap + p;
+                    size_t ri = (size_t)depth * cap + p;
                     ps.rec_pos[ri] = make_float4(r_pos.x, r_pos.y, r_pos.z, (cont && r_store) ? 1.f : 0.f);
                     if (cont && r_store) {
                         ps.rec_nrm[ri] = make_float4(r_nrm.x, r_nrm.y, r_nrm.z, 0.f);
@@ -1028,7 +1027,7 @@ __global__ void __launch_bounds__(kThreads) k_finalize(SceneView sv, PathState p
             int nr = ps.nrec[p];
             F3 li = zero3();
             for (int i = nr - 1; i >= 0; i--) {
-                size_t ri = (size_t)i * ps.rcap + p;
+                size_t ri = (size_t)i * ps.capacity + p;
                 float4 pos = ps.rec_pos[ri];
                 if (collect && pos.w != 0.f && valid(li) && lum(li) > 0.f) {
                     unsigned slot = atomicAdd(ps.nvertices, 1u);
@@ -1055,12 +1054,12 @@ __global__ void __launch_bounds__(kThreads) k_finalize(SceneView sv, PathState p
             col = li;
         } else {
             col = f3(ps.L[p]);
-            if (collect && p < ps.rcap && valid(col)) {
+            if (collect && valid(col)) {
                 // Incident radiance along each recorded wi: what the path gathered
                 // after that vertex, divided by the throughput it carried.
                 int nr = ps.nrec[p];
                 for (int i = 0; i < nr; i++) {
-                    size_t ri = (size_t)i * ps.rcap + p;
+                    size_t ri = (size_t)i * ps.capacity + p;
                     float4 pos = ps.rec_pos[ri];
                     if (pos.w == 0.f) continue;
                     F3 tn = f3(ps.rec_w[ri]);
@@ -1603,8 +1602,7 @@ RenderState* state_of(pgx_ctx* ctx) {
 }
 
 int ensure_state(pgx_ctx* ctx, RenderState* rs, int64_t cap, int rec_depth, int64_t vcap, bool guide = false,
-                 int train_depth = 0, int64_t tcap = 0, bool batch = false, int64_t rcap = -1) {
-    if (rcap < 0 || rcap > cap) rcap = cap;
+                 int train_depth = 0, int64_t tcap = 0, bool batch = false) {
     if (cap > rs->capacity) {
         PGX_CUDA_TRY(ctx, rs->o.reserve(sizeof(float4) * cap));
         PGX_CUDA_TRY(ctx, rs->d.reserve(sizeof(float4) * cap));
@@ -1624,8 +1622,8 @@ int ensure_state(pgx_ctx* ctx, RenderState* rs, int64_t cap, int rec_depth, int6
         rs->capacity = cap;
         rs->rec_depth = 0;
     }
-    if (rec_depth > 0 && (rec_depth > rs->rec_depth || rs->rec_pos.bytes < sizeof(float4) * rec_depth * (size_t)rcap)) {
-        size_t nrec = (size_t)rec_depth * rcap;
+    if (rec_depth > rs->rec_depth) {
+        size_t nrec = (size_t)rec_depth * rs->capacity;
         PGX_CUDA_TRY(ctx, rs->rec_pos.reserve(sizeof(float4) * nrec));
         PGX_CUDA_TRY(ctx, rs->rec_nrm.reserve(sizeof(float4) * nrec));
         PGX_CUDA_TRY(ctx, rs->rec_wi.reserve(sizeof(float4) * nrec));
@@ -1641,9 +1639,8 @@ int ensure_state(pgx_ctx* ctx, RenderState* rs, int64_t cap, int rec_depth, int6
         PGX_CUDA_TRY(ctx, rs->guide.reserve(sizeof(float4) * mlp::kPacked * rs->capacity));
         rs->guide_capacity = rs->capacity;
     }
-    rs->rcap = rcap;
-    if (train_depth > 0 && (train_depth > rs->train_depth || rs->rec_wo.bytes < sizeof(float4) * train_depth * (size_t)rcap)) {
-        size_t nrec = (size_t)train_depth * rcap;
+    if (train_depth > 0 && (train_depth > rs->train_depth || rs->rec_wo.bytes < sizeof(float4) * train_depth * rs->capacity)) {
+        size_t nrec = (size_t)train_depth * rs->capacity;
         PGX_CUDA_TRY(ctx, rs->rec_wo.reserve(sizeof(float4) * nrec));
         PGX_CUDA_TRY(ctx, rs->rec_f.reserve(sizeof(float4) * nrec));
         rs->train_depth = train_depth;
@@ -1697,7 +1694,6 @@ PathState path_view(RenderState* rs) {
     ps.nvertices = c + 4 * (kMaxDepthCap + 2) + 2 * kStats;
     ps.vertices = rs->vertices.as<pgx_path_vertex>();
     ps.capacity = rs->capacity;
-    ps.rcap = rs->rcap;
     ps.vcapacity = rs->vcapacity;
     ps.guide = rs->guide.as<float4>();
     ps.rec_wo = rs->rec_wo.as<float4>();
@@ -1907,21 +1903,15 @@ extern "C" int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t fr
     // each, 6.4 GB): the depths where the queues have shrunk cost about the
     // same per wave whatever its size, so large waves amortise them (measured
     // on the 1280x720 interior: 1,726 Mrays/s at 4 spp per wave, 1,903 at 8,
-    // 1,998 at 16, 2,041 at 32).  Recording every path (guided-Li, the cache)
-    // bounds waves at 2^21 paths (per-depth vertex records cost 80 bytes per
-    // path and depth).  Training the learned guide needs records only for a
-    // sample of the radiance: its waves keep the full size and record the
-    // first 2^21 paths of each wave (paths are sample-major, so these are
-    // the wave's first samples of every pixel).
-    const int64_t kRecordPaths = (int64_t)1 << 21;
-    const int64_t target_paths = (guided_li || recording) ? kRecordPaths : ((int64_t)1 << 25);
+    // 1,998 at 16, 2,041 at 32).  Recording is bounded at 2^21 paths (per-depth
+    // vertex records cost 80 bytes per path and depth).
+    const int64_t target_paths = rec_depth ? (int64_t)(1 << 21) : (int64_t)(1 << 25);
     int batch = (int)std::max<int64_t>(1, std::min<int64_t>(frames, target_paths / std::max<int64_t>(npix, 1)));
-    if (train && !(cfg->flags & PGX_RENDER_TRAIN_WAVES)) batch = 1;  // one round of Adam steps after every frame
-    const int64_t rcap = (train && !guided_li && !recording) ? std::min<int64_t>(npix * batch, kRecordPaths) : npix * batch;
+    if (train) batch = 1;  // one round of Adam steps after every frame
     const int64_t vcap = recording ? npix * (cfg->max_depth + 1) * (collect_hi - collect_lo) : 0;
     const bool mlp_mode = cfg->mode == PGX_MODE_GUIDED_MLP;
     const int64_t tcap = train ? mlp_train_batch(ctx) : 0;
-    PGX_TRY(ensure_state(ctx, rs, npix * batch, rec_depth, vcap, mlp_mode, train ? rec_depth : 0, tcap, false, rcap));
+    PGX_TRY(ensure_state(ctx, rs, npix * batch, rec_depth, vcap, mlp_mode, train ? rec_depth : 0, tcap));
     if (mlp_mode)
         PGX_CUDA_TRY(ctx, cudaFuncSetAttribute(k_guide_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, kInferSmem));
     cudaStream_t s = ctx->stream;
@@ -1950,20 +1940,17 @@ extern "C" int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t fr
         fp.guide_depth = cfg->guide_depth > 0 ? cfg->guide_depth : kMaxDepthCap + 1;
         fp.train_keep = 1.f;
         if (train && rs->train_last > 0)
-            fp.train_keep = (float)std::min(1.0, (double)tcap / (1.25 * rs->train_last *
-                                                                  (double)std::min<int64_t>(npix * fp.batch, rcap)));
+            fp.train_keep = (float)std::min(1.0, (double)tcap / (1.25 * (double)rs->train_last * fp.batch));
         if (train) PGX_CUDA_TRY(ctx, cudaMemsetAsync(ps.ntrain, 0, sizeof(unsigned), s));
         launches += enqueue_frame(ctx, rs, fp, s, mlp_status);
         batches++;
         PGX_CUDA_TRY(ctx, cudaGetLastError());
         if (train) {
-            // `steps` Adam steps on this wave's radiance samples
+            // one Adam step on this batch's radiance samples
             unsigned nt = 0;
             PGX_CUDA_TRY(ctx, cudaMemcpyAsync(&nt, ps.ntrain, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
             PGX_CUDA_TRY(ctx, cudaStreamSynchronize(s));
-            // radiance samples per recorded path, for the next wave's keep share
-            rs->train_last = (double)nt / std::max(fp.train_keep, 1e-6f) /
-                             (double)std::min<int64_t>(npix * fp.batch, rcap);
+            rs->train_last = (int64_t)((double)nt / std::max(fp.train_keep, 1e-6f) / fp.batch);
             PGX_TRY(mlp_online_step(ctx, ps.train, std::min<int64_t>(nt, tcap)));
             launches += 4;
         }
