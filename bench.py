@@ -237,6 +237,11 @@ def run_pgx(args) -> dict:
     else:
         ranks.barrier()
     desc, depth, wl = make_workload(args.workload)
+    if args.res:
+        # a reduced image of the same scene (for profiler captures)
+        w, h = (int(x) for x in args.res.split("x"))
+        desc.camera = dict(desc.camera, width=w, height=h)
+        wl = f"{wl}, image reduced to {args.res}"
     mode = {"plain": abi.MODE_PLAIN, "guided_quadtree": abi.MODE_GUIDED_QUADTREE,
             "guided_mlp": abi.MODE_GUIDED_MLP}[args.mode]
     seed = 1 + 1000003 * ranks.rank  # each replica renders its own samples
@@ -937,6 +942,7 @@ def main() -> None:
     ap.add_argument("--workload", choices=["interior", "cornell"], default="interior")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-side-modes", action="store_true", help="skip the guided and depth-8 side measurements")
+    ap.add_argument("--res", default=None, help="WxH: render the workload at this image size (profiler captures)")
     ap.add_argument("--spp-per-step", type=int, default=32,
                     help="samples per pixel of one step: one pgx_render call, one wavefront")
     ap.add_argument("--study", choices=["relmse", "traversal", "adjoint", "batch"], default=None,
