@@ -538,6 +538,9 @@ typedef struct pgx_batch_tuning {
     int64_t wave_paths;           /* queue capacity: paths per wave            */
     int32_t trace_blocks_per_sm;  /* persistent traversal blocks per SM (1-8)  */
     int32_t shade_blocks_per_sm;  /* camera / shade / splat blocks per SM      */
+    int32_t stack_shared;         /* traversal stack entries kept in shared
+                                     memory (4, 8 or 16 of the 64; the rest
+                                     spill to local memory)                     */
 } pgx_batch_tuning;
 
 typedef struct pgx_batch_stats {
@@ -552,10 +555,12 @@ int pgx_batch_create(pgx_ctx* const* scenes, int32_t n, pgx_batch** out);
 int pgx_batch_destroy(pgx_batch* batch);
 /* Adds spp samples per pixel to every scene's film. */
 int pgx_batch_render(pgx_batch* batch, int32_t spp, uint64_t seed, int32_t max_depth);
-/* Times every candidate tuning (wave capacity 1M-32M paths, traversal and
- * shading grid sizes) on `spp` samples of the batch into a scratch film
- * (the scenes' films are not touched), keeps the fastest and returns it.
- * The traversal stack depth is fixed at 64 entries, as in the reference. */
+/* Times candidate tunings on `spp` samples of the batch into a scratch film
+ * (the scenes' films are not touched), keeps the fastest and returns it:
+ * every wave capacity (1M-32M paths) x traversal and shading grid size with
+ * the default stack split, then the shared-memory part of the traversal
+ * stack (4, 8 or 16 of its 64 entries, the reference's depth) at the best
+ * of those. */
 int pgx_batch_autotune(pgx_batch* batch, int32_t spp, int32_t max_depth, pgx_batch_tuning* best);
 int pgx_batch_set_tuning(pgx_batch* batch, const pgx_batch_tuning* tuning);
 int pgx_batch_get_stats(pgx_batch* batch, pgx_batch_stats* stats);

@@ -108,7 +108,8 @@ class CacheStats(C.Structure):
 
 
 class BatchTuning(C.Structure):
-    _fields_ = [("wave_paths", C.c_int64), ("trace_blocks_per_sm", C.c_int32), ("shade_blocks_per_sm", C.c_int32)]
+    _fields_ = [("wave_paths", C.c_int64), ("trace_blocks_per_sm", C.c_int32), ("shade_blocks_per_sm", C.c_int32),
+                ("stack_shared", C.c_int32)]
 
 
 class BatchStats(C.Structure):

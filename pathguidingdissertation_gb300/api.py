@@ -359,8 +359,9 @@ class Batch:
         self.check(self.lib.pgx_batch_autotune(self.h, spp, max_depth, C.byref(t)))
         return t
 
-    def set_tuning(self, wave_paths: int, trace_blocks_per_sm: int, shade_blocks_per_sm: int) -> None:
-        t = abi.BatchTuning(wave_paths, trace_blocks_per_sm, shade_blocks_per_sm)
+    def set_tuning(self, wave_paths: int, trace_blocks_per_sm: int, shade_blocks_per_sm: int,
+                   stack_shared: int = 8) -> None:
+        t = abi.BatchTuning(wave_paths, trace_blocks_per_sm, shade_blocks_per_sm, stack_shared)
         self.check(self.lib.pgx_batch_set_tuning(self.h, C.byref(t)))
 
     def stats(self) -> abi.BatchStats:

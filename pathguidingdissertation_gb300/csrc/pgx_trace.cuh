@@ -149,21 +149,26 @@ __device__ __forceinline__ bool bvh_trace(const BvhView& bvh, const xv3& o, cons
 }
 
 // ---- persistent traversal with lane refill ----------------------------------
-// Stack of one lane of the persistent traversal: the top kShortStack entries
-// live in shared memory (one column per thread of the block, so a warp's
-// accesses fall in distinct banks), deeper ones spill to local memory.
+// Stack of one lane of the persistent traversal (PGX_STACK_SIZE entries, the
+// reference's depth): the top SHORT entries live in shared memory (one column
+// per thread of the block, so a warp's accesses fall in distinct banks),
+// deeper ones spill to local memory.  SHORT trades shared memory (8 bytes x
+// 128 threads per entry, so resident blocks) against local-memory traffic;
+// the batch autotuner picks it from kShortStackChoices.
 constexpr int kShortStack = 8;
+constexpr int kShortStackChoices[] = {4, 8, 16};
 constexpr int kTraceMaxBlock = 128;  // block size of every kernel using trace_persistent
+template <int SHORT = kShortStack>
 struct TraceStack {
     int2* sh;  // this thread's column: entry i at sh[i * kTraceMaxBlock]
-    int2 loc[PGX_STACK_SIZE - kShortStack];
+    int2 loc[PGX_STACK_SIZE - SHORT];
     __device__ __forceinline__ void put(int i, int2 v) {
-        if (i < kShortStack)
+        if (i < SHORT)
             sh[i * kTraceMaxBlock] = v;
         else
-            loc[i - kShortStack] = v;
+            loc[i - SHORT] = v;
     }
-    __device__ __forceinline__ int2 get(int i) const { return i < kShortStack ? sh[i * kTraceMaxBlock] : loc[i - kShortStack]; }
+    __device__ __forceinline__ int2 get(int i) const { return i < SHORT ? sh[i * kTraceMaxBlock] : loc[i - SHORT]; }
 };
 
 // The same per-ray algorithm as bvh_trace, cut into steps (one interior node
@@ -213,8 +218,8 @@ struct SceneRoot {
 
 // One step; returns true when the ray is finished (for ANY, hit_id >= 0
 // marks an occluder).
-template <bool ANY, bool COUNT>
-__device__ __forceinline__ bool lane_step(const BvhView& bvh, TraceLane& L, TraceStack& stack, unsigned long long& n_interior,
+template <bool ANY, bool COUNT, class Stack>
+__device__ __forceinline__ bool lane_step(const BvhView& bvh, TraceLane& L, Stack& stack, unsigned long long& n_interior,
                                           unsigned long long& n_tris) {
     if (L.cnt > 0) {
         if ((unsigned)L.ref > (unsigned)bvh.n_tris || L.cnt > bvh.n_tris - L.ref) {
@@ -309,7 +314,7 @@ __device__ __forceinline__ bool lane_step(const BvhView& bvh, TraceLane& L, Trac
 // `store(i, lane)` consumes a finished ray, `root_of(i, bvh)` gives the tree
 // root ray i starts from (several trees can share the node and triangle
 // arrays).  `next` is a zeroed counter.  Must be called by whole warps.
-template <bool ANY, bool COUNT, class Load, class Store, class RootOf = SceneRoot>
+template <bool ANY, bool COUNT, class Load, class Store, class RootOf = SceneRoot, int SHORT = kShortStack>
 __device__ __forceinline__ void trace_persistent(const BvhView& bvh, unsigned n, unsigned* next, Load load,
                                                  Store store, unsigned long long& n_interior,
                                                  unsigned long long& n_tris, unsigned& status_or,
@@ -319,8 +324,8 @@ __device__ __forceinline__ void trace_persistent(const BvhView& bvh, unsigned n,
     constexpr int kMaxSteps = 64;
     constexpr int kCheckEvery = 8;    // steps between occupancy votes
     const int lane = threadIdx.x & 31;
-    __shared__ int2 s_stack[kShortStack * kTraceMaxBlock];
-    TraceStack stack;
+    __shared__ int2 s_stack[SHORT * kTraceMaxBlock];
+    TraceStack<SHORT> stack;
     stack.sh = s_stack + threadIdx.x;
     TraceLane L;
     int ray = -1;

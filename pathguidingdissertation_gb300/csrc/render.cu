@@ -282,7 +282,7 @@ constexpr int kPersistentBlocksPerSM = 8;
 
 // Closest hit for the queue of this depth: persistent warps with lane refill
 // (trace_persistent) over qcount[depth] rays.
-template <bool COUNT, bool BATCH = false>
+template <bool COUNT, bool BATCH = false, int SHORT = kShortStack>
 __global__ void __launch_bounds__(kThreads, kPersistentBlocksPerSM) k_extend(SceneView sv, PathState ps, int depth,
                                                                             const BatchInfo* binfo = nullptr) {
     const unsigned n = ps.qcount[depth];
@@ -302,8 +302,8 @@ __global__ void __launch_bounds__(kThreads, kPersistentBlocksPerSM) k_extend(Sce
         ps.hit[p] = make_float4(__int_as_float(id), L.tmax, L.hu, L.hv);
     };
     if (BATCH)
-        trace_persistent<false, COUNT>(sv.bvh, n, &ps.wcount[depth], load, store, ni, nt, status,
-                                       BatchRoot{binfo, ps.scene, q});
+        trace_persistent<false, COUNT, decltype(load), decltype(store), BatchRoot, SHORT>(
+            sv.bvh, n, &ps.wcount[depth], load, store, ni, nt, status, BatchRoot{binfo, ps.scene, q});
     else
         trace_persistent<false, COUNT>(sv.bvh, n, &ps.wcount[depth], load, store, ni, nt, status);
     if (COUNT) add_counts(&ps.stats[2], ni, nt);
@@ -312,7 +312,7 @@ __global__ void __launch_bounds__(kThreads, kPersistentBlocksPerSM) k_extend(Sce
 
 // Any hit for the shadow queue of this depth; unoccluded rays add their
 // contribution to the path's radiance.
-template <bool COUNT, bool BATCH = false>
+template <bool COUNT, bool BATCH = false, int SHORT = kShortStack>
 __global__ void __launch_bounds__(kThreads, kPersistentBlocksPerSM) k_shadow(SceneView sv, PathState ps, int depth,
                                                                             const BatchInfo* binfo = nullptr) {
     const unsigned n = ps.scount[depth];
@@ -333,8 +333,9 @@ __global__ void __launch_bounds__(kThreads, kPersistentBlocksPerSM) k_shadow(Sce
         }
     };
     if (BATCH)
-        trace_persistent<true, COUNT>(sv.bvh, n, &ps.wcount[kMaxDepthCap + 2 + depth], load, store, ni, nt, status,
-                                      BatchRoot{binfo, ps.scene, ps.sh_path});
+        trace_persistent<true, COUNT, decltype(load), decltype(store), BatchRoot, SHORT>(
+            sv.bvh, n, &ps.wcount[kMaxDepthCap + 2 + depth], load, store, ni, nt, status,
+            BatchRoot{binfo, ps.scene, ps.sh_path});
     else
         trace_persistent<true, COUNT>(sv.bvh, n, &ps.wcount[kMaxDepthCap + 2 + depth], load, store, ni, nt, status);
     if (COUNT) add_counts(&ps.stats[4], ni, nt);
@@ -2245,7 +2246,7 @@ struct pgx_batch {
     pgx_ctx* host = nullptr;        // merged arrays, stream, error text, path state
     std::vector<BatchInfo> info;    // per scene (roots and bases fixed at creation)
     DevBuf d_info, d_prefix, d_seed;
-    pgx_batch_tuning tuning{1 << 24, 8, 16};
+    pgx_batch_tuning tuning{1 << 24, 8, 16, kShortStack};
     pgx_batch_stats stats{};
     cudaGraphExec_t graph = nullptr;
     int g_spp = -1, g_depth = -1;
@@ -2267,8 +2268,11 @@ int batch_fail(pgx_batch* b, int code, const char* fmt, ...) {
 }
 
 bool tuning_ok(const pgx_batch_tuning& t) {
+    bool stack_ok = false;
+    for (int c : kShortStackChoices) stack_ok |= t.stack_shared == c;
     return t.wave_paths >= (1 << 16) && t.wave_paths <= (1LL << 25) && t.trace_blocks_per_sm >= 1 &&
-           t.trace_blocks_per_sm <= kPersistentBlocksPerSM && t.shade_blocks_per_sm >= 1 && t.shade_blocks_per_sm <= 16;
+           t.trace_blocks_per_sm <= kPersistentBlocksPerSM && t.shade_blocks_per_sm >= 1 && t.shade_blocks_per_sm <= 16 &&
+           stack_ok;
 }
 
 // Per-scene tables for `spp` samples; films of the scenes, or one scratch
@@ -2316,11 +2320,19 @@ int batch_enqueue(pgx_batch* b, int64_t total, int depth, const pgx_batch_tuning
         cudaMemsetAsync(ps.ccount, 0, sizeof(unsigned) * kShadeClasses * (kMaxDepthCap + 2), s);
         k_camgen_batch<<<sg, kThreads, 0, s>>>(ps, bw);
         for (int d = 0; d <= depth; d++) {
-            k_extend<false, true><<<tg, kThreads, 0, s>>>(sv, ps, d, info);
+            switch (tu.stack_shared) {
+                case 4: k_extend<false, true, 4><<<tg, kThreads, 0, s>>>(sv, ps, d, info); break;
+                case 16: k_extend<false, true, 16><<<tg, kThreads, 0, s>>>(sv, ps, d, info); break;
+                default: k_extend<false, true, 8><<<tg, kThreads, 0, s>>>(sv, ps, d, info); break;
+            }
             k_classify<<<grid_for((bw.count + kClassifyItems - 1) / kClassifyItems), kThreads, 0, s>>>(sv, ps, d);
             for (int c = 0; c < kShadeClasses; c++)
                 launch_shade_class<PGX_MODE_PLAIN, true>(c, sg, s, sv, ps, fp, d, gv, info);
-            k_shadow<false, true><<<tg, kThreads, 0, s>>>(sv, ps, d, info);
+            switch (tu.stack_shared) {
+                case 4: k_shadow<false, true, 4><<<tg, kThreads, 0, s>>>(sv, ps, d, info); break;
+                case 16: k_shadow<false, true, 16><<<tg, kThreads, 0, s>>>(sv, ps, d, info); break;
+                default: k_shadow<false, true, 8><<<tg, kThreads, 0, s>>>(sv, ps, d, info); break;
+            }
         }
         k_finalize_batch<<<sg, kThreads, 0, s>>>(ps, bw);
     }
@@ -2541,25 +2553,32 @@ extern "C" int pgx_batch_autotune(pgx_batch* b, int32_t spp, int32_t max_depth, 
     const int shade_bps[] = {8, 16};
     float best_ms = 1e30f;
     pgx_batch_tuning pick = b->tuning;
+    auto trial = [&](const pgx_batch_tuning& t) -> int {
+        PGX_TRY(batch_state(b, t));
+        PGX_TRY(batch_enqueue(b, total, max_depth, t));  // warm-up
+        PGX_CUDA_TRY(h, cudaEventRecord(b->ev0, h->stream));
+        PGX_TRY(batch_enqueue(b, total, max_depth, t));
+        PGX_CUDA_TRY(h, cudaEventRecord(b->ev1, h->stream));
+        PGX_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        float ms = 0.f;
+        PGX_CUDA_TRY(h, cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+        if (ms < best_ms) {
+            best_ms = ms;
+            pick = t;
+        }
+        return PGX_OK;
+    };
+    // Queue capacity and block shapes at the default stack split, then the
+    // stack's shared-memory depth at the best of those.
     for (int64_t w : waves) {
         if (w > 2 * total && w != waves[0]) continue;  // larger waves than the work change nothing
         for (int tbp : trace_bps)
-            for (int sbp : shade_bps) {
-                pgx_batch_tuning t{w, tbp, sbp};
-                PGX_TRY(batch_state(b, t));
-                PGX_TRY(batch_enqueue(b, total, max_depth, t));  // warm-up
-                PGX_CUDA_TRY(h, cudaEventRecord(b->ev0, h->stream));
-                PGX_TRY(batch_enqueue(b, total, max_depth, t));
-                PGX_CUDA_TRY(h, cudaEventRecord(b->ev1, h->stream));
-                PGX_CUDA_TRY(h, cudaStreamSynchronize(h->stream));
-                float ms = 0.f;
-                PGX_CUDA_TRY(h, cudaEventElapsedTime(&ms, b->ev0, b->ev1));
-                if (ms < best_ms) {
-                    best_ms = ms;
-                    pick = t;
-                }
-            }
+            for (int sbp : shade_bps) PGX_TRY(trial(pgx_batch_tuning{w, tbp, sbp, kShortStack}));
     }
+    const pgx_batch_tuning shape = pick;
+    for (int sh : kShortStackChoices)
+        if (sh != kShortStack) PGX_TRY(trial(pgx_batch_tuning{shape.wave_paths, shape.trace_blocks_per_sm,
+                                                              shape.shade_blocks_per_sm, sh}));
     b->tuning = pick;
     if (best) *best = pick;
     return PGX_OK;

@@ -53,6 +53,7 @@ def test_autotune_keeps_films_and_tuning_applies(pgx_lib):
     b = Batch(ctxs)
     t = b.autotune(spp=1, max_depth=8)
     assert t.wave_paths >= 1 << 20 and 1 <= t.trace_blocks_per_sm <= 8 and t.shade_blocks_per_sm >= 1
+    assert t.stack_shared in (4, 8, 16)
     for c in ctxs:
         rgb, _, n = c.film()
         assert n == 0 and not rgb.any()
@@ -60,6 +61,20 @@ def test_autotune_keeps_films_and_tuning_applies(pgx_lib):
     b.render(2, seed=9)
     with pytest.raises(abi.PgxError):
         b.set_tuning(1 << 16, 100, 8)
+    with pytest.raises(abi.PgxError):
+        b.set_tuning(1 << 20, 8, 16, stack_shared=5)
+    # the stack's shared-memory depth changes where entries live, not the
+    # traversal: the same images
+    films = []
+    for sh in (4, 8, 16):
+        for c in ctxs:
+            c.clear()
+        b.set_tuning(1 << 20, 8, 16, stack_shared=sh)
+        b.render(2, seed=9)
+        films.append([c.film()[0].astype(np.float64) for c in ctxs])
+    for other in films[1:]:
+        for a, r in zip(other, films[0]):
+            assert _close(a, r) < 1e-5
     b.close()
     for c in ctxs:
         c.close()
