@@ -234,6 +234,8 @@ typedef struct pgx_render_stats {
     double ms_extend;
     double ms_shadow;
     double ms_shade;
+    int64_t guide_fallbacks;  /* learned-guide vertices guided by the QuadTree
+                                 instead (pgx_mlp_set_fallback)              */
 } pgx_render_stats;
 
 /* Reference `PathVertex` (Renderer.h:42-47) without the Vec4 w lanes. */
@@ -490,6 +492,15 @@ int pgx_mlp_train_step(pgx_ctx* ctx, const pgx_radiance_sample* samples, int64_t
  * continuation (the default); 0 leaves out the emission reached directly
  * from the vertex, which next-event estimation also samples. */
 int pgx_mlp_configure(pgx_ctx* ctx, float lr, float decay, int64_t batch, int32_t steps, int32_t direct);
+/* The QuadTree guide as the learned guide's fallback.  While a radiance
+ * cache with direction quadtrees exists (pgx_cache_build, or a render with
+ * record_paths), the radiance samples the network is trained on (online or
+ * pgx_mlp_train_step) are counted per cache region; in PGX_MODE_GUIDED_MLP a
+ * vertex whose region has fewer than min_samples of them is guided by the
+ * region's quadtree instead of the network (the same one-sample MIS with the
+ * BSDF).  A new network, new parameters or a rebuilt cache start every
+ * region at zero.  Default 256; 0 turns the fallback off. */
+int pgx_mlp_set_fallback(pgx_ctx* ctx, int32_t min_samples);
 
 /* ---- differentiable rendering (extension; the reference renders forward only) ----
  * Plain path tracing with NEE + MIS (PGX_MODE_PLAIN's estimator, box

@@ -98,7 +98,7 @@ class RenderStats(C.Structure):
                 ("extend_interior_visits", C.c_int64), ("extend_tri_tests", C.c_int64),
                 ("shadow_interior_visits", C.c_int64), ("shadow_tri_tests", C.c_int64),
                 ("ms_total", C.c_double), ("ms_extend", C.c_double), ("ms_shadow", C.c_double),
-                ("ms_shade", C.c_double)]
+                ("ms_shade", C.c_double), ("guide_fallbacks", C.c_int64)]
 
 
 class CacheStats(C.Structure):
@@ -164,6 +164,7 @@ SIGNATURES = {
     "pgx_mlp_gradient": (C.c_int, [_P, _P, _I64, _P, C.POINTER(C.c_double)]),
     "pgx_mlp_train_step": (C.c_int, [_P, _P, _I64, C.c_float, C.POINTER(C.c_double)]),
     "pgx_mlp_configure": (C.c_int, [_P, C.c_float, C.c_float, _I64, _I32, _I32]),
+    "pgx_mlp_set_fallback": (C.c_int, [_P, _I32]),
     "pgx_diff_set_params": (C.c_int, [_P, _P, _P, _P]),
     "pgx_diff_render": (C.c_int, [_P, _I32, C.c_uint64, _I32, _P]),
     "pgx_diff_adjoint": (C.c_int, [_P, _I32, C.c_uint64, _I32, _P, _P, _P, _P]),

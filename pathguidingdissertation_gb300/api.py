@@ -296,6 +296,11 @@ class Context:
         self.check(self.lib.pgx_mlp_train_step(self.h, ptr(s), len(s), lr, C.byref(loss)))
         return loss.value
 
+    def mlp_set_fallback(self, min_samples: int) -> None:
+        """pgx_mlp_set_fallback: regions whose training samples number fewer
+        than min_samples are guided by the QuadTree guide (0: never)."""
+        self.check(self.lib.pgx_mlp_set_fallback(self.h, int(min_samples)))
+
     def mlp_configure(self, lr: float = 5e-3, decay: float = 0.998, batch: int = 262144, steps: int = 4,
                       direct: bool = True) -> None:
         self.check(self.lib.pgx_mlp_configure(self.h, lr, decay, batch, steps, int(direct)))

@@ -54,6 +54,7 @@ struct CacheState {
     int64_t n_records = 0;
     int64_t n_nodes = 0;
     int n_regions = 0;
+    uint64_t generation = 0;  // bumped by every build
     bool valid = false;
     bool pss = false;  // quadtrees over the diffuse BSDF's primary samples
     double build_ms = 0.0;
@@ -753,6 +754,16 @@ GuideView guide_view(const pgx_ctx* ctx) {
     return g;
 }
 
+uint64_t guide_generation(const pgx_ctx* ctx) {
+    const CacheState* cs = static_cast<const CacheState*>(ctx->cache_state);
+    return cs ? cs->generation : 0;
+}
+
+int guide_regions(const pgx_ctx* ctx) {
+    const CacheState* cs = static_cast<const CacheState*>(ctx->cache_state);
+    return (cs && cs->valid && cs->n_records > 0) ? cs->n_regions : 0;
+}
+
 bool guide_ready(const pgx_ctx* ctx) {
     const CacheState* cs = static_cast<const CacheState*>(ctx->cache_state);
     return cs && cs->valid && cs->n_records > 0;
@@ -762,6 +773,7 @@ bool guide_ready(const pgx_ctx* ctx) {
 int cache_build_device(pgx_ctx* ctx, const pgx_path_vertex* d_records, int64_t n, bool pss) {
     CacheState* cs = cstate(ctx);
     cs->valid = false;
+    cs->generation++;
     cs->pss = pss;
     if (n < 0 || n > (int64_t)INT32_MAX / 2) return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "cache: bad record count");
     auto t0 = std::chrono::steady_clock::now();

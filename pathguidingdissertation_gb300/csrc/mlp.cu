@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "pgx_ctx.h"
+#include "pgx_guide.cuh"
 #include "pgx_mlp.cuh"
 
 using namespace mlp;
@@ -47,6 +48,12 @@ struct MlpState {
     int64_t step = 0;
     bool valid = false;
     int sms = 0;
+    // Training samples per radiance-cache region (the QuadTree guide's
+    // regions), for the fallback: counts of cache build `count_gen`.
+    DevBuf region_count;
+    uint64_t count_gen = 0;
+    int count_regions = 0;
+    int fallback_min = 256;  // below this many samples a region uses the QuadTree guide (0: never)
 };
 
 MlpState* state(pgx_ctx* ctx) {
@@ -368,6 +375,15 @@ int check_status(pgx_ctx* ctx, const char* who) {
     return PGX_OK;
 }
 
+// Training samples (13 floats, position first) per radiance-cache region.
+__global__ void k_count_regions(GuideView gv, const float* __restrict__ samples, int64_t n, int* __restrict__ counts) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float* sm = samples + i * kSampleFloats;
+        const int r = guide_region_index(gv, f3(sm[0], sm[1], sm[2]));
+        if (r >= 0) atomicAdd(counts + r, 1);
+    }
+}
+
 }  // namespace
 
 // ---- internal entry points for the renderer -------------------------------------------------
@@ -479,6 +495,7 @@ extern "C" int pgx_mlp_init(pgx_ctx* ctx, uint64_t seed, const float* bmin, cons
     PGX_CUDA_TRY(ctx, cudaMemsetAsync(st->m2.p, 0, pb, ctx->stream));
     st->step = 0;
     st->valid = true;
+    st->count_gen = 0;  // a new network has seen no samples anywhere
     PGX_TRY(refresh_images(ctx));
     PGX_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     return PGX_OK;
@@ -503,6 +520,7 @@ extern "C" int pgx_mlp_set_params(pgx_ctx* ctx, const float* params) {
     PGX_CUDA_TRY(ctx, cudaMemsetAsync(st->m1.p, 0, kParams * sizeof(float), ctx->stream));
     PGX_CUDA_TRY(ctx, cudaMemsetAsync(st->m2.p, 0, kParams * sizeof(float), ctx->stream));
     st->step = 0;
+    st->count_gen = 0;  // parameters from elsewhere: no samples counted against the cache
     PGX_TRY(refresh_images(ctx));
     PGX_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     return PGX_OK;
@@ -557,6 +575,7 @@ static int train_host(pgx_ctx* ctx, const pgx_radiance_sample* samples, int64_t 
     PGX_CUDA_TRY(ctx, cudaMemcpyAsync(st->scratch.p, samples, sb, cudaMemcpyHostToDevice, ctx->stream));
     double l = 0.0;
     PGX_TRY(mlp_train_device(ctx, st->scratch.as<float>(), n, lr, &l, update));
+    if (update) PGX_TRY(mlp_count_regions(ctx, st->scratch.as<float>(), n));
     if (loss) *loss = l;
     if (grad_out) {
         PGX_CUDA_TRY(ctx, cudaMemcpyAsync(grad_out, st->grad.p, kParams * sizeof(float), cudaMemcpyDeviceToHost,
@@ -598,13 +617,67 @@ int mlp_train_direct(pgx_ctx* ctx) { return state(ctx)->direct; }
 int mlp_online_step(pgx_ctx* ctx, const float* samples, int64_t n) {
     MlpState* st = state(ctx);
     if (!st->valid || n <= 0) return PGX_OK;
+    int64_t used = 0;
     for (int k = 0; k < st->steps; k++) {
         int64_t off = (int64_t)k * st->batch;
         int64_t nk = std::min(st->batch, n - off);
         if (nk <= 0 || (k > 0 && nk < st->batch / 4)) break;
         float lr = st->lr * powf(st->decay, (float)st->step);
         PGX_TRY(mlp_train_device(ctx, samples + off * kSampleFloats, nk, lr, nullptr, true));
+        used = off + nk;
     }
+    return mlp_count_regions(ctx, samples, used);
+}
+
+// Adds the training samples' positions to the per-region counts of the
+// current radiance cache (reset whenever the cache or the network is new).
+int mlp_count_regions(pgx_ctx* ctx, const float* samples, int64_t n) {
+    MlpState* st = state(ctx);
+    if (!st->valid || n <= 0 || !guide_ready(ctx)) return PGX_OK;
+    const GuideView gv = guide_view(ctx);
+    if (gv.pss) return PGX_OK;  // primary-sample trees cannot stand in for directions
+    const uint64_t gen = guide_generation(ctx);
+    const int nreg = guide_regions(ctx);
+    if (nreg <= 0) return PGX_OK;
+    if (st->count_gen != gen || st->count_regions != nreg) {
+        PGX_CUDA_TRY(ctx, st->region_count.reserve(sizeof(int) * (size_t)nreg));
+        PGX_CUDA_TRY(ctx, cudaMemsetAsync(st->region_count.p, 0, sizeof(int) * (size_t)nreg, ctx->stream));
+        st->count_gen = gen;
+        st->count_regions = nreg;
+    }
+    k_count_regions<<<(unsigned)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, ctx->stream>>>(
+        gv, samples, n, st->region_count.as<int>());
+    PGX_CUDA_TRY(ctx, cudaGetLastError());
+    return PGX_OK;
+}
+
+const int* mlp_region_counts(pgx_ctx* ctx, int* min_samples) {
+    MlpState* st = ctx->mlp_state ? static_cast<MlpState*>(ctx->mlp_state) : nullptr;
+    *min_samples = 0;
+    if (!st || !st->valid || st->fallback_min <= 0 || !guide_ready(ctx)) return nullptr;
+    if (guide_view(ctx).pss || guide_regions(ctx) <= 0) return nullptr;
+    if (st->count_gen != guide_generation(ctx) || st->count_regions != guide_regions(ctx)) {
+        // nothing counted against this cache yet: every region is untrained
+        if (mlp_count_regions_reset(ctx) != PGX_OK) return nullptr;
+    }
+    *min_samples = st->fallback_min;
+    return st->region_count.as<int>();
+}
+
+int mlp_count_regions_reset(pgx_ctx* ctx) {
+    MlpState* st = state(ctx);
+    const int nreg = guide_regions(ctx);
+    PGX_CUDA_TRY(ctx, st->region_count.reserve(sizeof(int) * (size_t)std::max(nreg, 1)));
+    PGX_CUDA_TRY(ctx, cudaMemsetAsync(st->region_count.p, 0, sizeof(int) * (size_t)std::max(nreg, 1), ctx->stream));
+    st->count_gen = guide_generation(ctx);
+    st->count_regions = nreg;
+    return PGX_OK;
+}
+
+extern "C" int pgx_mlp_set_fallback(pgx_ctx* ctx, int32_t min_samples) {
+    PGX_TRY(ensure_ready(ctx, "pgx_mlp_set_fallback"));
+    if (min_samples < 0) return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_mlp_set_fallback: negative count");
+    state(ctx)->fallback_min = min_samples;
     return PGX_OK;
 }
 

@@ -56,6 +56,10 @@ struct GuideView {
 
 GuideView guide_view(const pgx_ctx* ctx);
 bool guide_ready(const pgx_ctx* ctx);
+// Number of the cache build (changes whenever the cache is rebuilt) and its
+// region count; 0 regions when there is no cache.
+uint64_t guide_generation(const pgx_ctx* ctx);
+int guide_regions(const pgx_ctx* ctx);
 int cache_build_device(pgx_ctx* ctx, const pgx_path_vertex* d_records, int64_t n, bool pss = false);
 
 __device__ __forceinline__ void dir_to_uv(F3 w, float& u, float& v) {
@@ -196,13 +200,14 @@ static __device__ void quad_sample(const QuadNode* qn, int root, float r1, float
 }
 
 // Region of x: descend the point BVH from the root, entering the child whose
-// box is nearer to x (0 when inside; ties to the left), until a region root.
-__device__ __forceinline__ int guide_region_root(const GuideView& g, F3 x) {
+// box is nearer to x (0 when inside; ties to the left), until a region root;
+// returns the region's index (-1 when a leaf comes first).
+__device__ __forceinline__ int guide_region_index(const GuideView& g, F3 x) {
     if (!g.valid || g.n_nodes <= 0) return -1;
     int node = 0;
     for (int d = 0; d < 64; d++) {
         int r = g.node_region[node];
-        if (r >= 0) return g.region_qroot[r];
+        if (r >= 0) return r;
         CacheTravNode n = g.nodes[node];
         int l = __float_as_int(n.bmin.w), rt = __float_as_int(n.bmax.w);
         if (l < 0) return -1;
@@ -216,6 +221,12 @@ __device__ __forceinline__ int guide_region_root(const GuideView& g, F3 x) {
         node = (box_d(b) < box_d(a)) ? rt : l;
     }
     return -1;
+}
+
+// The quadtree root of x's region (-1: no region or no flux).
+__device__ __forceinline__ int guide_region_root(const GuideView& g, F3 x) {
+    const int r = guide_region_index(g, x);
+    return r >= 0 ? g.region_qroot[r] : -1;
 }
 
 // Solid-angle pdf of the guide (quadtree mixed with a uniform share).

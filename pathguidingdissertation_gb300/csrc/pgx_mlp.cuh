@@ -394,5 +394,11 @@ MlpView mlp_view(pgx_ctx* ctx);
 int mlp_train_device(pgx_ctx* ctx, const float* samples, int64_t n, float lr, double* loss, bool update);
 int mlp_query_device(pgx_ctx* ctx, const float* q, const float* aux, int64_t n, int mode, float* out, float* out2);
 int mlp_online_step(pgx_ctx* ctx, const float* samples, int64_t n);
+// QuadTree fallback of the learned guide: training samples counted per
+// radiance-cache region; the counts of the current cache and the threshold
+// below which a region counts as untrained (nullptr / 0 when off).
+int mlp_count_regions(pgx_ctx* ctx, const float* samples, int64_t n);
+int mlp_count_regions_reset(pgx_ctx* ctx);
+const int* mlp_region_counts(pgx_ctx* ctx, int* min_samples);
 int64_t mlp_train_batch(pgx_ctx* ctx);
 int mlp_train_direct(pgx_ctx* ctx);

@@ -84,6 +84,7 @@ struct PathState {
     int64_t vcapacity;
     // learned guide: per-path mixture (10 float4), training records
     float4* guide;
+    int* fallback;    // per path: QuadTree root standing in for the network (-1: the network, -2: the BSDF)
     float4* rec_wo;   // wo
     float4* rec_f;    // f |cos| / pdf of the continuation
     float* train;     // radiance samples, 13 floats each
@@ -96,7 +97,7 @@ struct RenderState {
     DevBuf o, d, T, L, hit, pix, rng, flags, nrec, q0, q1, sh_path, sh_o, sh_d, sh_c;
     DevBuf rec_pos, rec_nrm, rec_wi, rec_w, rec_e;
     DevBuf counters, vertices, cqueue, ccount;
-    DevBuf guide, rec_wo, rec_f, train, scene;
+    DevBuf guide, fallback, rec_wo, rec_f, train, scene;
     int64_t capacity = 0;
     int rec_depth = 0;
     int64_t guide_capacity = 0;
@@ -523,7 +524,8 @@ constexpr int kInferSmem = mlp::kImageBytes + mlp::kBiasFloats * 4 + kInferGroup
 constexpr uint32_t kInferCols = 256;  // >= 64 per group, a power of two
 
 __global__ void __launch_bounds__(128 * kInferGroups, 2) k_guide_infer(SceneView sv, PathState ps, int depth, MlpView mv,
-                                                                   int* status) {
+                                                                   int* status, GuideView gv, const int* region_count,
+                                                                   int fallback_min) {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint64_t mbar[kInferGroups];
     __shared__ int flag[kInferGroups];
@@ -588,12 +590,26 @@ __global__ void __launch_bounds__(128 * kInferGroups, 2) k_guide_infer(SceneView
             if (s.tg == 0) atomicAdd(status, 1);
             break;
         }
+        // QuadTree fallback: where the network has been trained on fewer
+        // than fallback_min radiance samples of the vertex's cache region,
+        // that region's quadtree guides instead (as in the QuadTree mode:
+        // the BSDF alone where the region recorded no flux, marked -2).
+        int fb = -1;
+        if (need && region_count) {
+            const int r = guide_region_index(gv, x);
+            if (r >= 0 && region_count[r] < fallback_min) fb = gv.region_qroot[r] >= 0 ? gv.region_qroot[r] : -2;
+        }
+        const unsigned nfb = __ballot_sync(0xFFFFFFFFu, fb != -1);
+        if ((s.tg & 31) == 0 && nfb) atomicAdd(&ps.stats[6], (unsigned long long)__popc(nfb));
         if (need) {
-            float4 gm[mlp::kPacked];
-            mlp::pack_mixture(raw, gm);
-            float4* dst = ps.guide + (size_t)p * mlp::kPacked;
+            ps.fallback[p] = fb;
+            if (fb == -1) {
+                float4 gm[mlp::kPacked];
+                mlp::pack_mixture(raw, gm);
+                float4* dst = ps.guide + (size_t)p * mlp::kPacked;
 #pragma unroll
-            for (int j = 0; j < mlp::kPacked; j++) dst[j] = gm[j];
+                for (int j = 0; j < mlp::kPacked; j++) dst[j] = gm[j];
+            }
         }
     }
     tc::fence_before_sync();
@@ -775,8 +791,16 @@ __global__ void __launch_bounds__(kThreads, kShadeBlocksPerSM) k_shade(SceneView
                         qroot = guide_region_root(gv, sd.x);
                     if (MODE == PGX_MODE_GUIDED_PSS && depth < fp.guide_depth && gv.pss && pss_surface<KIND>(m))
                         qroot = guide_region_root(gv, sd.x);
-                    const bool use_mix =
+                    bool use_mix =
                         MODE == PGX_MODE_GUIDED_MLP && depth < fp.guide_depth && mlp_guided_surface<KIND>(m);
+                    if (MODE == PGX_MODE_GUIDED_MLP && use_mix) {
+                        // the region's quadtree stands in for an untrained network
+                        const int fb = ps.fallback[p];
+                        if (fb != -1) {
+                            qroot = fb >= 0 ? fb : -1;
+                            use_mix = false;
+                        }
+                    }
                     const float4* mix = use_mix ? ps.guide + (size_t)p * mlp::kPacked : nullptr;
                     if (MODE == PGX_MODE_GUIDED_LI) {
                         next_event_draws(sv, m, rng);
@@ -817,7 +841,7 @@ __global__ void __launch_bounds__(kThreads, kShadeBlocksPerSM) k_shade(SceneView
                         F3 f;
                         float pdf;
                         F3 wi;
-                        if (MODE == PGX_MODE_GUIDED_QUADTREE)
+                        if (MODE == PGX_MODE_GUIDED_QUADTREE || (MODE == PGX_MODE_GUIDED_MLP && qroot >= 0))
                             wi = guided_sample<KIND>(gv, fp.guide_fraction, m, sv.tex, sd, rng, f, pdf, qroot);
                         else if (MODE == PGX_MODE_GUIDED_PSS)
                             wi = pss_guided_sample<KIND>(gv, fp.guide_fraction, m, sv.tex, sd, rng, f, pdf, qroot);
@@ -1638,6 +1662,7 @@ int ensure_state(pgx_ctx* ctx, RenderState* rs, int64_t cap, int rec_depth, int6
     }
     if (guide && rs->guide_capacity < rs->capacity) {
         PGX_CUDA_TRY(ctx, rs->guide.reserve(sizeof(float4) * mlp::kPacked * rs->capacity));
+        PGX_CUDA_TRY(ctx, rs->fallback.reserve(sizeof(int) * rs->capacity));
         rs->guide_capacity = rs->capacity;
     }
     if (train_depth > 0 && (train_depth > rs->train_depth || rs->rec_wo.bytes < sizeof(float4) * train_depth * rs->capacity)) {
@@ -1697,6 +1722,7 @@ PathState path_view(RenderState* rs) {
     ps.capacity = rs->capacity;
     ps.vcapacity = rs->vcapacity;
     ps.guide = rs->guide.as<float4>();
+    ps.fallback = rs->fallback.as<int>();
     ps.rec_wo = rs->rec_wo.as<float4>();
     ps.rec_f = rs->rec_f.as<float4>();
     ps.train = rs->train.as<float>();
@@ -1739,6 +1765,8 @@ int enqueue_frame(pgx_ctx* ctx, RenderState* rs, const FrameParams& fp, cudaStre
     PathState ps = path_view(rs);
     GuideView gv = guide_view(ctx);
     MlpView mv = fp.mode == PGX_MODE_GUIDED_MLP ? mlp_view(ctx) : MlpView{};
+    int fb_min = 0;
+    const int* fb_counts = fp.mode == PGX_MODE_GUIDED_MLP ? mlp_region_counts(ctx, &fb_min) : nullptr;
     const int64_t n = (int64_t)ctx->width * ctx->height * fp.batch;
     const unsigned g = grid_for(n);
     const bool prof = fp.profile != 0;  // stage events
@@ -1761,7 +1789,8 @@ int enqueue_frame(pgx_ctx* ctx, RenderState* rs, const FrameParams& fp, cudaStre
             const int64_t tiles = (n + mlp::kRows - 1) / mlp::kRows;
             const int64_t ctas = (tiles + kInferGroups - 1) / kInferGroups;
             const unsigned ig = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ctas, (int64_t)pgx_num_sms() * 2));
-            k_guide_infer<<<ig, 128 * kInferGroups, kInferSmem, s>>>(sv, ps, depth, mv, mlp_status);
+            k_guide_infer<<<ig, 128 * kInferGroups, kInferSmem, s>>>(sv, ps, depth, mv, mlp_status, gv, fb_counts,
+                                                                      fb_min);
             launches++;
         }
         for (int c = 0; c < kShadeClasses; c++) {
@@ -1982,6 +2011,7 @@ extern "C" int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t fr
     rst.extend_tri_tests = (int64_t)st[3];
     rst.shadow_interior_visits = (int64_t)st[4];
     rst.shadow_tri_tests = (int64_t)st[5];
+    rst.guide_fallbacks = (int64_t)st[6];
     rst.kernel_launches = launches;
     rst.extend_launches = batches * (cfg->max_depth + 1);
     rst.ms_total = ms;

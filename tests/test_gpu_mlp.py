@@ -260,3 +260,43 @@ def test_trained_guide_lowers_the_error(ctx):
     assert e_learned < 0.75 * e_plain, summary
     assert e_learned < 0.8 * e_untrained, summary
     assert e_learned < 0.9 * e_quadtree, summary
+
+
+def test_quadtree_fallback_for_untrained_regions(ctx):
+    """The QuadTree guide stands in for the learned guide in radiance-cache
+    regions where the network has seen fewer than pgx_mlp_set_fallback's
+    count of training samples.  With an untrained network every guided
+    vertex falls back, and the image equals the QuadTree mode's (same
+    random numbers, same estimator); after online training the network
+    takes over most vertices; with the fallback off it takes all."""
+    desc = scenes.interior(seed=3, target_tris=20000, n_objects=40, width=64, height=36, env_width=256,
+                           env_height=128)
+    ctx.upload(desc)
+    ctx.bvh_build()
+    ctx.clear()
+    ctx.render(2, mode=abi.MODE_PLAIN, seed=1, max_depth=8, record_paths=2)  # the radiance cache
+    ctx.clear()
+    ctx.render(4, mode=abi.MODE_GUIDED_QUADTREE, seed=7, max_depth=8, guide_fraction=0.5)
+    q, _, _ = ctx.film()
+    ctx.mlp_init(3)
+    ctx.clear()
+    ctx.render(4, mode=abi.MODE_GUIDED_MLP, seed=7, max_depth=8, guide_fraction=0.5)
+    untrained = ctx.render_stats().guide_fallbacks
+    m, _, _ = ctx.film()
+    assert untrained > 0
+    rel = np.abs(m.astype(np.float64) - q) / np.maximum(np.abs(q.astype(np.float64)), 1e-3)
+    assert rel.max() < 1e-4, rel.max()
+
+    ctx.mlp_configure(lr=5e-3, decay=0.998, batch=1 << 14, steps=4)
+    ctx.clear()
+    ctx.render(24, mode=abi.MODE_GUIDED_MLP, seed=11, max_depth=8, train_guide=True)
+    ctx.clear()
+    ctx.render(4, mode=abi.MODE_GUIDED_MLP, seed=7, max_depth=8, guide_fraction=0.5)
+    trained = ctx.render_stats().guide_fallbacks
+    assert trained < 0.5 * untrained, (trained, untrained)
+    ctx.mlp_set_fallback(0)
+    ctx.clear()
+    ctx.render(4, mode=abi.MODE_GUIDED_MLP, seed=7, max_depth=8, guide_fraction=0.5)
+    assert ctx.render_stats().guide_fallbacks == 0
+    with pytest.raises(abi.PgxError):
+        ctx.mlp_set_fallback(-1)
