@@ -576,13 +576,14 @@ def run_adjoint_study(args) -> dict:
     from pathguidingdissertation_gb300.api import Context
 
     pkg_build.build()
-    desc = scenes.terrain()
+    # --diff-grid / --diff-res / --diff-spp shrink the case (profiler captures)
+    desc = scenes.terrain(grid=args.diff_grid, width=args.diff_res, height=args.diff_res)
     ctx = Context(0)
     ctx.upload(desc)
     ctx.bvh_build()
     nm = len(desc.materials)
     rng = np.random.default_rng(1)
-    depth, spp, seed = 8, 64, 11
+    depth, spp, seed = 8, args.diff_spp, 11
     env0 = desc.env.astype(np.float32)
     rough0 = desc.materials["roughness"].astype(np.float32)
     ctx.diff_set_params(env=(env0 + rng.normal(0, 0.05, env0.shape) * np.maximum(env0, 1e-3)).astype(np.float32)
@@ -660,6 +661,8 @@ def run_adjoint_study(args) -> dict:
     fd_s = time.perf_counter() - t0
     ctx.diff_set_params()
     ctx.close()
+    if not res:  # --fd-params 0: timing only
+        res = [("none", 1.0, 1.0, None)]
     fd = np.array([r[1] for r in res])
     ad = np.array([r[2] for r in res])
     rel = np.abs(ad - fd) / np.maximum(np.abs(fd), 1e-30)
@@ -668,12 +671,13 @@ def run_adjoint_study(args) -> dict:
     rel_raw = np.abs(ad - raw) / np.maximum(np.abs(raw), 1e-30)
     scale = np.abs(fd).max()
     significant = np.abs(fd) > 1e-3 * scale
-    paths = 512 * 512 * spp
+    paths = args.diff_res * args.diff_res * spp
     return {
         "study": "adjoint gradients vs central finite differences, fBm heightfield",
         "fd_step": "albedo offsets and roughness: central differences at h = 1e-3 and 5e-4 combined by Richardson "
                    "extrapolation; environment texels: 0.1 x max(1, texel) (exact: the loss is quadratic in a texel)",
-        "workload": f"terrain {desc.ntris} tris, {nm} materials, env 512x256, 512x512, depth {depth}",
+        "workload": f"terrain {desc.ntris} tris, {nm} materials, env 512x256, {args.diff_res}x{args.diff_res}, "
+                    f"depth {depth}",
         "loss": loss, "spp": spp, "target_spp": 256,
         "primal_s": primal_s, "adjoint_s": adjoint_s, "target_s": target_s,
         "primal_mpaths_per_s": paths / primal_s / 1e6, "adjoint_mpaths_per_s": paths / adjoint_s / 1e6,
@@ -964,6 +968,9 @@ def main() -> None:
     ap.add_argument("--mlp-indirect", action="store_true", help="train the learned guide on indirect light only")
     ap.add_argument("--trav-rays", type=int, default=10_000_000)
     ap.add_argument("--fd-params", type=int, default=256)
+    ap.add_argument("--diff-grid", type=int, default=1024, help="adjoint study: heightfield vertices per side")
+    ap.add_argument("--diff-res", type=int, default=512, help="adjoint study: image width and height")
+    ap.add_argument("--diff-spp", type=int, default=64, help="adjoint study: samples per pixel of the loss render")
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--batch-res", type=int, default=0, help="0: resolutions drawn from {128,256,512,1024}")
     ap.add_argument("--batch-max-tris", type=float, default=2e6)

@@ -114,7 +114,7 @@ struct RenderState {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t prof[kProfEvents] = {};
     // differentiable rendering: evaluation parameters and scratch
-    DevBuf d_mats, d_env, d_partial, d_img, d_dimg, d_genv, d_galb, d_grough;
+    DevBuf d_mats, d_env, d_partial, d_img, d_dimg, d_genv, d_galb, d_grough, d_next;
     bool d_params = false;
 };
 
@@ -1172,6 +1172,7 @@ struct DiffView {
     double* g_env;            // [env W*H*3]
     double* g_alb;            // [nmats*3]
     double* g_rough;          // [nmats]
+    unsigned long long* next; // adjoint: next sample to take (zeroed before the launch)
     int nmats;
 };
 
@@ -1266,24 +1267,55 @@ __device__ __forceinline__ F3 safe_div3(F3 a, F3 b) {
     return f3(a.x / fmaxf(b.x, 1e-6f), a.y / fmaxf(b.y, 1e-6f), a.z / fmaxf(b.z, 1e-6f));
 }
 
-// One path from its seed.  Returns the path's radiance.  GRAD: delta is the
-// adjoint of the sample's value; each vertex keeps what its gradient terms
-// need (DiffVertex) and the terms are emitted after the last vertex, when
-// the path's total radiance is known and the sample is known to be kept by
-// the film (finite) — one traversal per sample (path replay
-// backpropagation, Vicini et al. 2021, with the replay's second pass folded
-// into per-vertex records held by the thread).
+// State of one path of the differentiable estimator between bounces.
+struct DiffPath {
+    F3 o, dir;
+    F3 T, Ts, L;          // evaluation and sampling throughput, radiance so far
+    F3 delta;             // adjoint of the sample's value (gradient pass)
+    F3 esc_dir, esc_w;    // escaped ray: direction, T x MIS weight
+    uint64_t rng;
+    float prev_pdf;
+    int depth, nvtx;
+    bool prev_spec, escaped;
+};
+
+__device__ __forceinline__ void diff_begin(DiffPath& P, uint64_t rng, F3 o, F3 dir, F3 delta) {
+    P.o = o;
+    P.dir = dir;
+    P.T = f3(1.f, 1.f, 1.f);
+    P.Ts = P.T;
+    P.L = zero3();
+    P.delta = delta;
+    P.esc_dir = zero3();
+    P.esc_w = zero3();
+    P.rng = rng;
+    P.prev_pdf = 0.f;
+    P.depth = 0;
+    P.nvtx = 0;
+    P.prev_spec = false;
+    P.escaped = false;
+}
+
+// One bounce of the path: trace, background or emitter, NEE, Russian
+// roulette, continuation.  Returns true when the path has ended.  GRAD: the
+// vertex keeps what its gradient terms need (DiffVertex) in vtx[P.nvtx].
 template <bool GRAD>
-__device__ F3 diff_path(const SceneView& sv, const DiffView& dv, uint64_t rng, F3 o, F3 dir, F3 delta,
-                        const DiffAcc& acc) {
-    F3 T = f3(1.f, 1.f, 1.f), Ts = T, L = zero3();
-    bool prev_spec = false;
-    float prev_pdf = 0.f;
-    DiffVertex vtx[GRAD ? kMaxDepthCap + 1 : 1];
-    int nvtx = 0;
-    F3 esc_dir = zero3(), esc_w = zero3();  // escaped ray: direction, T x MIS weight
-    bool escaped = false;
-    for (int depth = 0; depth <= dv.max_depth; depth++) {
+__device__ bool diff_step(const SceneView& sv, const DiffView& dv, DiffPath& P, DiffVertex* vtx) {
+    F3& o = P.o;
+    F3& dir = P.dir;
+    F3& T = P.T;
+    F3& Ts = P.Ts;
+    F3& L = P.L;
+    uint64_t& rng = P.rng;
+    bool& prev_spec = P.prev_spec;
+    float& prev_pdf = P.prev_pdf;
+    int& nvtx = P.nvtx;
+    bool& escaped = P.escaped;
+    F3& esc_dir = P.esc_dir;
+    F3& esc_w = P.esc_w;
+    const int depth = P.depth;
+    {
+
         int id;
         float t, hu, hv;
         int status;
@@ -1312,7 +1344,7 @@ __device__ F3 diff_path(const SceneView& sv, const DiffView& dv, uint64_t rng, F
                     esc_w = T * w;
                 }
             }
-            break;
+            return true;
         }
         Shading sd;
         DevMaterial ms;
@@ -1341,7 +1373,7 @@ __device__ F3 diff_path(const SceneView& sv, const DiffView& dv, uint64_t rng, F
                     L = L + (T * em) * power_heuristic(pab, (1.f / tri_area) * pmf);
                 }
             }
-            break;
+            return true;
         }
         // ---- next-event estimation (next_event with detached pdfs) ----
         if (!bsdf_pure_specular(ms) && sv.nlights > 0) {
@@ -1433,10 +1465,10 @@ __device__ F3 diff_path(const SceneView& sv, const DiffView& dv, uint64_t rng, F
                 T = divs(T, q);
                 Ts = divs(Ts, q);
             } else {
-                break;
+                return true;
             }
         }
-        if (depth == dv.max_depth) break;
+        if (depth == dv.max_depth) return true;
         // ---- continuation: sampled with the sampling material ----
         const bool spec = bsdf_pure_specular(ms);
         uint64_t rng0 = rng;
@@ -1444,7 +1476,7 @@ __device__ F3 diff_path(const SceneView& sv, const DiffView& dv, uint64_t rng, F
         float pdf;
         F3 wi = bsdf_sample(ms, sv.tex, sd, rng, fs, pdf);
         float cos_t = fabsf(dot(wi, sd.sn));
-        if (pdf <= 0.f || cos_t <= 0.f) break;
+        if (pdf <= 0.f || cos_t <= 0.f) return true;
         F3 fe;
         if (spec) {
             // deterministic directions: the evaluation material's own sample
@@ -1461,16 +1493,28 @@ __device__ F3 diff_path(const SceneView& sv, const DiffView& dv, uint64_t rng, F
         }
         T = divs(T * fe * cos_t, pdf);
         Ts = divs(Ts * fs * cos_t, pdf);
-        if (lum(Ts) <= 0.f) break;
-        if (isnan(Ts.x) || isnan(Ts.y) || isnan(Ts.z)) break;
-        if (isinf(Ts.x) || isinf(Ts.y) || isinf(Ts.z)) break;
-        if (Ts.x < 0.f || Ts.y < 0.f || Ts.z < 0.f) break;
+        if (lum(Ts) <= 0.f) return true;
+        if (isnan(Ts.x) || isnan(Ts.y) || isnan(Ts.z)) return true;
+        if (isinf(Ts.x) || isinf(Ts.y) || isinf(Ts.z)) return true;
+        if (Ts.x < 0.f || Ts.y < 0.f || Ts.z < 0.f) return true;
         float sgn = (dot(wi, sd.gn) >= 0.f) ? 1.f : -1.f;
         o = sd.x + sd.gn * (PGX_EPSILON * sgn);
         dir = wi;
         prev_spec = spec;
         prev_pdf = pdf;
+    
     }
+    return ++P.depth > dv.max_depth;
+}
+
+// The gradient terms of a finished path: emitted once its radiance L is
+// known, and only when L is finite (the film drops the other samples).
+template <bool GRAD>
+__device__ void diff_finish(const DiffView& dv, const DiffPath& P, const DiffVertex* vtx, const DiffAcc& acc) {
+    const F3 L = P.L, delta = P.delta;
+    const int nvtx = P.nvtx;
+    const bool escaped = P.escaped;
+    const F3 esc_dir = P.esc_dir, esc_w = P.esc_w;
     if (GRAD && valid(L)) {  // the film drops non-finite samples: no gradient from them
         for (int j = 0; j < nvtx; j++) {
             const DiffVertex& v = vtx[j];
@@ -1489,7 +1533,25 @@ __device__ F3 diff_path(const SceneView& sv, const DiffView& dv, uint64_t rng, F
         }
         if (escaped) env_scatter(dv.env_e, esc_dir, delta * esc_w, dv.g_env);
     }
-    return L;
+}
+
+// One path from its seed.  Returns the path's radiance.  GRAD: delta is the
+// adjoint of the sample's value; each vertex keeps what its gradient terms
+// need (DiffVertex) and the terms are emitted after the last vertex, when
+// the path's total radiance is known and the sample is known to be kept by
+// the film (finite) — one traversal per sample (path replay
+// backpropagation, Vicini et al. 2021, with the replay's second pass folded
+// into per-vertex records held by the thread).
+template <bool GRAD>
+__device__ F3 diff_path(const SceneView& sv, const DiffView& dv, uint64_t rng, F3 o, F3 dir, F3 delta,
+                        const DiffAcc& acc) {
+    DiffPath P;
+    DiffVertex vtx[GRAD ? kMaxDepthCap + 1 : 1];
+    diff_begin(P, rng, o, dir, delta);
+    while (!diff_step<GRAD>(sv, dv, P, vtx)) {
+    }
+    diff_finish<GRAD>(dv, P, vtx, acc);
+    return P.L;
 }
 
 // Sample s of pixel (x, y): jitter, camera ray, target pixel of the box
@@ -1548,6 +1610,10 @@ __global__ void k_diff_gather(const double* __restrict__ partial, int W, int H, 
     }
 }
 
+// Persistent warps over the samples (pixel-major within each sample index):
+// a lane whose path has ended takes the next sample from dv.next at once
+// (warp-aggregated atomicAdd), so short and long paths share the warp's
+// issue slots instead of each warp waiting for its longest path.
 __global__ void __launch_bounds__(kThreads) k_diff_adjoint(SceneView sv, DiffView dv) {
     extern __shared__ double sacc[];  // [nmats*3 + nmats] when it fits
     const bool shared_acc = dv.nmats * 4 * (int)sizeof(double) <= 32 * 1024;
@@ -1561,25 +1627,50 @@ __global__ void __launch_bounds__(kThreads) k_diff_adjoint(SceneView sv, DiffVie
         acc.alb = dv.g_alb;
         acc.rough = dv.g_rough;
     }
+    constexpr unsigned kFull = 0xFFFFFFFFu;
     const int64_t npix = (int64_t)sv.width * sv.height;
-    const int64_t items = npix * dv.spp;
+    const unsigned long long items = (unsigned long long)npix * (unsigned long long)dv.spp;
     const F3 origin = f3(sv.cam.origin[0], sv.cam.origin[1], sv.cam.origin[2]);
     const float inv_spp = 1.f / (float)dv.spp;
-    // One sample per thread: neighbouring threads take neighbouring pixels
-    // of the same sample index (coherent camera rays).
-    for (int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; item < items;
-         item += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t pixel = item % npix;
-        const int s = (int)(item / npix);
-        int x = (int)(pixel % sv.width), y = (int)(pixel / sv.width);
-        uint64_t rng;
-        F3 dir;
-        int k = diff_camera(sv, dv, pixel, s, rng, dir);
-        if (k < 0) continue;
-        int64_t tp = (int64_t)(y + k / 2) * sv.width + (x + k % 2);
-        F3 delta = f3(dv.dimg[3 * tp], dv.dimg[3 * tp + 1], dv.dimg[3 * tp + 2]) * inv_spp;
-        if (delta.x == 0.f && delta.y == 0.f && delta.z == 0.f) continue;
-        diff_path<true>(sv, dv, rng, origin, dir, delta, acc);
+    const int lane = threadIdx.x & 31;
+    DiffPath P;
+    DiffVertex vtx[kMaxDepthCap + 1];
+    bool active = false, exhausted = false;
+    for (;;) {
+        const bool need = !active && !exhausted;
+        const unsigned m = __ballot_sync(kFull, need);
+        if (m) {
+            const int leader = __ffs(m) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(dv.next, (unsigned long long)__popc(m));
+            base = __shfl_sync(kFull, base, leader);
+            if (need) {
+                const unsigned long long item = base + (unsigned long long)__popc(m & ((1u << lane) - 1u));
+                if (item < items) {
+                    const int64_t pixel = (int64_t)(item % (unsigned long long)npix);
+                    const int smp = (int)(item / (unsigned long long)npix);
+                    const int x = (int)(pixel % sv.width), y = (int)(pixel / sv.width);
+                    uint64_t rng;
+                    F3 dir;
+                    const int k = diff_camera(sv, dv, pixel, smp, rng, dir);
+                    if (k >= 0) {
+                        const int64_t tp = (int64_t)(y + k / 2) * sv.width + (x + k % 2);
+                        const F3 delta = f3(dv.dimg[3 * tp], dv.dimg[3 * tp + 1], dv.dimg[3 * tp + 2]) * inv_spp;
+                        if (delta.x != 0.f || delta.y != 0.f || delta.z != 0.f) {
+                            diff_begin(P, rng, origin, dir, delta);
+                            active = true;
+                        }
+                    }
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        if (__all_sync(kFull, !active && exhausted)) break;
+        if (active && diff_step<true>(sv, dv, P, vtx)) {
+            diff_finish<true>(dv, P, vtx, acc);
+            active = false;
+        }
     }
     if (shared_acc) {
         __syncthreads();
@@ -2206,14 +2297,23 @@ extern "C" int pgx_diff_adjoint(pgx_ctx* ctx, int32_t spp, uint64_t seed, int32_
     PGX_CUDA_TRY(ctx, cudaMemsetAsync(rs->d_genv.p, 0, sizeof(double) * std::max<size_t>(ef, 1), s));
     PGX_CUDA_TRY(ctx, cudaMemsetAsync(rs->d_galb.p, 0, sizeof(double) * std::max<size_t>(3 * nm, 1), s));
     PGX_CUDA_TRY(ctx, cudaMemsetAsync(rs->d_grough.p, 0, sizeof(double) * std::max<size_t>(nm, 1), s));
+    PGX_CUDA_TRY(ctx, rs->d_next.reserve(sizeof(unsigned long long)));
+    PGX_CUDA_TRY(ctx, cudaMemsetAsync(rs->d_next.p, 0, sizeof(unsigned long long), s));
     DiffView dv = diff_view(ctx, rs, spp, seed, max_depth);
     dv.dimg = rs->d_dimg.as<float>();
     dv.g_env = ef ? rs->d_genv.as<double>() : nullptr;
     dv.g_alb = rs->d_galb.as<double>();
     dv.g_rough = rs->d_grough.as<double>();
+    dv.next = rs->d_next.as<unsigned long long>();
     const size_t sm = nm * 4 * sizeof(double) <= 32 * 1024 ? nm * 4 * sizeof(double) : 0;
     SceneView sv = scene_view(ctx);
-    k_diff_adjoint<<<grid_for(npix * (int64_t)spp), kThreads, sm, s>>>(sv, dv);
+    // persistent: as many blocks as are resident at once
+    int per_sm = 0;
+    PGX_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_diff_adjoint, kThreads, sm));
+    const unsigned ag = (unsigned)std::max<int64_t>(
+        1, std::min<int64_t>((npix * (int64_t)spp + kThreads - 1) / kThreads,
+                             (int64_t)pgx_num_sms() * std::max(per_sm, 1)));
+    k_diff_adjoint<<<ag, kThreads, sm, s>>>(sv, dv);
     PGX_CUDA_TRY(ctx, cudaGetLastError());
     std::vector<double> he(grad_env && ef ? ef : 0), ha(grad_albedo ? 3 * nm : 0), hr(grad_roughness ? nm : 0);
     if (!he.empty())
