@@ -260,10 +260,12 @@ def run_pgx(args) -> dict:
     cst = ctx.render_stats()
     visits_per_ray = cst.extend_interior_visits / max(cst.extension_rays, 1)
     tris_per_ray = cst.extend_tri_tests / max(cst.extension_rays, 1)
+    sh_visits_per_ray = cst.shadow_interior_visits / max(cst.shadow_rays, 1)
+    sh_tris_per_ray = cst.shadow_tri_tests / max(cst.shadow_rays, 1)
     torch.cuda.synchronize()
     ranks.barrier()
-    rays = paths = ext_rays = 0
-    ms = ms_ext = ms_shade = 0.0
+    rays = paths = ext_rays = sh_rays = 0
+    ms = ms_ext = ms_shade = ms_shadow = 0.0
     ext_launches = launches = 0
     with ClockSampler() as clk:
         for k in range(args.steps):
@@ -276,7 +278,9 @@ def run_pgx(args) -> dict:
             ms += st.ms_total
             ms_ext += st.ms_extend
             ms_shade += st.ms_shade
+            ms_shadow += st.ms_shadow
             ext_rays += st.extension_rays
+            sh_rays += st.shadow_rays
             ext_launches += st.extend_launches
             launches += st.kernel_launches
         torch.cuda.synchronize()
@@ -375,6 +379,47 @@ def run_pgx(args) -> dict:
         "shade_share_of_step": ms_shade / ms if ms else None,
         "note": "latency-bound (dependent gathers of shading data, 64 registers); traffic not captured",
     }
+    # The other half of the metric: equal-time relMSE of the learned guide
+    # against plain path tracing (a reduced form of --study relmse: the
+    # converged image at 8,192 spp instead of 65,536; not part of the timed
+    # steps).  Rank 0 of a single-GPU run only.
+    equal_time = None
+    if not args.no_equal_time and ranks.world == 1 and args.workload == "interior" and not args.res:
+        import copy
+        sa = copy.copy(args)
+        sa.study_res, sa.ref_spp, sa.plain_spp, sa.guide, sa.metric = "1280x720", 8192, 1024, "mlp", "robust"
+        sa.guide_fraction, sa.train_frames, sa.ref_cache, sa.save_images = 0.75, 64, None, None
+        print("[bench] equal-time relMSE study", file=sys.stderr, flush=True)
+        r = run_relmse_study(sa)
+        equal_time = {
+            "study": "learned guide vs plain GPU path tracing, time to plain's 1024-spp relMSE",
+            "workload": r["workload"], "reference_spp": sa.ref_spp,
+            "metric": "relMSE (x-r)^2/(r^2+0.01) without the 0.1 % largest pixel errors; plain relMSE beside",
+            "plain_ms": r["plain"]["ms"], "plain_relmse": r["plain"]["relmse"],
+            "plain_relmse_plain_metric": r["plain"]["relmse_other_metric"],
+            "guided_train_ms": r["guided"]["train_ms"], "guided_ms_to_plain_error": r["guided"]["ms_to_plain_error"],
+            "guided_relmse_at_plain_time": r["guided"]["relmse_at_plain_time"],
+            "time_ratio_guided_over_plain": r["time_ratio_guided_over_plain"],
+            "time_ratio_plain_metric": r["time_ratio_other_metric"],
+        }
+    # k_shadow (any hit): node and triangle fetches of the shadow rays over
+    # its CUDA-event time; like k_extend it reads a tree that stays in L2.
+    sh_bytes = (sh_visits_per_ray * 64 + sh_tris_per_ray * 48) * sh_rays
+    sh_achieved = sh_bytes / (ms_shadow * 1e-3) / 1e9 if ms_shadow > 0 else None
+    roofline_shadow = {
+        "kernel": "k_shadow (any-hit traversal of the NEE shadow rays)",
+        "bound": "issue",
+        "achieved": sh_achieved,
+        "peak": peaks["hbm_gbs"],
+        "unit": "GB/s",
+        "frac": (sh_achieved / peaks["hbm_gbs"]) if sh_achieved else None,
+        "nodes_per_ray": sh_visits_per_ray,
+        "tris_per_ray": sh_tris_per_ray,
+        "mrays_per_s": sh_rays / (ms_shadow * 1e-3) / 1e6 if ms_shadow > 0 else None,
+        "shadow_share_of_step": ms_shadow / ms if ms else None,
+        "note": "algorithmic node (64 B) and triangle (48 B) bytes per second against the HBM copy rate; the tree "
+                "is L2-resident as for k_extend",
+    }
     print("[bench] device runs done; CPU baseline next", file=sys.stderr, flush=True)
     cpu = cpu_baseline_reference(desc) if not args.no_cpu_baseline and ranks.world == 1 else None
     print("[bench] CPU baseline done", file=sys.stderr, flush=True)
@@ -403,8 +448,10 @@ def run_pgx(args) -> dict:
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": C.sizeof(abi.Camera),
                 "d2h_bytes_per_step": H * W * 3 * 4},
         "modes": side,
+        "equal_time": equal_time,
         "roofline": roofline,
         "roofline_shade": roofline_shade,
+        "roofline_shadow": roofline_shadow,
         "cpu_baseline": cpu,
         "clocks": clocks,
     }
@@ -946,6 +993,7 @@ def main() -> None:
     ap.add_argument("--workload", choices=["interior", "cornell"], default="interior")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-side-modes", action="store_true", help="skip the guided and depth-8 side measurements")
+    ap.add_argument("--no-equal-time", action="store_true", help="skip the reduced equal-time relMSE study")
     ap.add_argument("--res", default=None, help="WxH: render the workload at this image size (profiler captures)")
     ap.add_argument("--spp-per-step", type=int, default=32,
                     help="samples per pixel of one step: one pgx_render call, one wavefront")
