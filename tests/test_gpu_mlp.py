@@ -217,7 +217,7 @@ def test_online_training_updates_the_guide(ctx):
 
 
 def test_trained_guide_lowers_the_error(ctx):
-    """What the trained network gains: on the small interior (160 x 90, the
+    """What the trained network gains: on the small interior (320 x 180, the
     sky-and-sun environment seen through the window), at equal spp, the
     image rendered with the online-trained learned guide has a lower relMSE
     against a 4,096-spp plain render than (a) plain path tracing, (b) the
@@ -225,11 +225,11 @@ def test_trained_guide_lowers_the_error(ctx):
     trained on as many samples.  relMSE = mean((x - r)^2 / (r^2 + 0.01)) over
     pixels, without the 0.1 % largest per-pixel errors (sun fireflies)."""
     from pathguidingdissertation_gb300.metrics import relmse_robust
-    desc = scenes.interior(seed=2, target_tris=40000, n_objects=80, width=160, height=90, env_width=512,
+    desc = scenes.interior(seed=2, target_tris=40000, n_objects=80, width=320, height=180, env_width=512,
                            env_height=256)
     ctx.upload(desc)
     ctx.bvh_build()
-    depth, spp, train = 10, 64, 32
+    depth, spp, train = 10, 64, 64
 
     def image(mode, seed, **kw):
         ctx.clear()
@@ -245,7 +245,7 @@ def test_trained_guide_lowers_the_error(ctx):
 
     ctx.mlp_init(3)
     e_untrained = relmse_robust(image(abi.MODE_GUIDED_MLP, 7, guide_fraction=0.75), ref)
-    ctx.mlp_configure(lr=5e-3, decay=0.998, batch=1 << 16, steps=4)
+    ctx.mlp_configure(lr=5e-3, decay=0.998, batch=1 << 16, steps=2)
     ctx.clear()
     ctx.render(train, mode=abi.MODE_GUIDED_MLP, seed=11, max_depth=depth, train_guide=True, guide_fraction=0.75)
     e_learned = relmse_robust(image(abi.MODE_GUIDED_MLP, 7, guide_fraction=0.75), ref)
