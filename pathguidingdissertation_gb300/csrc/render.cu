@@ -114,7 +114,7 @@ struct RenderState {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t prof[kProfEvents] = {};
     // differentiable rendering: evaluation parameters and scratch
-    DevBuf d_mats, d_env, d_partial, d_img, d_dimg, d_genv, d_galb, d_grough, d_next;
+    DevBuf d_mats, d_env, d_partial, d_img, d_dimg, d_genv, d_galb, d_grough, d_next, d_samples;
     bool d_params = false;
 };
 
@@ -1172,7 +1172,9 @@ struct DiffView {
     double* g_env;            // [env W*H*3]
     double* g_alb;            // [nmats*3]
     double* g_rough;          // [nmats]
-    unsigned long long* next; // adjoint: next sample to take (zeroed before the launch)
+    unsigned long long* next; // next sample to take (zeroed before each launch)
+    float4* samples;          // primal: values of the chunk's samples
+    int s0, ns;               // primal: the chunk's samples [s0, s0 + ns)
     int nmats;
 };
 
@@ -1569,26 +1571,78 @@ __device__ __forceinline__ int diff_camera(const SceneView& sv, const DiffView& 
     return (by - y) * 2 + (bx - x);  // 0..3: which neighbour (right, down)
 }
 
+// Primal samples [s0, s0 + ns) on persistent warps with lane refill (as the
+// adjoint): sample i of the chunk (pixel-major) stores its value and the box
+// filter's target neighbour k in samples[i] (w = -1 when the film drops it).
+// The per-pixel sums happen afterwards in sample order (k_diff_accumulate),
+// so the image does not depend on which lane traced which sample.
 __global__ void __launch_bounds__(kThreads) k_diff_primal(SceneView sv, DiffView dv) {
+    constexpr unsigned kFull = 0xFFFFFFFFu;
     const int64_t npix = (int64_t)sv.width * sv.height;
+    const unsigned long long items = (unsigned long long)npix * (unsigned long long)dv.ns;
     const F3 origin = f3(sv.cam.origin[0], sv.cam.origin[1], sv.cam.origin[2]);
-    for (int64_t pixel = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; pixel < npix;
-         pixel += (int64_t)gridDim.x * blockDim.x) {
-        double acc[4][3] = {};
-        DiffAcc none{nullptr, nullptr};
-        for (int s = 0; s < dv.spp; s++) {
-            uint64_t rng;
-            F3 dir;
-            int k = diff_camera(sv, dv, pixel, s, rng, dir);
-            F3 c = diff_path<false>(sv, dv, rng, origin, dir, zero3(), none);
-            if (k < 0 || !valid(c)) continue;
-            acc[k][0] += (double)c.x;
-            acc[k][1] += (double)c.y;
-            acc[k][2] += (double)c.z;
+    const int lane = threadIdx.x & 31;
+    DiffAcc none{nullptr, nullptr};
+    DiffPath P;
+    DiffVertex vtx[1];
+    bool active = false, exhausted = false;
+    unsigned long long mine = 0;
+    int k = -1;
+    for (;;) {
+        const bool need = !active && !exhausted;
+        const unsigned m = __ballot_sync(kFull, need);
+        if (m) {
+            const int leader = __ffs(m) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(dv.next, (unsigned long long)__popc(m));
+            base = __shfl_sync(kFull, base, leader);
+            if (need) {
+                mine = base + (unsigned long long)__popc(m & ((1u << lane) - 1u));
+                if (mine < items) {
+                    const int64_t pixel = (int64_t)(mine % (unsigned long long)npix);
+                    const int smp = dv.s0 + (int)(mine / (unsigned long long)npix);
+                    uint64_t rng;
+                    F3 dir;
+                    k = diff_camera(sv, dv, pixel, smp, rng, dir);
+                    diff_begin(P, rng, origin, dir, zero3());
+                    active = true;
+                } else {
+                    exhausted = true;
+                }
+            }
         }
-        double* out = dv.partial + pixel * 12;
-        for (int k = 0; k < 4; k++)
-            for (int c = 0; c < 3; c++) out[3 * k + c] = acc[k][c];
+        if (__all_sync(kFull, !active && exhausted)) break;
+        if (active && diff_step<false>(sv, dv, P, vtx)) {
+            const F3 c = P.L;
+            const bool keep = k >= 0 && valid(c);
+            dv.samples[mine] = make_float4(c.x, c.y, c.z, keep ? (float)k : -1.f);
+            active = false;
+        }
+    }
+}
+
+// Adds each pixel's samples of a chunk to its four neighbour sums, in sample
+// order (deterministic).
+__global__ void k_diff_accumulate(const float4* __restrict__ samples, int64_t npix, int ns, double* __restrict__ partial) {
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += (int64_t)gridDim.x * blockDim.x) {
+        double acc[12];
+        double* out = partial + p * 12;
+#pragma unroll
+        for (int j = 0; j < 12; j++) acc[j] = out[j];
+        for (int j = 0; j < ns; j++) {
+            const float4 v = samples[(int64_t)j * npix + p];
+            if (v.w < 0.f) continue;
+            const int k = (int)v.w;
+#pragma unroll
+            for (int kk = 0; kk < 4; kk++)  // constant indexes: acc stays in registers
+                if (k == kk) {
+                    acc[3 * kk + 0] += (double)v.x;
+                    acc[3 * kk + 1] += (double)v.y;
+                    acc[3 * kk + 2] += (double)v.z;
+                }
+        }
+#pragma unroll
+        for (int j = 0; j < 12; j++) out[j] = acc[j];
     }
 }
 
@@ -2265,11 +2319,28 @@ extern "C" int pgx_diff_render(pgx_ctx* ctx, int32_t spp, uint64_t seed, int32_t
     const int64_t npix = (int64_t)ctx->width * ctx->height;
     PGX_CUDA_TRY(ctx, rs->d_partial.reserve(sizeof(double) * 12 * npix));
     PGX_CUDA_TRY(ctx, rs->d_img.reserve(sizeof(double) * 3 * npix));
+    // sample values of up to 1 GiB at a time
+    const int chunk = (int)std::max<int64_t>(1, std::min<int64_t>(spp, ((int64_t)1 << 30) / (16 * npix)));
+    PGX_CUDA_TRY(ctx, rs->d_samples.reserve(sizeof(float4) * (size_t)npix * chunk));
+    PGX_CUDA_TRY(ctx, rs->d_next.reserve(sizeof(unsigned long long)));
     DiffView dv = diff_view(ctx, rs, spp, seed, max_depth);
     dv.partial = rs->d_partial.as<double>();
+    dv.samples = rs->d_samples.as<float4>();
+    dv.next = rs->d_next.as<unsigned long long>();
     SceneView sv = scene_view(ctx);
     cudaStream_t s = ctx->stream;
-    k_diff_primal<<<grid_for(npix), kThreads, 0, s>>>(sv, dv);
+    PGX_CUDA_TRY(ctx, cudaMemsetAsync(dv.partial, 0, sizeof(double) * 12 * npix, s));
+    int per_sm = 0;
+    PGX_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_diff_primal, kThreads, 0));
+    for (int s0 = 0; s0 < spp; s0 += chunk) {
+        dv.s0 = s0;
+        dv.ns = std::min(chunk, spp - s0);
+        const unsigned pg = (unsigned)std::max<int64_t>(
+            1, std::min<int64_t>((npix * dv.ns + kThreads - 1) / kThreads, (int64_t)pgx_num_sms() * std::max(per_sm, 1)));
+        PGX_CUDA_TRY(ctx, cudaMemsetAsync(dv.next, 0, sizeof(unsigned long long), s));
+        k_diff_primal<<<pg, kThreads, 0, s>>>(sv, dv);
+        k_diff_accumulate<<<grid_for(npix), kThreads, 0, s>>>(dv.samples, npix, dv.ns, dv.partial);
+    }
     k_diff_gather<<<grid_for(npix), kThreads, 0, s>>>(dv.partial, ctx->width, ctx->height, spp, rs->d_img.as<double>());
     PGX_CUDA_TRY(ctx, cudaGetLastError());
     PGX_CUDA_TRY(ctx, cudaMemcpyAsync(image, rs->d_img.p, sizeof(double) * 3 * npix, cudaMemcpyDeviceToHost, s));
