@@ -1145,10 +1145,10 @@ __global__ void __launch_bounds__(kThreads) k_finalize(SceneView sv, PathState p
 //    roulette, the environment's sampling tables) use the uploaded scene,
 //    while radiance is evaluated with the "evaluation" parameters -- the
 //    environment texels, a per-material albedo offset and GGX roughness.
-//    Each thread sums its samples per target pixel in double, and a gather
-//    kernel adds the 4 neighbours' partial sums in a fixed order, so the
-//    image is deterministic and a finite difference between two parameter
-//    sets differs only through the samples a parameter touches;
+//    Sample values are summed per target pixel in double in sample order,
+//    and a gather kernel adds the 4 neighbours' partial sums in a fixed
+//    order, so the image is deterministic and a finite difference between
+//    two parameter sets differs only through the samples a parameter touches;
 //  * adjoint: with evaluation = uploaded parameters, one thread per sample
 //    traces the path once from its seed; every vertex j keeps (in the
 //    thread's registers and local memory, never in global memory) what its
