@@ -552,7 +552,7 @@ def run_relmse_study(args) -> dict:
         mode = abi.MODE_GUIDED_PSS if args.guide == "pss" else abi.MODE_GUIDED_QUADTREE
         for it in range(args.train_iters):
             ctx.clear()
-            n = 1 << it
+            n = (1 << it) if it else args.train_first
             m = abi.MODE_PLAIN if (it == 0 and args.guide == "quadtree") else mode
             train_ms += render_ms(n, m, 11 + it, record_paths=n, guide_fraction=args.guide_fraction)
             train_ms += ctx.cache_stats().build_ms
@@ -1003,6 +1003,7 @@ def main() -> None:
     ap.add_argument("--ref-spp", type=int, default=16384)
     ap.add_argument("--plain-spp", type=int, default=1024)
     ap.add_argument("--train-iters", type=int, default=6)
+    ap.add_argument("--train-first", type=int, default=1, help="QuadTree/PSS study: frames of the first (unguided) cache pass")
     ap.add_argument("--guide-fraction", type=float, default=0.5)
     ap.add_argument("--guide", choices=["mlp", "quadtree", "pss"], default="mlp")
     ap.add_argument("--metric", choices=["robust", "plain"], default="robust")
