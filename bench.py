@@ -534,14 +534,14 @@ def run_relmse_study(args) -> dict:
         # Learned guide: online training on the first `train_frames` frames
         # (`mlp_steps` Adam steps per frame, batch 2^18), which stay in the image.
         ctx.mlp_init(3)
-        ctx.mlp_configure(lr=args.mlp_lr, decay=args.mlp_decay, batch=1 << 18, steps=args.mlp_steps,
+        ctx.mlp_configure(lr=args.mlp_lr, decay=args.mlp_decay, batch=args.mlp_batch, steps=args.mlp_steps,
                           direct=not args.mlp_indirect)
         mode = abi.MODE_GUIDED_MLP
         train_ms = render_ms(args.train_frames, mode, 13, guide_fraction=args.guide_fraction, train_guide=True,
                              guide_depth=args.guide_depth)
         train_spp = args.train_frames
         extra = {"train_frames": args.train_frames, "lr": args.mlp_lr, "lr_decay": args.mlp_decay,
-                 "adam_steps_per_frame": args.mlp_steps, "guide_depth": args.guide_depth,
+                 "adam_steps_per_frame": args.mlp_steps, "batch": args.mlp_batch, "guide_depth": args.guide_depth,
                  "target": "indirect" if args.mlp_indirect else "full incident radiance"}
     else:
         # QuadTree (directions) or PSS (primary samples): train the cache over
@@ -1011,6 +1011,7 @@ def main() -> None:
     ap.add_argument("--mlp-lr", type=float, default=5e-3)
     ap.add_argument("--mlp-decay", type=float, default=0.998)
     ap.add_argument("--mlp-steps", type=int, default=4)
+    ap.add_argument("--mlp-batch", type=int, default=1 << 18, help="learned guide: radiance samples per Adam step")
     ap.add_argument("--ref-cache", default=None, help="npy file keeping the converged image between study runs")
     ap.add_argument("--save-images", default=None, help="directory for the study's final plain and guided images")
     ap.add_argument("--guide-depth", type=int, default=0, help="guide the first N bounces only (0: all)")
