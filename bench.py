@@ -545,25 +545,31 @@ def run_relmse_study(args) -> dict:
                  "target": "indirect" if args.mlp_indirect else "full incident radiance"}
     else:
         # QuadTree (directions) or PSS (primary samples): train the cache over
-        # `train_iters` iterations of 1, 2, 4, ... frames (the first unguided,
-        # the rest guided by the previous cache; every iteration's records
-        # rebuild the cache, in the domain of the mode that recorded them),
-        # all timed.
+        # `train_iters` iterations of train_first x 1, 2, 4, ... frames (the
+        # first unguided, the rest guided by the previous cache; every
+        # iteration's records rebuild the cache, in the domain of the mode
+        # that recorded them, weighted by Lum(Li) |cos| / pdf), all timed.
+        # The training frames are unbiased samples too and stay in the image.
         mode = abi.MODE_GUIDED_PSS if args.guide == "pss" else abi.MODE_GUIDED_QUADTREE
+        ctx.guide_configure(region_records=args.qt_region, refine_fraction=args.qt_refine,
+                            clamp_median=args.qt_clamp, uniform_share=args.qt_uniform,
+                            compensate=args.qt_compensate)
+        builds = []
         for it in range(args.train_iters):
-            ctx.clear()
-            n = (1 << it) if it else args.train_first
+            n = args.train_first << it
             m = abi.MODE_PLAIN if (it == 0 and args.guide == "quadtree") else mode
             train_ms += render_ms(n, m, 11 + it, record_paths=n, guide_fraction=args.guide_fraction)
-            train_ms += ctx.cache_stats().build_ms
+            builds.append(ctx.cache_stats().build_ms)
+            train_ms += builds[-1]
             train_spp += n
-        extra = {"train_iters": args.train_iters, "cache_records": ctx.cache_stats().records}
-        ctx.clear()
+        extra = {"train_iters": args.train_iters, "train_first": args.train_first,
+                 "cache_records": ctx.cache_stats().records, "cache_build_ms": builds,
+                 "guide_params": ctx.guide_params()}
     guided_ms = 0.0
     curve = []
-    reached_ms = None
+    reached_ms = reached_chunk_ms = None
     chunk = max(1, args.plain_spp // 32)
-    total = train_spp if args.guide == "mlp" else 0
+    total = train_spp
     while total < 4 * args.plain_spp:
         guided_ms += render_ms(chunk, mode, 17 + total, guide_fraction=args.guide_fraction,
                                guide_depth=args.guide_depth)
@@ -573,6 +579,14 @@ def run_relmse_study(args) -> dict:
         curve.append((total, train_ms + guided_ms, err, other(img, ref)))
         if reached_ms is None and err <= plain_err:
             reached_ms = train_ms + guided_ms
+            if len(curve) >= 2:
+                # between the last two points, 1 / relMSE grows linearly in
+                # time (relMSE ~ 1 / t): the crossing inside this chunk
+                (_, t0, e0, _), (_, t1, e1, _) = curve[-2], curve[-1]
+                if e0 > plain_err > 0 and e1 > 0:
+                    f = (1.0 / plain_err - 1.0 / e0) / (1.0 / e1 - 1.0 / e0)
+                    reached_ms = t0 + f * (t1 - t0)
+            reached_chunk_ms = train_ms + guided_ms
         if train_ms + guided_ms >= 2.0 * plain_ms and reached_ms is not None:
             break
         if train_ms + guided_ms >= 4.0 * plain_ms:
@@ -584,7 +598,14 @@ def run_relmse_study(args) -> dict:
             eq_err = e0 + (e1 - e0) * (plain_ms - t0) / max(t1 - t0, 1e-9)
     # the same ratio under the other metric (robust <-> plain relMSE)
     plain_other = other(plain_img, ref)
-    reached_other = next((t for _, t, _, e in curve if e <= plain_other), None)
+    reached_other = None
+    for k, (_, t, _, e) in enumerate(curve):
+        if e <= plain_other:
+            reached_other = t
+            if k > 0 and curve[k - 1][3] > plain_other > 0 and e > 0:
+                t0, e0 = curve[k - 1][1], curve[k - 1][3]
+                reached_other = t0 + (1.0 / plain_other - 1.0 / e0) / (1.0 / e - 1.0 / e0) * (t - t0)
+            break
     guided_img = image()
     if args.save_images:
         d = Path(args.save_images)
@@ -602,7 +623,8 @@ def run_relmse_study(args) -> dict:
                   "rrmse_metrics_h": rrmse_reference_metric(plain_img, ref)},
         "guided": dict(extra, guide=args.guide, train_spp=train_spp, train_ms=train_ms,
                        guide_fraction=args.guide_fraction, spp_rendered=total,
-                       ms_to_plain_error=reached_ms, relmse_at_plain_time=eq_err,
+                       ms_to_plain_error=reached_ms, ms_to_plain_error_chunk_end=reached_chunk_ms,
+                       relmse_at_plain_time=eq_err,
                        rrmse_metrics_h_final=rrmse_reference_metric(guided_img, ref),
                        curve=[{"spp": a, "ms": b, "relmse": c, "relmse_other_metric": d} for a, b, c, d in curve]),
         "time_ratio_guided_over_plain": (reached_ms / plain_ms) if reached_ms else None,
@@ -1003,8 +1025,14 @@ def main() -> None:
     ap.add_argument("--ref-spp", type=int, default=16384)
     ap.add_argument("--plain-spp", type=int, default=1024)
     ap.add_argument("--train-iters", type=int, default=6)
-    ap.add_argument("--train-first", type=int, default=1, help="QuadTree/PSS study: frames of the first (unguided) cache pass")
+    ap.add_argument("--train-first", type=int, default=1,
+                    help="QuadTree/PSS study: frames of the first (unguided) cache pass; iteration k renders 2^k x as many")
     ap.add_argument("--guide-fraction", type=float, default=0.5)
+    ap.add_argument("--qt-region", type=int, default=1024, help="QuadTree guide: records per region")
+    ap.add_argument("--qt-refine", type=float, default=0.01, help="QuadTree guide: flux share that splits a cell")
+    ap.add_argument("--qt-clamp", type=float, default=10.0, help="QuadTree guide: flux clamp x median (0: none)")
+    ap.add_argument("--qt-uniform", type=float, default=0.2, help="QuadTree guide: uniform share of its samples")
+    ap.add_argument("--qt-compensate", type=float, default=0.0, help="QuadTree guide: MIS compensation (0: off)")
     ap.add_argument("--guide", choices=["mlp", "quadtree", "pss"], default="mlp")
     ap.add_argument("--metric", choices=["robust", "plain"], default="robust")
     ap.add_argument("--train-frames", type=int, default=64)

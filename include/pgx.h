@@ -392,6 +392,14 @@ int pgx_cache_get_stats(pgx_ctx* ctx, pgx_cache_stats* out);
 /* Copies the cache out: nodes (root first) and the records in leaf order. */
 int pgx_cache_export(pgx_ctx* ctx, pgx_cache_node* nodes, int64_t* nnodes,
                      pgx_path_vertex* records, int64_t* nrecords);
+/* Flux weight of each exported record, in the same order (extension; the
+ * QuadTree guide's deposits): Lum(Li) |cos(normal, wi)| / pdf(wi) for the
+ * records of plain, QuadTree, PSS and learned-guide renders (pdf: the density
+ * wi was sampled with, so the weights estimate Li |cos| whatever sampled
+ * them, Mueller et al. 2017), Lum(Li) for host records and guided-Li
+ * records; non-finite or negative weights are 0.  weights == NULL: count
+ * only. */
+int pgx_cache_export_weights(pgx_ctx* ctx, float* weights, int64_t* nrecords);
 /* k nearest cached records to each query point (extension; the reference
  * has no cache query).  idx is nq*k record indices into the exported record
  * order (-1 when fewer than k exist), d2 the squared distances, ascending,
@@ -405,15 +413,45 @@ int pgx_cache_knn(pgx_ctx* ctx, const float* queries, int64_t nq, int32_t k,
  * pdf of direction dirs[i] under the QuadTree alone (0 where the region has
  * no recorded flux); pgx_guide_sample maps two uniforms u2[2i], u2[2i+1] to a
  * QuadTree direction and its pdf (pdf 0 and direction (0,0,1) when the
- * region has no flux).  The renderer mixes this distribution with a 20 %
- * uniform share.  positions, dirs: n*3 floats. */
+ * region has no flux).  The renderer mixes this distribution with a
+ * uniform share (pgx_guide_params).  positions, dirs: n*3 floats. */
 int pgx_guide_pdf(pgx_ctx* ctx, const float* positions, const float* dirs, int64_t n, float* pdf);
 int pgx_guide_sample(pgx_ctx* ctx, const float* positions, const float* u2, int64_t n, float* dirs, float* pdf);
 
+/* Parameters of the QuadTree guide (extension; Mueller et al. 2017 fix rho =
+ * 1 % and leave the rest to the implementation).  Defaults in brackets.
+ *   region_records  regions are the point-BVH subtrees whose record count
+ *                   first drops to this (256 .. 2^20) [1024]
+ *   refine_fraction a quadtree cell is split while one of its children holds
+ *                   more than this share of the region's flux (0, 1] [0.01]
+ *   clamp_median    a record's flux (luminance of Li) is clamped at this
+ *                   multiple of the region's median flux; 0: no clamp [10]
+ *   uniform_share   share of the guide's samples drawn uniformly over the
+ *                   sphere (or the primary-sample square) [0, 1) [0.2]
+ *   compensate      MIS compensation (Karlik et al. 2019): every leaf's flux
+ *                   less compensate x the region's mean flux over the leaf's
+ *                   area, floored at 0, so the guide concentrates on what
+ *                   the BSDF samples poorly; regions left with under 5 % of
+ *                   their flux keep the plain tree; 0: off [0, 4] [0]
+ * region_records, refine_fraction, clamp_median and compensate shape the next
+ * cache build; uniform_share applies to every later render and guide query. */
+typedef struct pgx_guide_params {
+    int32_t region_records;
+    float refine_fraction;
+    float clamp_median;
+    float uniform_share;
+    float compensate;
+} pgx_guide_params;
+/* params == NULL restores the defaults; out-of-range values are rejected
+ * with PGX_ERR_INVALID_ARG and change nothing. */
+int pgx_guide_configure(pgx_ctx* ctx, const pgx_guide_params* params);
+int pgx_guide_get_params(pgx_ctx* ctx, pgx_guide_params* out);
+
 /* One region of the QuadTree guide: the point-BVH subtree (root node `node`)
- * whose record count first drops to 1,024 (the whole cache when it holds at
- * most 1,024 records), owning records [first, first + count) of the exported
- * record order; its quadtree starts at quad node `qroot` (-1: no flux). */
+ * whose record count first drops to pgx_guide_params.region_records (the
+ * whole cache when it holds at most that many records), owning records
+ * [first, first + count) of the exported record order; its quadtree starts
+ * at quad node `qroot` (-1: no flux). */
 typedef struct pgx_guide_region {
     int32_t first;
     int32_t count;

@@ -10,7 +10,8 @@ the published method pgx follows instead:
 * Müller, Gross, Novák, "Practical Path Guiding for Efficient Light-Transport
   Simulation" (EGSR 2017), §3-4: a directional quadtree per spatial region
   over a cylindrical equal-area map of the sphere, built from radiance
-  records whose flux is the luminance of Li; a cell is subdivided while it
+  records whose flux estimates Li |cos| (the renderer's weight Lum(Li) |cos| /
+  pdf; the luminance of Li for records without one); a cell is subdivided while it
   holds more than a fraction rho = 1 % of the region's flux; the pdf is the
   product of 4 x (child flux / cell flux) along the descent; sampling picks
   children in proportion to flux and maps the remaining uniforms into the
@@ -20,12 +21,15 @@ the published method pgx follows instead:
   (MyMath.h:412-423) and the cosine sampler's inverse of
   DiffuseBSDF::invert (Materials.h:163-171) for trees over the BSDF's
   primary samples (the reference's intended design, Renderer.h:403-414).
-* pgx's own bounds: spatial regions are the point-BVH subtrees (the
-  reference's PointBVHNode, Renderer.h:71-234) whose record count first
-  drops to 1,024; records are clamped at 10 x the region's median positive
-  luminance (the median found by 24 bisection steps on the value); at most
+* pgx's own bounds (pgx_guide_params; defaults in brackets): spatial
+  regions are the point-BVH subtrees (the reference's PointBVHNode,
+  Renderer.h:71-234) whose record count first drops to region_records
+  [1,024]; records are clamped at clamp_median [10] x the region's median
+  positive luminance (the median found by 24 bisection steps on the value;
+  0 = no clamp); cells are refined at refine_fraction [rho = 1 %]; at most
   256 cells per region and depth 10; a child is only refined when it holds
-  at least 2 records; the guide mixes the tree with a 20 % uniform share.
+  at least 2 records; optionally MIS compensation of the leaves (Karlík et
+  al. 2019) [off]; the guide mixes the tree with a uniform share [20 %].
 
 Decisions (median, membership of a record in a cell) use float32 arithmetic
 in the kernel's operation order so that the trees come out node for node the
@@ -136,13 +140,14 @@ def subtree_ranges(nodes: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
     return first, count
 
 
-def regions_from_bvh(nodes: np.ndarray, n_records: int) -> list[tuple[int, int, int]]:
+def regions_from_bvh(nodes: np.ndarray, n_records: int,
+                     region_max: int = REGION_MAX) -> list[tuple[int, int, int]]:
     """(first, count, node) of every region, in record order: the subtrees
-    whose record count first drops to REGION_MAX (the root when the cache
+    whose record count first drops to region_max (the root when the cache
     holds at most that many records)."""
     if n_records == 0 or len(nodes) == 0:
         return []
-    if n_records <= REGION_MAX:
+    if n_records <= region_max:
         return [(0, n_records, 0)]
     first, count = subtree_ranges(nodes)
     out = []
@@ -152,7 +157,7 @@ def regions_from_bvh(nodes: np.ndarray, n_records: int) -> list[tuple[int, int, 
         if nodes[i]["left"] < 0:
             continue  # a leaf of a region above the bound cannot exist (leaves hold <= 8)
         for c in (int(nodes[i]["left"]), int(nodes[i]["right"])):
-            if count[c] <= REGION_MAX:
+            if count[c] <= region_max:
                 out.append((int(first[c]), int(count[c]), c))
             else:
                 stack.append(c)
@@ -174,15 +179,56 @@ def median_bisection(w: np.ndarray) -> F:
     return hi
 
 
-def build_quadtree(records: np.ndarray, pss: bool = False):
+def flux_weights(w) -> np.ndarray:
+    """Given per-record flux weights, float32, non-finite or non-positive -> 0."""
+    w = np.asarray(w, F)
+    with np.errstate(invalid="ignore"):
+        ok = np.isfinite(w) & (w > 0)
+    return np.where(ok, w, F(0.0)).astype(F)
+
+
+def compensate_tree(tree, alpha: float):
+    """MIS compensation (Karlík, Šik, Vévoda, Skřivan, Křivánek, "MIS
+    compensation: optimizing sampling techniques in multiple importance
+    sampling", SIGGRAPH Asia 2019) of a quadtree: every leaf loses alpha x
+    the tree's mean flux over its area (floored at 0), interior cells are
+    the sums of their children; a tree left with under 5 % of its flux is
+    returned unchanged."""
+    depth = [0] * len(tree)
+    for i, (_, child) in enumerate(tree):
+        for c in child:
+            if c >= 0:
+                depth[c] = depth[i] + 1
+    tot = sum(tree[0][0])
+    comp = [0.0] * len(tree)
+    for i in range(len(tree) - 1, -1, -1):
+        flux, child = tree[i]
+        sub = alpha * tot * 4.0 ** -(depth[i] + 1)
+        comp[i] = sum(comp[c] if c >= 0 else max(f - sub, 0.0) for f, c in zip(flux, child))
+    if comp[0] < 0.05 * tot:
+        return tree
+    out = []
+    for i, (flux, child) in enumerate(tree):
+        sub = alpha * tot * 4.0 ** -(depth[i] + 1)
+        out.append(([comp[c] if c >= 0 else max(f - sub, 0.0) for f, c in zip(flux, child)], child))
+    return out
+
+
+def build_quadtree(records: np.ndarray, pss: bool = False, clamp_median: float = float(CLAMP_MEDIAN),
+                   rho: float = RHO, weights=None, compensate: float = 0.0):
     """One region's quadtree: list of (flux[4] float64, child[4]) in
     breadth-first order (cell 0 the root), or None when the region has no
-    flux."""
-    w = luminance(records["Li"])
+    flux.  A record's flux is its weight (the renderer's Lum(Li) |cos| / pdf,
+    which estimates Li |cos| whatever distribution sampled wi; Müller et
+    al. 2017 divide by the pdf too) or, without weights, Lum(Li)."""
+    w = luminance(records["Li"]) if weights is None else flux_weights(weights)
     if not np.any(w > 0):
         return None
-    clamp = F(CLAMP_MEDIAN * median_bisection(w))
-    wc = np.minimum(w, clamp).astype(np.float64)
+    if clamp_median > 0:
+        clamp = F(F(clamp_median) * median_bisection(w))
+        wc = np.minimum(w, clamp).astype(np.float64)
+    else:
+        wc = w.astype(np.float64)
     total = float(wc.sum())
     if not (total > 0) or not np.isfinite(total):
         return None
@@ -193,7 +239,7 @@ def build_quadtree(records: np.ndarray, pss: bool = False):
         ok = np.ones(len(u), bool)
     keep = (w > 0) & ok
     u, v, wc = u[keep], v[keep], wc[keep]
-    thresh = RHO * total
+    thresh = rho * total
     cells = [(F(0), F(0), F(1), 0)]
     out = []
     head = 0
@@ -215,7 +261,7 @@ def build_quadtree(records: np.ndarray, pss: bool = False):
                 child[c] = len(cells)
                 cells.append((F(u0 + F(half * F(c & 1))), F(v0 + F(half * F(c >> 1))), half, depth + 1))
         out.append((flux, child))
-    return out
+    return compensate_tree(out, compensate) if compensate > 0 else out
 
 
 def quad_pdf(tree, u: float, v: float) -> float:
@@ -294,10 +340,14 @@ class Guide:
     """The whole guide over an exported cache (point-BVH nodes and records
     in leaf order)."""
 
-    def __init__(self, nodes: np.ndarray, records: np.ndarray, pss: bool = False):
+    def __init__(self, nodes: np.ndarray, records: np.ndarray, pss: bool = False, region_max: int = REGION_MAX,
+                 clamp_median: float = float(CLAMP_MEDIAN), rho: float = RHO, weights=None,
+                 compensate: float = 0.0):
         self.nodes = nodes
-        self.regions = regions_from_bvh(nodes, len(records))
-        self.trees = [build_quadtree(records[f:f + c], pss) for f, c, _ in self.regions]
+        self.regions = regions_from_bvh(nodes, len(records), region_max)
+        self.trees = [build_quadtree(records[f:f + c], pss, clamp_median, rho,
+                                     None if weights is None else weights[f:f + c], compensate)
+                      for f, c, _ in self.regions]
         self.root_region = {node: i for i, (_, _, node) in enumerate(self.regions)}
 
     def tree_at(self, x):

@@ -107,6 +107,11 @@ class CacheStats(C.Structure):
                 ("mean_leaf_depth", C.c_double), ("build_ms", C.c_double)]
 
 
+class GuideParams(C.Structure):
+    _fields_ = [("region_records", C.c_int32), ("refine_fraction", C.c_float), ("clamp_median", C.c_float),
+                ("uniform_share", C.c_float), ("compensate", C.c_float)]
+
+
 class BatchTuning(C.Structure):
     _fields_ = [("wave_paths", C.c_int64), ("trace_blocks_per_sm", C.c_int32), ("shade_blocks_per_sm", C.c_int32),
                 ("stack_shared", C.c_int32)]
@@ -151,10 +156,13 @@ SIGNATURES = {
     "pgx_cache_build_from_render": (C.c_int, [_P]),
     "pgx_cache_get_stats": (C.c_int, [_P, C.POINTER(CacheStats)]),
     "pgx_cache_export": (C.c_int, [_P, _P, C.POINTER(_I64), _P, C.POINTER(_I64)]),
+    "pgx_cache_export_weights": (C.c_int, [_P, _P, C.POINTER(_I64)]),
     "pgx_cache_knn": (C.c_int, [_P, _P, _I64, _I32, _P, _P]),
     "pgx_guide_pdf": (C.c_int, [_P, _P, _P, _I64, _P]),
     "pgx_guide_sample": (C.c_int, [_P, _P, _P, _I64, _P, _P]),
     "pgx_guide_export": (C.c_int, [_P, _P, C.POINTER(_I32), _P, C.POINTER(_I32)]),
+    "pgx_guide_configure": (C.c_int, [_P, C.POINTER(GuideParams)]),
+    "pgx_guide_get_params": (C.c_int, [_P, C.POINTER(GuideParams)]),
     "pgx_mlp_init": (C.c_int, [_P, C.c_uint64, _P, _P]),
     "pgx_mlp_get_params": (C.c_int, [_P, _P]),
     "pgx_mlp_set_params": (C.c_int, [_P, _P]),

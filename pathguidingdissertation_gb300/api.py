@@ -217,6 +217,15 @@ class Context:
         self.check(self.lib.pgx_cache_export(self.h, ptr(nodes), C.byref(nn), ptr(recs), C.byref(nr)))
         return nodes, recs
 
+    def cache_weights(self) -> np.ndarray:
+        """The QuadTree guide's flux weight of each exported record
+        (pgx_cache_export_weights)."""
+        nr = C.c_int64()
+        self.check(self.lib.pgx_cache_export_weights(self.h, None, C.byref(nr)))
+        w = np.zeros(nr.value, np.float32)
+        self.check(self.lib.pgx_cache_export_weights(self.h, ptr(w), C.byref(nr)))
+        return w
+
     def guide_pdf(self, positions: np.ndarray, dirs: np.ndarray) -> np.ndarray:
         p = np.ascontiguousarray(positions, np.float32).reshape(-1, 3)
         d = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
@@ -241,6 +250,20 @@ class Context:
         if nreg.value:
             self.check(self.lib.pgx_guide_export(self.h, ptr(regions), C.byref(nreg), ptr(qnodes), C.byref(pss)))
         return regions, qnodes, bool(pss.value)
+
+    def guide_configure(self, region_records: int = 1024, refine_fraction: float = 0.01,
+                        clamp_median: float = 10.0, uniform_share: float = 0.2, compensate: float = 0.0) -> None:
+        """QuadTree guide parameters (pgx_guide_configure): region size,
+        refinement share, flux clamp and MIS compensation shape the next
+        cache build; the uniform share applies to later renders and
+        queries."""
+        gp = abi.GuideParams(region_records, refine_fraction, clamp_median, uniform_share, compensate)
+        self.check(self.lib.pgx_guide_configure(self.h, C.byref(gp)))
+
+    def guide_params(self) -> dict:
+        gp = abi.GuideParams()
+        self.check(self.lib.pgx_guide_get_params(self.h, C.byref(gp)))
+        return {f: getattr(gp, f) for f, _ in gp._fields_}
 
     # ---- learned guide ----
     def mlp_init(self, seed: int = 1, bmin=None, bmax=None) -> None:

@@ -14,6 +14,7 @@
 // quickselect.
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <vector>
 
 #include "pgx_ctx.h"
@@ -26,7 +27,6 @@ constexpr int kSmall = 256;      // one-thread subtrees at or below this size
 constexpr int kChunk = 2048;
 constexpr int kThreads = 256;
 constexpr int kPer = kChunk / kThreads;
-constexpr int kRegionMax = 1024;  // guide region size bound
 constexpr int kStack = 128;
 
 struct PItem {
@@ -50,6 +50,8 @@ struct PMisc {
 
 struct CacheState {
     DevBuf recs_in, recs, pos, idx, idx2, nodes, trav, items, items2, hist, chunks, small, misc, regions, region_of;
+    DevBuf wts_in, wts;  // flux weight per record (input order, then leaf order)
+    DevBuf uvs;          // quadtree coordinates of each record's wi, leaf order (-1: outside the domain)
     DevBuf qroot, qnodes, knn_q, knn_i, knn_d, node_region;
     int64_t n_records = 0;
     int64_t n_nodes = 0;
@@ -81,7 +83,7 @@ __global__ void k_pos(const pgx_path_vertex* __restrict__ r, int64_t n, float4* 
 }
 
 __global__ void k_root(const float4* __restrict__ pos, int64_t n, PMisc* misc, pgx_cache_node* nodes, PItem* items,
-                       int* small, int* acc) {
+                       int* small, int* acc, int region_max) {
     // acc: 6 ordered ints reduced by k_root_bounds
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
     pgx_cache_node& r = nodes[0];
@@ -97,7 +99,7 @@ __global__ void k_root(const float4* __restrict__ pos, int64_t n, PMisc* misc, p
     misc->nsmall = 0;
     misc->nregions = 0;
     misc->overflow = 0;
-    if (n <= kRegionMax) misc->nregions = 1;  // region 0 = the root, written by the host
+    if (n <= region_max) misc->nregions = 1;  // region 0 = the root, written by the host
     if (n <= kLeafMax) return;
     if (n <= kSmall) {
         small[0] = 0;
@@ -319,7 +321,7 @@ __global__ void k_pcopy(const PItem* __restrict__ items, const int2* __restrict_
 }
 
 __global__ void k_pcommit(PItem* items, int nitems, PItem* next, int next_cap, int* small, int small_cap,
-                          pgx_cache_node* nodes, int2* regions, int* node_region, PMisc* misc) {
+                          pgx_cache_node* nodes, int2* regions, int* node_region, PMisc* misc, int region_max) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nitems) return;
     PItem& it = items[i];
@@ -341,7 +343,7 @@ __global__ void k_pcommit(PItem* items, int nitems, PItem* next, int next_cap, i
         ch.left = ch.right = -1;
         ch.offset = cs;
         ch.used = cn;
-        if (cn <= kRegionMax && it.used > kRegionMax) {
+        if (cn <= region_max && it.used > region_max) {
             int r = atomicAdd(&misc->nregions, 1);
             regions[r] = make_int2(cs, cn);
             node_region[c + side] = r;
@@ -445,10 +447,38 @@ __global__ void k_psmall(const int* __restrict__ small, PMisc* misc, int* idx, c
     }
 }
 
-__global__ void k_gather(const pgx_path_vertex* __restrict__ in, const int* __restrict__ idx, int64_t n,
-                         pgx_path_vertex* __restrict__ out) {
+// Default flux weight of a record: the luminance of its Li.  The quadtree
+// build clamps weights at clamp_median x the region's median weight
+// (pgx_guide_params; 0 = no clamp) so that a few very bright records (the
+// sun seen through a specular chain) need not take the whole distribution.
+__device__ __forceinline__ float record_lum(const pgx_path_vertex& v) {
+    float w = ((0.2126f * v.Li[0]) + (0.7152f * v.Li[1])) + (0.0722f * v.Li[2]);
+    return (isfinite(w) && w > 0.f) ? w : 0.f;
+}
+
+// Records into leaf order, with their flux weights (the given ones, the
+// renderer's Lum(Li) |cos| / pdf, or Lum(Li); non-finite or negative -> 0)
+// and the quadtree coordinates of their wi: the cylindrical map of the
+// direction, or the diffuse sampler's primary sample (pss; (-1, -1) below
+// the hemisphere, which no cell contains).
+__global__ void k_gather(const pgx_path_vertex* __restrict__ in, const float* __restrict__ w_in,
+                         const int* __restrict__ idx, int64_t n, pgx_path_vertex* __restrict__ out,
+                         float* __restrict__ w_out, float2* __restrict__ uv_out, int pss) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = in[idx[i]];
+    if (i >= n) return;
+    const int j = idx[i];
+    const pgx_path_vertex v = in[j];
+    out[i] = v;
+    float w = w_in ? w_in[j] : record_lum(v);
+    w_out[i] = (isfinite(w) && w > 0.f) ? w : 0.f;
+    const F3 wi = f3(v.wi[0], v.wi[1], v.wi[2]);
+    float u, vv;
+    if (pss) {
+        if (!pss_uv(f3(v.normal[0], v.normal[1], v.normal[2]), wi, u, vv)) u = vv = -1.f;
+    } else {
+        dir_to_uv(wi, u, vv);
+    }
+    uv_out[i] = make_float2(u, vv);
 }
 
 __global__ void k_trav(const pgx_cache_node* __restrict__ nodes, int64_t nn, CacheTravNode* __restrict__ out) {
@@ -473,16 +503,6 @@ __global__ void k_regions(const int2* __restrict__ regions, int nreg, const pgx_
     }
 }
 
-// Record weight for the guide: luminance of Li, clamped at kClampMedian x the
-// region's median luminance so that a few very bright records (the sun seen
-// through a specular chain) do not take the whole distribution.
-constexpr float kClampMedian = 10.f;
-
-__device__ __forceinline__ float record_lum(const pgx_path_vertex& v) {
-    float w = ((0.2126f * v.Li[0]) + (0.7152f * v.Li[1])) + (0.0722f * v.Li[2]);
-    return (isfinite(w) && w > 0.f) ? w : 0.f;
-}
-
 __device__ __forceinline__ float warp_sum(float v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
     return v;
@@ -498,22 +518,25 @@ __device__ __forceinline__ int warp_sum_i(int v) {
 constexpr int kQtWarps = 4;
 
 __global__ void __launch_bounds__(32 * kQtWarps) k_quadtree(const int2* __restrict__ regions, int nreg,
-                                                            const pgx_path_vertex* __restrict__ recs,
+                                                            const float2* __restrict__ uvs,
+                                                            const float* __restrict__ wts,
                                                             int* __restrict__ qroot, QuadNode* __restrict__ qnodes,
-                                                            int pss) {
+                                                            float clamp_median, float refine, float compensate) {
     __shared__ float s_u[kQtWarps][PGX_QT_MAX_NODES], s_v[kQtWarps][PGX_QT_MAX_NODES],
-        s_s[kQtWarps][PGX_QT_MAX_NODES];
+        s_s[kQtWarps][PGX_QT_MAX_NODES], s_c[kQtWarps][PGX_QT_MAX_NODES];
     __shared__ unsigned char s_d[kQtWarps][PGX_QT_MAX_NODES];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int r = blockIdx.x * kQtWarps + warp;
     if (r >= nreg) return;  // uniform per warp
     int2 g = regions[r];
-    const pgx_path_vertex* rr = recs + g.x;
-    // Median of the positive luminances by bisection on the value.
+    const float2* ruv = uvs + g.x;
+    const float* rw = wts + g.x;
+    // Median of the positive luminances by bisection on the value (only
+    // needed for the clamp).
     float lo = FLT_MAX, hi = 0.f;
     int pos = 0;
     for (int i = lane; i < g.y; i += 32) {
-        float w = record_lum(rr[i]);
+        float w = rw[i];
         if (w > 0.f) {
             lo = fminf(lo, w);
             hi = fmaxf(hi, w);
@@ -530,11 +553,11 @@ __global__ void __launch_bounds__(32 * kQtWarps) k_quadtree(const int2* __restri
         return;
     }
     const int half_count = (pos + 1) / 2;
-    for (int it = 0; it < 24; it++) {
+    for (int it = 0; it < (clamp_median > 0.f ? 24 : 0); it++) {
         float mid = 0.5f * (lo + hi);
         int below = 0;
         for (int i = lane; i < g.y; i += 32) {
-            float w = record_lum(rr[i]);
+            float w = rw[i];
             if (w > 0.f && w <= mid) below++;
         }
         below = warp_sum_i(below);
@@ -543,9 +566,9 @@ __global__ void __launch_bounds__(32 * kQtWarps) k_quadtree(const int2* __restri
         else
             lo = mid;
     }
-    const float clamp = kClampMedian * hi;
+    const float clamp = clamp_median > 0.f ? clamp_median * hi : FLT_MAX;
     float total = 0.f;
-    for (int i = lane; i < g.y; i += 32) total += fminf(record_lum(rr[i]), clamp);
+    for (int i = lane; i < g.y; i += 32) total += fminf(rw[i], clamp);
     total = warp_sum(total);
     if (!(total > 0.f) || !isfinite(total)) {
         if (lane == 0) qroot[r] = -1;
@@ -564,22 +587,17 @@ __global__ void __launch_bounds__(32 * kQtWarps) k_quadtree(const int2* __restri
     }
     __syncwarp();
     int nn = 1, head = 0;
-    const float thresh = 0.01f * total;
+    const float thresh = refine * total;
     while (head < nn) {
         int node = head++;
         float u0 = cu[node], v0 = cv[node], sz = cs[node], half = sz * 0.5f;
         float flux[4] = {0.f, 0.f, 0.f, 0.f};
         int cnt[4] = {0, 0, 0, 0};
         for (int i = lane; i < g.y; i += 32) {
-            float w = fminf(record_lum(rr[i]), clamp);
+            float w = fminf(rw[i], clamp);
             if (!(w > 0.f)) continue;
-            float u, vv;
-            const F3 wi = f3(rr[i].wi[0], rr[i].wi[1], rr[i].wi[2]);
-            if (pss) {
-                if (!pss_uv(f3(rr[i].normal[0], rr[i].normal[1], rr[i].normal[2]), wi, u, vv)) continue;
-            } else {
-                dir_to_uv(wi, u, vv);
-            }
+            const float2 uv = ruv[i];
+            const float u = uv.x, vv = uv.y;
             if (u < u0 || u >= u0 + sz || vv < v0 || vv >= v0 + sz) continue;
             int c = 2 * (vv >= v0 + half ? 1 : 0) + (u >= u0 + half ? 1 : 0);
             flux[c] += w;
@@ -603,6 +621,29 @@ __global__ void __launch_bounds__(32 * kQtWarps) k_quadtree(const int2* __restri
         }
         __syncwarp();
         if (lane == 0) out[node] = q;
+    }
+    if (compensate > 0.f && lane == 0) {
+        // MIS compensation: leaves lose compensate x the mean flux over their
+        // area (floored at 0); interior fluxes are the sums of their
+        // children, computed leaves-up (reverse breadth-first order).
+        const QuadNode root = out[0];
+        const float tot = ((root.flux[0] + root.flux[1]) + root.flux[2]) + root.flux[3];
+        float* comp = s_c[warp];
+        for (int node = nn - 1; node >= 0; node--) {
+            const QuadNode q = out[node];
+            const float sub = compensate * tot * ldexpf(1.f, -2 * (cd[node] + 1));
+            float sum = 0.f;
+            for (int c = 0; c < 4; c++) sum += q.child[c] >= 0 ? comp[q.child[c]] : fmaxf(q.flux[c] - sub, 0.f);
+            comp[node] = sum;
+        }
+        if (comp[0] >= 0.05f * tot) {
+            for (int node = 0; node < nn; node++) {
+                QuadNode q = out[node];
+                const float sub = compensate * tot * ldexpf(1.f, -2 * (cd[node] + 1));
+                for (int c = 0; c < 4; c++) q.flux[c] = q.child[c] >= 0 ? comp[q.child[c]] : fmaxf(q.flux[c] - sub, 0.f);
+                out[node] = q;
+            }
+        }
     }
     if (lane == 0) qroot[r] = 0;  // region-relative; k_rebase makes it absolute
 }
@@ -751,6 +792,7 @@ GuideView guide_view(const pgx_ctx* ctx) {
     g.qnodes = cs->qnodes.as<QuadNode>();
     g.node_region = cs->node_region.as<int>();
     g.pss = cs->pss ? 1 : 0;
+    g.uniform = ctx->guide.uniform_share;
     return g;
 }
 
@@ -770,7 +812,8 @@ bool guide_ready(const pgx_ctx* ctx) {
 }
 
 // Builds the cache from n records already on the device.
-int cache_build_device(pgx_ctx* ctx, const pgx_path_vertex* d_records, int64_t n, bool pss) {
+int cache_build_device(pgx_ctx* ctx, const pgx_path_vertex* d_records, int64_t n, bool pss,
+                       const float* d_weights) {
     CacheState* cs = cstate(ctx);
     cs->valid = false;
     cs->generation++;
@@ -789,9 +832,20 @@ int cache_build_device(pgx_ctx* ctx, const pgx_path_vertex* d_records, int64_t n
     const int64_t item_cap = n / (kSmall / 2) + 64;
     const int64_t chunk_cap = n / kChunk + item_cap + 64;
     const int64_t small_cap = n / (kLeafMax / 2) + 64;
-    const int64_t reg_cap = n / (kRegionMax / 4) + 64;
+    // Parameters of this build (later pgx_guide_configure calls shape the next one).
+    const int region_max = ctx->guide.region_records;
+    const float clamp_median = ctx->guide.clamp_median, refine = ctx->guide.refine_fraction;
+    const float compensate = ctx->guide.compensate;
+    const int64_t reg_cap = n / (region_max / 4) + 64;
     PGX_CUDA_TRY(ctx, cs->recs_in.reserve(sizeof(pgx_path_vertex) * n));
     PGX_CUDA_TRY(ctx, cs->recs.reserve(sizeof(pgx_path_vertex) * n));
+    PGX_CUDA_TRY(ctx, cs->wts.reserve(sizeof(float) * n));
+    PGX_CUDA_TRY(ctx, cs->uvs.reserve(sizeof(float2) * n));
+    if (d_weights) {
+        PGX_CUDA_TRY(ctx, cs->wts_in.reserve(sizeof(float) * n));
+        PGX_CUDA_TRY(ctx, cudaMemcpyAsync(cs->wts_in.p, d_weights, sizeof(float) * n, cudaMemcpyDeviceToDevice,
+                                          ctx->stream));
+    }
     PGX_CUDA_TRY(ctx, cs->pos.reserve(sizeof(float4) * n));
     PGX_CUDA_TRY(ctx, cs->idx.reserve(sizeof(int) * n));
     PGX_CUDA_TRY(ctx, cs->idx2.reserve(sizeof(int) * n));
@@ -808,7 +862,7 @@ int cache_build_device(pgx_ctx* ctx, const pgx_path_vertex* d_records, int64_t n
     // -1 everywhere; region roots get their region index (the root: region 0
     // when the whole cache is one region).
     PGX_CUDA_TRY(ctx, cudaMemsetAsync(cs->node_region.p, 0xFF, sizeof(int) * max_nodes, s));
-    if (n <= kRegionMax) PGX_CUDA_TRY(ctx, cudaMemsetAsync(cs->node_region.p, 0, sizeof(int), s));
+    if (n <= region_max) PGX_CUDA_TRY(ctx, cudaMemsetAsync(cs->node_region.p, 0, sizeof(int), s));
     if (d_records != cs->recs_in.as<pgx_path_vertex>())
         PGX_CUDA_TRY(ctx, cudaMemcpyAsync(cs->recs_in.p, d_records, sizeof(pgx_path_vertex) * n,
                                           cudaMemcpyDeviceToDevice, s));
@@ -829,7 +883,7 @@ int cache_build_device(pgx_ctx* ctx, const pgx_path_vertex* d_records, int64_t n
     int hacc[8] = {INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN, 0, 0};
     PGX_CUDA_TRY(ctx, cudaMemcpyAsync(acc, hacc, sizeof(hacc), cudaMemcpyHostToDevice, s));
     k_root_bounds<<<std::min<unsigned>(blocks_for(n, 256), 4 * pgx_num_sms()), 256, 0, s>>>(pos, n, acc);
-    k_root<<<1, 32, 0, s>>>(pos, n, misc, nodes, items, small, acc);
+    k_root<<<1, 32, 0, s>>>(pos, n, misc, nodes, items, small, acc, region_max);
     PGX_CUDA_TRY(ctx, cudaMemsetAsync(hist, 0, sizeof(int) * 256 * item_cap, s));
     PGX_CUDA_TRY(ctx, cudaGetLastError());
     int nitems = 0;
@@ -850,7 +904,7 @@ int cache_build_device(pgx_ctx* ctx, const pgx_path_vertex* d_records, int64_t n
         k_pcopy<<<grid, kThreads, 0, s>>>(items, chunks, misc, idx, idx2);
         k_pcommit<<<blocks_for(nitems, 128), 128, 0, s>>>(items, nitems, items2, (int)item_cap, small,
                                                           (int)small_cap, nodes, regions, cs->node_region.as<int>(),
-                                                          misc);
+                                                          misc, region_max);
         PGX_CUDA_TRY(ctx, cudaGetLastError());
         PGX_CUDA_TRY(ctx, cudaMemcpyAsync(&nitems, &misc->nitems_next, sizeof(int), cudaMemcpyDeviceToHost, s));
         PGX_CUDA_TRY(ctx, cudaStreamSynchronize(s));
@@ -865,21 +919,24 @@ int cache_build_device(pgx_ctx* ctx, const pgx_path_vertex* d_records, int64_t n
     PGX_CUDA_TRY(ctx, cudaStreamSynchronize(s));
     if (hm.overflow) return pgx_fail(ctx, PGX_ERR_OVERFLOW, "cache build: internal overflow (%d)", hm.overflow);
     cs->n_nodes = hm.node_count;
-    if (n <= kRegionMax) {
+    if (n <= region_max) {
         int2 r0 = make_int2(0, (int)n);
         PGX_CUDA_TRY(ctx, cudaMemcpyAsync(regions, &r0, sizeof(r0), cudaMemcpyHostToDevice, s));
         hm.nregions = 1;
     }
     cs->n_regions = hm.nregions;
     pgx_path_vertex* recs = cs->recs.as<pgx_path_vertex>();
-    k_gather<<<blocks_for(n, 256), 256, 0, s>>>(cs->recs_in.as<pgx_path_vertex>(), idx, n, recs);
+    k_gather<<<blocks_for(n, 256), 256, 0, s>>>(cs->recs_in.as<pgx_path_vertex>(),
+                                                d_weights ? cs->wts_in.as<float>() : nullptr, idx, n, recs,
+                                                cs->wts.as<float>(), cs->uvs.as<float2>(), pss ? 1 : 0);
     k_trav<<<blocks_for(cs->n_nodes, 256), 256, 0, s>>>(nodes, cs->n_nodes, cs->trav.as<CacheTravNode>());
     // Records carry their region id; leaves below regions are inside them.
     k_regions<<<std::max(1, cs->n_regions), 128, 0, s>>>(regions, cs->n_regions, recs, pos);
     PGX_CUDA_TRY(ctx, cs->qroot.reserve(sizeof(int) * std::max(1, cs->n_regions)));
     PGX_CUDA_TRY(ctx, cs->qnodes.reserve(sizeof(QuadNode) * PGX_QT_MAX_NODES * (size_t)std::max(1, cs->n_regions)));
     k_quadtree<<<blocks_for(cs->n_regions, kQtWarps), 32 * kQtWarps, 0, s>>>(
-        regions, cs->n_regions, recs, cs->qroot.as<int>(), cs->qnodes.as<QuadNode>(), pss ? 1 : 0);
+        regions, cs->n_regions, cs->uvs.as<float2>(), cs->wts.as<float>(), cs->qroot.as<int>(),
+        cs->qnodes.as<QuadNode>(), clamp_median, refine, compensate);
     k_rebase_children<<<std::max(1, cs->n_regions), 128, 0, s>>>(cs->qnodes.as<QuadNode>(), cs->qroot.as<int>(),
                                                                    cs->n_regions);
     k_rebase<<<blocks_for(cs->n_regions, 128), 128, 0, s>>>(cs->qroot.as<int>(), cs->n_regions);
@@ -892,6 +949,7 @@ int cache_build_device(pgx_ctx* ctx, const pgx_path_vertex* d_records, int64_t n
 
 int64_t render_vertex_count(pgx_ctx* ctx);
 const pgx_path_vertex* render_vertices(pgx_ctx* ctx);
+const float* render_vertex_weights(pgx_ctx* ctx);
 
 extern "C" int pgx_cache_build(pgx_ctx* ctx, const pgx_path_vertex* records, int64_t n) {
     if (!ctx) return PGX_ERR_INVALID_ARG;
@@ -912,7 +970,7 @@ extern "C" int pgx_cache_build_from_render(pgx_ctx* ctx) {
     const pgx_path_vertex* v = render_vertices(ctx);
     int64_t n = render_vertex_count(ctx);
     if (!v) return pgx_fail(ctx, PGX_ERR_STATE, "pgx_cache_build_from_render: no recorded path vertices");
-    return cache_build_device(ctx, v, n);
+    return cache_build_device(ctx, v, n, false, render_vertex_weights(ctx));
 }
 
 extern "C" int pgx_cache_get_stats(pgx_ctx* ctx, pgx_cache_stats* out) {
@@ -968,6 +1026,20 @@ extern "C" int pgx_cache_export(pgx_ctx* ctx, pgx_cache_node* nodes, int64_t* nn
         PGX_CUDA_TRY(ctx, cudaMemcpyAsync(records, cs->recs.p, sizeof(pgx_path_vertex) * cs->n_records,
                                           cudaMemcpyDeviceToHost, ctx->stream));
     PGX_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    return PGX_OK;
+}
+
+extern "C" int pgx_cache_export_weights(pgx_ctx* ctx, float* weights, int64_t* nrecords) {
+    if (!ctx) return PGX_ERR_INVALID_ARG;
+    ctx->err.clear();
+    CacheState* cs = static_cast<CacheState*>(ctx->cache_state);
+    if (!cs || !cs->valid) return pgx_fail(ctx, PGX_ERR_STATE, "pgx_cache_export_weights: no cache");
+    if (nrecords) *nrecords = cs->n_records;
+    if (weights && cs->n_records > 0) {
+        PGX_CUDA_TRY(ctx, cudaMemcpyAsync(weights, cs->wts.p, sizeof(float) * cs->n_records, cudaMemcpyDeviceToHost,
+                                          ctx->stream));
+        PGX_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    }
     return PGX_OK;
 }
 
@@ -1030,6 +1102,32 @@ extern "C" int pgx_guide_pdf(pgx_ctx* ctx, const float* positions, const float* 
 extern "C" int pgx_guide_sample(pgx_ctx* ctx, const float* positions, const float* u2, int64_t n, float* dirs,
                                 float* pdf) {
     return guide_query(ctx, positions, u2, n, 1, dirs, pdf);
+}
+
+extern "C" int pgx_guide_configure(pgx_ctx* ctx, const pgx_guide_params* params) {
+    if (!ctx) return PGX_ERR_INVALID_ARG;
+    ctx->err.clear();
+    const pgx_guide_params defaults{1024, 0.01f, 10.f, 0.2f, 0.f};
+    const pgx_guide_params p = params ? *params : defaults;
+    if (p.region_records < 256 || p.region_records > (1 << 20))
+        return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_guide_configure: region_records %d outside [256, 2^20]",
+                        (int)p.region_records);
+    if (!(p.refine_fraction > 0.f && p.refine_fraction <= 1.f))
+        return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_guide_configure: refine_fraction must be in (0, 1]");
+    if (!(p.clamp_median >= 0.f) || !std::isfinite(p.clamp_median))
+        return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_guide_configure: clamp_median must be finite and >= 0");
+    if (!(p.uniform_share >= 0.f && p.uniform_share < 1.f))
+        return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_guide_configure: uniform_share must be in [0, 1)");
+    if (!(p.compensate >= 0.f && p.compensate <= 4.f))
+        return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_guide_configure: compensate must be in [0, 4]");
+    ctx->guide = p;
+    return PGX_OK;
+}
+
+extern "C" int pgx_guide_get_params(pgx_ctx* ctx, pgx_guide_params* out) {
+    if (!ctx || !out) return PGX_ERR_INVALID_ARG;
+    *out = ctx->guide;
+    return PGX_OK;
 }
 
 extern "C" int pgx_guide_export(pgx_ctx* ctx, pgx_guide_region* regions, int32_t* nregions, pgx_quad_node* qnodes,

@@ -11,8 +11,9 @@
 // is the luminance of its Li (Mueller et al. 2017, "Practical Path Guiding").
 //
 // At a shading point the region is found by descending the point BVH; the
-// guide is the region's quadtree mixed with a 20 % uniform share, records are
-// weighted by their luminance clamped at 10x the region's median, and the
+// guide is the region's quadtree mixed with a uniform share (20 % by
+// default), records are weighted by their luminance, by default clamped at
+// 10x the region's median (pgx_guide_params in pgx.h), and the
 // continuation direction is drawn by one-sample MIS between the guide and
 // the BSDF (probability `guide_fraction` for the guide), and the combined
 // pdf is used both for the throughput and for the MIS weights of NEE and of
@@ -25,8 +26,6 @@
 
 #define PGX_QT_MAX_DEPTH 10
 #define PGX_QT_MAX_NODES 256
-// Share of the guide's samples drawn uniformly over the sphere (defensive).
-#define PGX_GUIDE_UNIFORM 0.2f
 
 // Interior quadtree cell: flux of its four children (index = 2*yhalf + xhalf
 // in (u, v)) and their node indices within the region (-1 = leaf).
@@ -52,6 +51,7 @@ struct GuideView {
     const QuadNode* __restrict__ qnodes;
     const int* __restrict__ node_region;  // region index of region-root nodes, else -1
     int pss;  // 1: the quadtrees are over the diffuse BSDF's primary samples, 0: over directions
+    float uniform;  // share of the guide's samples drawn uniformly (defensive)
 };
 
 GuideView guide_view(const pgx_ctx* ctx);
@@ -60,7 +60,9 @@ bool guide_ready(const pgx_ctx* ctx);
 // region count; 0 regions when there is no cache.
 uint64_t guide_generation(const pgx_ctx* ctx);
 int guide_regions(const pgx_ctx* ctx);
-int cache_build_device(pgx_ctx* ctx, const pgx_path_vertex* d_records, int64_t n, bool pss = false);
+// d_weights: flux weight per record (nullptr: the luminance of its Li).
+int cache_build_device(pgx_ctx* ctx, const pgx_path_vertex* d_records, int64_t n, bool pss = false,
+                       const float* d_weights = nullptr);
 
 __device__ __forceinline__ void dir_to_uv(F3 w, float& u, float& v) {
     float c = fminf(fmaxf(w.z, -1.f), 1.f);
@@ -233,7 +235,7 @@ __device__ __forceinline__ int guide_region_root(const GuideView& g, F3 x) {
 __device__ __forceinline__ float guide_pdf_dir(const GuideView& g, int qroot, F3 wi) {
     float u, v;
     dir_to_uv(wi, u, v);
-    return ((1.f - PGX_GUIDE_UNIFORM) * quad_pdf(g.qnodes, qroot, u, v) + PGX_GUIDE_UNIFORM) *
+    return ((1.f - g.uniform) * quad_pdf(g.qnodes, qroot, u, v) + g.uniform) *
            (1.f / (4.f * 3.14159265f));
 }
 
@@ -254,7 +256,7 @@ __device__ __forceinline__ bool pss_uv(F3 n, F3 wi, float& u, float& v) {
 __device__ __forceinline__ float guide_pdf_uv(const GuideView& g, int qroot, float u, float v) {
     u = fminf(fmaxf(u, 0.f), 0.99999994f);
     v = fminf(fmaxf(v, 0.f), 0.99999994f);
-    return (1.f - PGX_GUIDE_UNIFORM) * quad_pdf(g.qnodes, qroot, u, v) + PGX_GUIDE_UNIFORM;
+    return (1.f - g.uniform) * quad_pdf(g.qnodes, qroot, u, v) + g.uniform;
 }
 
 // Solid-angle pdf of the one-sample mixture at wi.
@@ -277,7 +279,7 @@ __device__ __forceinline__ F3 guided_sample(const GuideView& g, float frac, cons
         float r1 = pgx_rng_next(rng), r2 = pgx_rng_next(rng);
         float u, v;
         float pick = sel / frac;  // reuse the selection number for the uniform share
-        if (pick < PGX_GUIDE_UNIFORM) {
+        if (pick < g.uniform) {
             u = r1;
             v = r2;
         } else {
@@ -328,7 +330,7 @@ __device__ __forceinline__ F3 pss_guided_sample(const GuideView& g, float frac, 
     const float sel = pgx_rng_next(rng);
     const float r1 = pgx_rng_next(rng), r2 = pgx_rng_next(rng);
     float u = r1, v = r2;
-    if (sel < frac && sel / frac >= PGX_GUIDE_UNIFORM) quad_sample(g.qnodes, qroot, r1, r2, u, v);
+    if (sel < frac && sel / frac >= g.uniform) quad_sample(g.qnodes, qroot, r1, r2, u, v);
     FixedSampler fs{u, v, 0};
     float bp;
     F3 wi;

@@ -79,6 +79,7 @@ struct PathState {
     unsigned* wcount;  // [2 * (kMaxDepthCap + 2)] persistent-traversal work counters
     unsigned long long* stats;  // [0] ext rays [1] shadow rays [2,3] extend nodes/tris [4,5] shadow nodes/tris
     pgx_path_vertex* vertices;
+    float* vweight;   // per vertex: flux weight for the QuadTree guide (plain, QuadTree and PSS records)
     unsigned* nvertices;
     int64_t capacity;
     int64_t vcapacity;
@@ -96,7 +97,7 @@ struct PathState {
 struct RenderState {
     DevBuf o, d, T, L, hit, pix, rng, flags, nrec, q0, q1, sh_path, sh_o, sh_d, sh_c;
     DevBuf rec_pos, rec_nrm, rec_wi, rec_w, rec_e;
-    DevBuf counters, vertices, cqueue, ccount;
+    DevBuf counters, vertices, vweight, cqueue, ccount;
     DevBuf guide, fallback, rec_wo, rec_f, train, scene;
     int64_t capacity = 0;
     int rec_depth = 0;
@@ -106,6 +107,7 @@ struct RenderState {
     int64_t train_last = 0;   // samples the previous batch produced
     int64_t vcapacity = 0;
     int64_t nvertices_last = 0;
+    bool vweight_valid = false;  // the last recording wrote flux weights (not guided-Li)
     // captured frame graph
     cudaGraphExec_t graph = nullptr;
     int graph_mode = -1, graph_depth = -1, graph_batch = -1, graph_record = -1;
@@ -755,6 +757,7 @@ __global__ void __launch_bounds__(kThreads, kShadeBlocksPerSM) k_shade(SceneView
             // guided-Li record of this vertex (Renderer.h:419-427)
             F3 r_pos = zero3(), r_nrm = zero3(), r_wi = zero3(), r_w = zero3(), r_e = zero3();
             F3 r_wo = zero3(), r_f = zero3();
+            float r_pdf = 0.f;  // solid-angle pdf the continuation was sampled with
             bool r_store = false;
             if (CLS != 0 && id >= 0) {
                 Shading sd;
@@ -879,6 +882,7 @@ __global__ void __launch_bounds__(kThreads, kShadeBlocksPerSM) k_shade(SceneView
                                 // surfaces that sample through it.
                                 r_store = !spec && (MODE != PGX_MODE_GUIDED_PSS || pss_surface<KIND>(m));
                                 r_wi = wi;
+                                r_pdf = pdf;
                                 r_w = T;  // throughput after this vertex
                             }
                             float sgn = (dot(wi, sd.gn) >= 0.f) ? 1.f : -1.f;
@@ -935,7 +939,7 @@ __global__ void __launch_bounds__(kThreads, kShadeBlocksPerSM) k_shade(SceneView
                     ps.rec_pos[ri] = make_float4(r_pos.x, r_pos.y, r_pos.z, (cont && r_store) ? 1.f : 0.f);
                     if (cont && r_store) {
                         ps.rec_nrm[ri] = make_float4(r_nrm.x, r_nrm.y, r_nrm.z, 0.f);
-                        ps.rec_wi[ri] = make_float4(r_wi.x, r_wi.y, r_wi.z, 0.f);
+                        ps.rec_wi[ri] = make_float4(r_wi.x, r_wi.y, r_wi.z, r_pdf);
                         ps.rec_w[ri] = make_float4(r_w.x, r_w.y, r_w.z, 0.f);
                         if (MODE == PGX_MODE_GUIDED_MLP && fp.train) {
                             ps.rec_wo[ri] = make_float4(r_wo.x, r_wo.y, r_wo.z, 0.f);
@@ -1129,6 +1133,14 @@ __global__ void __launch_bounds__(kThreads) k_finalize(SceneView sv, PathState p
                     v.Li[1] = li.y;
                     v.Li[2] = li.z;
                     ps.vertices[slot] = v;
+                    // Flux weight for the QuadTree guide: Lum(Li) |cos| / pdf
+                    // (Mueller et al. 2017 divide by the sampling pdf).  Over
+                    // directions its expected density is Li |cos|, over the
+                    // cosine sampler's primary samples pi Li, whichever
+                    // distribution sampled wi, so training on guided paths
+                    // does not compound the previous guide.
+                    const float cos_n = fabsf(nr4.x * wi.x + nr4.y * wi.y + nr4.z * wi.z);
+                    ps.vweight[slot] = wi.w > 0.f ? lum(li) * cos_n / wi.w : 0.f;
                 }
             }
         }
@@ -1803,6 +1815,7 @@ int ensure_state(pgx_ctx* ctx, RenderState* rs, int64_t cap, int rec_depth, int6
     }
     if (vcap > rs->vcapacity) {
         PGX_CUDA_TRY(ctx, rs->vertices.reserve(sizeof(pgx_path_vertex) * vcap));
+        PGX_CUDA_TRY(ctx, rs->vweight.reserve(sizeof(float) * vcap));
         rs->vcapacity = vcap;
     }
     if (guide && rs->guide_capacity < rs->capacity) {
@@ -1864,6 +1877,7 @@ PathState path_view(RenderState* rs) {
     ps.stats = reinterpret_cast<unsigned long long*>(c + 4 * (kMaxDepthCap + 2));
     ps.nvertices = c + 4 * (kMaxDepthCap + 2) + 2 * kStats;
     ps.vertices = rs->vertices.as<pgx_path_vertex>();
+    ps.vweight = rs->vweight.as<float>();
     ps.capacity = rs->capacity;
     ps.vcapacity = rs->vcapacity;
     ps.guide = rs->guide.as<float4>();
@@ -2025,6 +2039,13 @@ const pgx_path_vertex* render_vertices(pgx_ctx* ctx) {
     return rs ? rs->vertices.as<pgx_path_vertex>() : nullptr;
 }
 
+// Flux weights of the recorded vertices (nullptr for guided-Li records,
+// which the guide weighs by Lum(Li)).
+const float* render_vertex_weights(pgx_ctx* ctx) {
+    RenderState* rs = static_cast<RenderState*>(ctx->render_state);
+    return (rs && rs->vweight_valid) ? rs->vweight.as<float>() : nullptr;
+}
+
 extern "C" int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t frames) {
     if (!ctx) return PGX_ERR_INVALID_ARG;
     ctx->err.clear();
@@ -2078,9 +2099,9 @@ extern "C" int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t fr
     // each, 6.4 GB): the depths where the queues have shrunk cost about the
     // same per wave whatever its size, so large waves amortise them (measured
     // on the 1280x720 interior: 1,726 Mrays/s at 4 spp per wave, 1,903 at 8,
-    // 1,998 at 16, 2,041 at 32).  Recording is bounded at 2^21 paths (per-depth
-    // vertex records cost 80 bytes per path and depth).
-    const int64_t target_paths = rec_depth ? (int64_t)(1 << 21) : (int64_t)(1 << 25);
+    // 1,998 at 16, 2,041 at 32).  Recording is bounded at 2^23 paths (per-depth
+    // vertex records cost 80 bytes per path and depth: 7 GB at depth 10).
+    const int64_t target_paths = rec_depth ? (int64_t)(1 << 23) : (int64_t)(1 << 25);
     int batch = (int)std::max<int64_t>(1, std::min<int64_t>(frames, target_paths / std::max<int64_t>(npix, 1)));
     if (train) batch = 1;  // one round of Adam steps after every frame
     const int64_t vcap = recording ? npix * (cfg->max_depth + 1) * (collect_hi - collect_lo) : 0;
@@ -2165,9 +2186,13 @@ extern "C" int pgx_render(pgx_ctx* ctx, const pgx_render_config* cfg, int32_t fr
     rst.ms_shadow = times.shadow;
     if (recording) {
         rs->nvertices_last = std::min<int64_t>(nv, rs->vcapacity);
+        rs->vweight_valid = cfg->mode != PGX_MODE_GUIDED_LI;
         rst.path_vertices = rs->nvertices_last;
+        // Guided-Li records (the reference's recorder) weigh by Lum(Li);
+        // the others by Lum(Li) |cos| / pdf.
         PGX_TRY(cache_build_device(ctx, rs->vertices.as<pgx_path_vertex>(), rs->nvertices_last,
-                                   cfg->mode == PGX_MODE_GUIDED_PSS));
+                                   cfg->mode == PGX_MODE_GUIDED_PSS,
+                                   render_vertex_weights(ctx)));
     }
     return PGX_OK;
 }

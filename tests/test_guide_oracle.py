@@ -126,3 +126,29 @@ def test_regions_from_a_median_split_tree():
         nodes[i]["left"], nodes[i]["right"], nodes[i]["offset"], nodes[i]["used"] = l, r, o, u
     assert go.regions_from_bvh(nodes, 3000) == [(0, 750, 3), (750, 750, 4), (1500, 750, 5), (2250, 750, 6)]
     assert go.regions_from_bvh(nodes[:1], 800) == [(0, 800, 0)]
+
+
+def test_mis_compensation():
+    """Compensated trees: each leaf's mass is its flux less alpha x the mean
+    flux over its area, floored at 0, renormalised; the density still
+    integrates to 1 and a uniform tree is left unchanged (nothing would
+    remain)."""
+    recs = lobes_records(4000, 5, lobes=3, spread=0.1)
+    plain = go.build_quadtree(recs)
+    comp = go.build_quadtree(recs, compensate=1.0)
+    assert [c for _, c in comp] == [c for _, c in plain]
+    lp, lc = _leaves(plain), _leaves(comp)
+    assert abs(sum(m for *_, m in lc) - 1.0) < 1e-12
+    kept = [max(m - h * h, 0.0) for (*_, h, m) in lp]  # mass - alpha * area, alpha = 1
+    norm = sum(kept)
+    for (u0, v0, h, m), k in zip(lc, kept):
+        assert abs(m - k / norm) <= 1e-9
+    # the compensated density is sharper where the plain one is high
+    assert max(m / (h * h) for *_, h, m in lc) > max(m / (h * h) for *_, h, m in lp)
+    # a uniform field: compensation would remove everything, the tree stays
+    rng = np.random.default_rng(6)
+    u = np.zeros(20000, PV)
+    d = rng.normal(size=(20000, 3))
+    u["wi"] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    u["Li"] = 1.0
+    assert go.build_quadtree(u, compensate=1.0) == go.build_quadtree(u)
