@@ -179,26 +179,46 @@ def cpu_baseline_reference(desc, frames_budget_s: float = 12.0) -> dict | None:
                       f"{rays} rays in {secs:.2f} s"}
 
 
-def prepare_mode(ctx, mode: int, depth: int) -> None:
-    """Untimed set-up of a guided estimator: the radiance cache from a 1-spp
-    guided-Li pass (QuadTree), or the learned guide trained online on 16
-    frames."""
+# Training recipes of the guides on the 1280x720 interior (measured with
+# --study relmse): the QuadTree guide from an unguided pass of 8 frames and a
+# guided pass of 16 (each rebuilding the cache), 16,384-record regions,
+# guide fraction 0.7; the learned guide trained online on 64 frames.
+QT_RECIPE = dict(train_first=8, train_iters=2, qt_region=16384, qt_refine=0.01, qt_clamp=10.0, qt_uniform=0.2,
+                 qt_compensate=0.0, guide_fraction=0.7)
+MLP_RECIPE = dict(guide_fraction=0.75, train_frames=64)
+
+
+def prepare_mode(ctx, mode: int, depth: int) -> float:
+    """Untimed set-up of a guided estimator (the QuadTree cache or the
+    learned guide, trained by the recipes above); returns the guide
+    fraction its renders use."""
     from pathguidingdissertation_gb300 import abi
-    ctx.clear()  # the guided-Li pass records its vertices only while SPP < 16 (Renderer.h:720-746)
+    ctx.clear()
     if mode == abi.MODE_GUIDED_QUADTREE:
-        ctx.render(1, mode=abi.MODE_GUIDED_LI, seed=99, max_depth=depth, record_paths=True)
+        r = QT_RECIPE
+        ctx.guide_configure(region_records=r["qt_region"], refine_fraction=r["qt_refine"],
+                            clamp_median=r["qt_clamp"], uniform_share=r["qt_uniform"],
+                            compensate=r["qt_compensate"])
+        for it in range(r["train_iters"]):
+            n = r["train_first"] << it
+            ctx.render(n, mode=abi.MODE_PLAIN if it == 0 else mode, seed=99 + it, max_depth=depth,
+                       record_paths=n, guide_fraction=r["guide_fraction"])
+        return r["guide_fraction"]
     if mode == abi.MODE_GUIDED_MLP:
         ctx.mlp_init(3)
         ctx.mlp_configure(lr=5e-3, decay=0.998, batch=1 << 18, steps=4)
-        ctx.render(16, mode=mode, seed=99, max_depth=depth, train_guide=True)
+        ctx.render(16, mode=mode, seed=99, max_depth=depth, train_guide=True,
+                   guide_fraction=MLP_RECIPE["guide_fraction"])
+        return MLP_RECIPE["guide_fraction"]
+    return 0.5
 
 
 def side_mode_rate(ctx, mode: int, depth: int, spp: int, steps: int, seed: int, flush, ranks) -> dict:
     """Mrays/s and Mpaths/s of one more estimator on the bench's workload."""
     import torch
-    prepare_mode(ctx, mode, depth)
+    frac = prepare_mode(ctx, mode, depth)
     ctx.clear()
-    ctx.render(spp, mode=mode, seed=seed, max_depth=depth, timing=True)  # warm-up
+    ctx.render(spp, mode=mode, seed=seed, max_depth=depth, timing=True, guide_fraction=frac)  # warm-up
     torch.cuda.synchronize()
     ranks.barrier()
     rays = paths = 0
@@ -206,7 +226,7 @@ def side_mode_rate(ctx, mode: int, depth: int, spp: int, steps: int, seed: int, 
     for _ in range(steps):
         flush.zero_()
         torch.cuda.synchronize()
-        ctx.render(spp, mode=mode, seed=seed, max_depth=depth, timing=True)
+        ctx.render(spp, mode=mode, seed=seed, max_depth=depth, timing=True, guide_fraction=frac)
         st = ctx.render_stats()
         rays += st.extension_rays + st.shadow_rays
         paths += st.paths
@@ -248,15 +268,15 @@ def run_pgx(args) -> dict:
     ctx = Context(ranks.local)
     ctx.upload(desc)
     ctx.bvh_build()
-    prepare_mode(ctx, mode, depth)
+    frac = prepare_mode(ctx, mode, depth)
     ctx.clear()
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     spp = args.spp_per_step
     for i in range(args.warmup):
-        ctx.render(spp, mode=mode, seed=seed, max_depth=depth, timing=True)
+        ctx.render(spp, mode=mode, seed=seed, max_depth=depth, timing=True, guide_fraction=frac)
     # Node/triangle fetch counts of one step of the same workload (the counting
     # traversal kernels; untimed).  The timed steps run the uncounted kernels.
-    ctx.render(spp, mode=mode, seed=seed, max_depth=depth, profile=True)
+    ctx.render(spp, mode=mode, seed=seed, max_depth=depth, profile=True, guide_fraction=frac)
     cst = ctx.render_stats()
     visits_per_ray = cst.extend_interior_visits / max(cst.extension_rays, 1)
     tris_per_ray = cst.extend_tri_tests / max(cst.extension_rays, 1)
@@ -271,7 +291,7 @@ def run_pgx(args) -> dict:
         for k in range(args.steps):
             flush.zero_()
             torch.cuda.synchronize()
-            ctx.render(spp, mode=mode, seed=seed, max_depth=depth, timing=True)
+            ctx.render(spp, mode=mode, seed=seed, max_depth=depth, timing=True, guide_fraction=frac)
             st = ctx.render_stats()
             rays += st.extension_rays + st.shadow_rays
             paths += st.paths
@@ -314,7 +334,7 @@ def run_pgx(args) -> dict:
     import ctypes as C
     from pathguidingdissertation_gb300.api import camera_struct
     cam = camera_struct(desc.camera)
-    cfg = abi.RenderConfig(mode, depth, seed, 0.5, 0, 0)
+    cfg = abi.RenderConfig(mode, depth, seed, frac, 0, 0)
     spp_read = C.c_int32()
     e2e_rays = 0
     ranks.barrier()
@@ -386,22 +406,33 @@ def run_pgx(args) -> dict:
     equal_time = None
     if not args.no_equal_time and ranks.world == 1 and args.workload == "interior" and not args.res:
         import copy
-        sa = copy.copy(args)
-        sa.study_res, sa.ref_spp, sa.plain_spp, sa.guide, sa.metric = "1280x720", 8192, 1024, "mlp", "robust"
-        sa.guide_fraction, sa.train_frames, sa.ref_cache, sa.save_images = 0.75, 64, None, None
-        print("[bench] equal-time relMSE study", file=sys.stderr, flush=True)
-        r = run_relmse_study(sa)
+        import tempfile
         equal_time = {
-            "study": "learned guide vs plain GPU path tracing, time to plain's 1024-spp relMSE",
-            "workload": r["workload"], "reference_spp": sa.ref_spp,
-            "metric": "relMSE (x-r)^2/(r^2+0.01) without the 0.1 % largest pixel errors; plain relMSE beside",
-            "plain_ms": r["plain"]["ms"], "plain_relmse": r["plain"]["relmse"],
-            "plain_relmse_plain_metric": r["plain"]["relmse_other_metric"],
-            "guided_train_ms": r["guided"]["train_ms"], "guided_ms_to_plain_error": r["guided"]["ms_to_plain_error"],
-            "guided_relmse_at_plain_time": r["guided"]["relmse_at_plain_time"],
-            "time_ratio_guided_over_plain": r["time_ratio_guided_over_plain"],
-            "time_ratio_plain_metric": r["time_ratio_other_metric"],
+            "study": "QuadTree and learned guides vs plain GPU path tracing, time to plain's 1024-spp relMSE",
+            "reference_spp": 8192,
+            "metric": "relMSE (x-r)^2/(r^2+0.01) without the 0.1 % largest pixel errors; the plain relMSE beside",
+            "guides": {},
         }
+        with tempfile.TemporaryDirectory() as td:
+            for guide, recipe in (("quadtree", QT_RECIPE), ("mlp", MLP_RECIPE)):
+                sa = copy.copy(args)
+                sa.study_res, sa.ref_spp, sa.plain_spp, sa.guide, sa.metric = "1280x720", 8192, 1024, guide, "robust"
+                sa.ref_cache, sa.save_images = str(Path(td) / "reference.npy"), None  # one converged image for both
+                for k, v in recipe.items():
+                    setattr(sa, k, v)
+                print(f"[bench] equal-time relMSE study ({guide})", file=sys.stderr, flush=True)
+                r = run_relmse_study(sa)
+                equal_time["workload"] = r["workload"]
+                equal_time["plain_ms"] = r["plain"]["ms"]
+                equal_time["plain_relmse"] = r["plain"]["relmse"]
+                equal_time["plain_relmse_plain_metric"] = r["plain"]["relmse_other_metric"]
+                equal_time["guides"][guide] = {
+                    "recipe": recipe,
+                    "train_ms": r["guided"]["train_ms"], "ms_to_plain_error": r["guided"]["ms_to_plain_error"],
+                    "relmse_at_plain_time": r["guided"]["relmse_at_plain_time"],
+                    "time_ratio_guided_over_plain": r["time_ratio_guided_over_plain"],
+                    "time_ratio_plain_metric": r["time_ratio_other_metric"],
+                }
     # k_shadow (any hit): node and triangle fetches of the shadow rays over
     # its CUDA-event time; like k_extend it reads a tree that stays in L2.
     sh_bytes = (sh_visits_per_ray * 64 + sh_tris_per_ray * 48) * sh_rays
@@ -537,7 +568,8 @@ def run_relmse_study(args) -> dict:
         ctx.mlp_configure(lr=args.mlp_lr, decay=args.mlp_decay, batch=args.mlp_batch, steps=args.mlp_steps,
                           direct=not args.mlp_indirect)
         mode = abi.MODE_GUIDED_MLP
-        train_ms = render_ms(args.train_frames, mode, 13, guide_fraction=args.guide_fraction, train_guide=True,
+        train_ms = render_ms(args.train_frames, mode, 13 + args.study_seed, guide_fraction=args.guide_fraction,
+                             train_guide=True,
                              guide_depth=args.guide_depth)
         train_spp = args.train_frames
         extra = {"train_frames": args.train_frames, "lr": args.mlp_lr, "lr_decay": args.mlp_decay,
@@ -558,7 +590,8 @@ def run_relmse_study(args) -> dict:
         for it in range(args.train_iters):
             n = args.train_first << it
             m = abi.MODE_PLAIN if (it == 0 and args.guide == "quadtree") else mode
-            train_ms += render_ms(n, m, 11 + it, record_paths=n, guide_fraction=args.guide_fraction)
+            train_ms += render_ms(n, m, 11 + it + args.study_seed, record_paths=n,
+                                  guide_fraction=args.guide_fraction)
             builds.append(ctx.cache_stats().build_ms)
             train_ms += builds[-1]
             train_spp += n
@@ -567,11 +600,11 @@ def run_relmse_study(args) -> dict:
                  "guide_params": ctx.guide_params()}
     guided_ms = 0.0
     curve = []
-    reached_ms = reached_chunk_ms = None
+    reached_ms = reached_chunk_ms = reached_other_seen = None
     chunk = max(1, args.plain_spp // 32)
     total = train_spp
     while total < 4 * args.plain_spp:
-        guided_ms += render_ms(chunk, mode, 17 + total, guide_fraction=args.guide_fraction,
+        guided_ms += render_ms(chunk, mode, 17 + total + args.study_seed, guide_fraction=args.guide_fraction,
                                guide_depth=args.guide_depth)
         total += chunk
         img = image()
@@ -587,7 +620,9 @@ def run_relmse_study(args) -> dict:
                     f = (1.0 / plain_err - 1.0 / e0) / (1.0 / e1 - 1.0 / e0)
                     reached_ms = t0 + f * (t1 - t0)
             reached_chunk_ms = train_ms + guided_ms
-        if train_ms + guided_ms >= 2.0 * plain_ms and reached_ms is not None:
+        if reached_other_seen is None and curve[-1][3] <= other(plain_img, ref):
+            reached_other_seen = total
+        if train_ms + guided_ms >= 2.0 * plain_ms and reached_ms is not None and reached_other_seen is not None:
             break
         if train_ms + guided_ms >= 4.0 * plain_ms:
             break
@@ -1043,6 +1078,7 @@ def main() -> None:
     ap.add_argument("--ref-cache", default=None, help="npy file keeping the converged image between study runs")
     ap.add_argument("--save-images", default=None, help="directory for the study's final plain and guided images")
     ap.add_argument("--guide-depth", type=int, default=0, help="guide the first N bounces only (0: all)")
+    ap.add_argument("--study-seed", type=int, default=0, help="relMSE study: offset of the guided renders' seeds")
     ap.add_argument("--mlp-indirect", action="store_true", help="train the learned guide on indirect light only")
     ap.add_argument("--trav-rays", type=int, default=10_000_000)
     ap.add_argument("--fd-params", type=int, default=256)
