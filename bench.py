@@ -213,6 +213,36 @@ def prepare_mode(ctx, mode: int, depth: int) -> float:
     return 0.5
 
 
+def box_rate(flush, spp: int = 16, steps: int = 10, warmup: int = 3) -> dict:
+    """Plain path tracing of the closed box (36 triangles, 256x256, depth 8,
+    16 spp per step: the reference's CPU-runnable configuration), device
+    time per step with the L2 flushed before each."""
+    import torch
+
+    from pathguidingdissertation_gb300 import abi
+    from pathguidingdissertation_gb300.api import Context
+    desc, depth, wl = make_workload("cornell")
+    ctx = Context(0)
+    ctx.upload(desc)
+    ctx.bvh_build()
+    ctx.clear()
+    for _ in range(warmup):
+        ctx.render(spp, mode=abi.MODE_PLAIN, seed=3, max_depth=depth, timing=True)
+    rays = paths = 0
+    ms = 0.0
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ctx.render(spp, mode=abi.MODE_PLAIN, seed=3, max_depth=depth, timing=True)
+        st = ctx.render_stats()
+        rays += st.extension_rays + st.shadow_rays
+        paths += st.paths
+        ms += st.ms_total
+    ctx.close()
+    return {"workload": wl, "spp_per_step": spp, "steps": steps, "ms_per_step": ms / steps,
+            "mrays_per_s": rays / (ms * 1e-3) / 1e6, "mpaths_per_s": paths / (ms * 1e-3) / 1e6}
+
+
 def side_mode_rate(ctx, mode: int, depth: int, spp: int, steps: int, seed: int, flush, ranks) -> dict:
     """Mrays/s and Mpaths/s of one more estimator on the bench's workload."""
     import torch
@@ -451,6 +481,27 @@ def run_pgx(args) -> dict:
         "note": "algorithmic node (64 B) and triangle (48 B) bytes per second against the HBM copy rate; the tree "
                 "is L2-resident as for k_extend",
     }
+    # The other configurations, each a bounded run outside the timed steps so
+    # that the line records them too: the plain box (16 spp, 256x256, depth
+    # 8), incoherent secondary rays on the 2M-triangle interior (10^7 rays),
+    # and the adjoint on the 2M-triangle terrain (with a few finite
+    # differences).  Rank 0 of a single-GPU run only.
+    workloads = None
+    if not args.no_workloads and ranks.world == 1 and args.workload == "interior" and not args.res:
+        import copy
+        print("[bench] other workloads", file=sys.stderr, flush=True)
+        workloads = {"plain_box": box_rate(flush)}
+        sa = copy.copy(args)
+        sa.trav_rays, sa.steps, sa.warmup, sa.no_cpu_baseline = 10_000_000, 5, 2, True
+        t = run_traversal_study(sa)
+        workloads["traversal_2m"] = {k: t[k] for k in ("scene", "rays", "ms", "mrays_per_s", "interior_nodes_per_ray",
+                                                       "triangles_per_ray", "alg_gbs", "hbm_frac")}
+        sa = copy.copy(args)
+        sa.fd_params, sa.diff_grid, sa.diff_res, sa.diff_spp = 24, 1024, 512, 64
+        a = run_adjoint_study(sa)
+        workloads["adjoint_terrain"] = {k: a[k] for k in (
+            "workload", "spp", "primal_mpaths_per_s", "adjoint_mpaths_per_s", "gradient_entries", "fd_params",
+            "rel_err_median", "frac_significant_within_1e-3_rel", "n_significant")}
     print("[bench] device runs done; CPU baseline next", file=sys.stderr, flush=True)
     cpu = cpu_baseline_reference(desc) if not args.no_cpu_baseline and ranks.world == 1 else None
     print("[bench] CPU baseline done", file=sys.stderr, flush=True)
@@ -480,6 +531,7 @@ def run_pgx(args) -> dict:
                 "d2h_bytes_per_step": H * W * 3 * 4},
         "modes": side,
         "equal_time": equal_time,
+        "workloads": workloads,
         "roofline": roofline,
         "roofline_shade": roofline_shade,
         "roofline_shadow": roofline_shadow,
@@ -1051,6 +1103,8 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-side-modes", action="store_true", help="skip the guided and depth-8 side measurements")
     ap.add_argument("--no-equal-time", action="store_true", help="skip the reduced equal-time relMSE study")
+    ap.add_argument("--no-workloads", action="store_true",
+                    help="skip the box, 2M-triangle traversal and adjoint measurements of the default line")
     ap.add_argument("--res", default=None, help="WxH: render the workload at this image size (profiler captures)")
     ap.add_argument("--spp-per-step", type=int, default=32,
                     help="samples per pixel of one step: one pgx_render call, one wavefront")
