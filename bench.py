@@ -502,6 +502,14 @@ def run_pgx(args) -> dict:
         workloads["adjoint_terrain"] = {k: a[k] for k in (
             "workload", "spp", "primal_mpaths_per_s", "adjoint_mpaths_per_s", "gradient_entries", "fd_params",
             "rel_err_median", "frac_significant_within_1e-3_rel", "n_significant")}
+        sa = copy.copy(args)
+        sa.batch_scenes, sa.batch_res, sa.batch_max_tris, sa.batch_relmse = 64, 0, 2e6, False
+        t0 = time.perf_counter()
+        bt = run_batch_study(sa)
+        workloads["batch_64_scenes"] = dict(
+            {k: bt[k] for k in ("scenes", "spp", "max_depth", "paths", "triangles_total", "tuning", "batch_mpaths_per_s",
+                                "graph_replay_mpaths_per_s", "sequential_mpaths_per_s")},
+            wall_s=time.perf_counter() - t0)
     print("[bench] device runs done; CPU baseline next", file=sys.stderr, flush=True)
     cpu = cpu_baseline_reference(desc) if not args.no_cpu_baseline and ranks.world == 1 else None
     print("[bench] CPU baseline done", file=sys.stderr, flush=True)
@@ -912,7 +920,7 @@ def run_batch_study(args) -> dict:
         ref = None
     for i, (sp, d, c) in enumerate(zip(specs, descs, ctxs)):
         row = dict(tris=int(d.ntris), res=sp["width"])
-        if sp["width"] <= 256 and d.ntris <= 300_000:
+        if getattr(args, "batch_relmse", True) and sp["width"] <= 256 and d.ntris <= 300_000:
             c.clear()
             c.render(1024, mode=abi.MODE_PLAIN, seed=77, max_depth=depth)
             conv = c.film()[0].astype(np.float64) / 1024
