@@ -628,11 +628,24 @@ def run_relmse_study(args) -> dict:
         ctx.mlp_configure(lr=args.mlp_lr, decay=args.mlp_decay, batch=args.mlp_batch, steps=args.mlp_steps,
                           direct=not args.mlp_indirect)
         mode = abi.MODE_GUIDED_MLP
-        train_ms = render_ms(args.train_frames, mode, 13 + args.study_seed, guide_fraction=args.guide_fraction,
-                             train_guide=True,
-                             guide_depth=args.guide_depth)
-        train_spp = args.train_frames
-        extra = {"train_frames": args.train_frames, "lr": args.mlp_lr, "lr_decay": args.mlp_decay,
+        if args.mlp_cache_frames > 0:
+            # QuadTree fallback: a radiance cache from unguided frames (kept in
+            # the image) guides the regions the network has not learned yet.
+            ctx.guide_configure(region_records=args.qt_region, refine_fraction=args.qt_refine,
+                                clamp_median=args.qt_clamp, uniform_share=args.qt_uniform,
+                                compensate=args.qt_compensate)
+            train_ms += render_ms(args.mlp_cache_frames, abi.MODE_PLAIN, 9 + args.study_seed,
+                                  record_paths=args.mlp_cache_frames)
+            train_ms += ctx.cache_stats().build_ms
+            train_spp += args.mlp_cache_frames
+            ctx.mlp_set_fallback(args.mlp_fallback)
+        train_ms += render_ms(args.train_frames, mode, 13 + args.study_seed, guide_fraction=args.guide_fraction,
+                              train_guide=True,
+                              guide_depth=args.guide_depth)
+        train_spp += args.train_frames
+        extra = {"train_frames": args.train_frames, "cache_frames": args.mlp_cache_frames,
+                 "fallback_min_samples": args.mlp_fallback if args.mlp_cache_frames > 0 else None,
+                 "lr": args.mlp_lr, "lr_decay": args.mlp_decay,
                  "adam_steps_per_frame": args.mlp_steps, "batch": args.mlp_batch, "guide_depth": args.guide_depth,
                  "target": "indirect" if args.mlp_indirect else "full incident radiance"}
     else:
@@ -1137,6 +1150,10 @@ def main() -> None:
     ap.add_argument("--mlp-decay", type=float, default=0.998)
     ap.add_argument("--mlp-steps", type=int, default=4)
     ap.add_argument("--mlp-batch", type=int, default=1 << 18, help="learned guide: radiance samples per Adam step")
+    ap.add_argument("--mlp-cache-frames", type=int, default=0,
+                    help="learned guide: unguided frames recorded into a QuadTree cache before training (its fallback)")
+    ap.add_argument("--mlp-fallback", type=int, default=256,
+                    help="learned guide: regions with fewer training samples than this use the QuadTree")
     ap.add_argument("--ref-cache", default=None, help="npy file keeping the converged image between study runs")
     ap.add_argument("--save-images", default=None, help="directory for the study's final plain and guided images")
     ap.add_argument("--guide-depth", type=int, default=0, help="guide the first N bounces only (0: all)")

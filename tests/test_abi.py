@@ -54,6 +54,9 @@ def test_version_and_null_ctx(pgx_lib):
     assert pgx_lib.pgx_version().startswith(b"pgx")
     assert pgx_lib.pgx_destroy(None) == 0
     assert pgx_lib.pgx_bvh_build(None) == 1  # PGX_ERR_INVALID_ARG
+    assert pgx_lib.pgx_guide_configure(None, None) == 1
+    assert pgx_lib.pgx_guide_get_params(None, None) == 1
+    assert pgx_lib.pgx_cache_export_weights(None, None, None) == 1
 
 
 def test_create_without_gpu_fails_cleanly(pgx_lib):
