@@ -107,6 +107,11 @@ struct DevEnv {
     const float* marg_cdf;     // H+1
     float marg_int;            // pMarginal->functionIntegral
     float power;               // totalIntegratedPower (Lights.h:200-210)
+    // Guide tables of the CDFs (nullptr: plain binary search): for bucket k
+    // of cdf_bucket(), the first CDF index in that bucket; H x (W + 1) and
+    // H + 1 entries.
+    const int* cond_guide;
+    const int* marg_guide;
 };
 
 struct SceneBoundsDev {
@@ -142,6 +147,7 @@ struct pgx_ctx {
 
     // environment map
     DevBuf env_texels, env_cond_func, env_cond_cdf, env_cond_int, env_marg_func, env_marg_cdf;
+    DevBuf env_cond_guide, env_marg_guide;
     DevEnv env{};
 
     // ---- BVH ----

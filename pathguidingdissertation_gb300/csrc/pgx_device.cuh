@@ -23,6 +23,14 @@ __device__ __forceinline__ float x_sub(float a, float b) { return __fsub_rn(a, b
 __device__ __forceinline__ float x_mul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float x_div(float a, float b) { return __fdiv_rn(a, b); }
 // std::min(a, b) / std::max(a, b): which operand wins decides NaN behaviour.
+// Bucket of a value in [0, 1] among K equal buckets, for the guide tables of
+// the environment's CDFs: built and read with this one function, so it only
+// needs to be monotone (a rounded product, truncated and clamped, is).
+__device__ __forceinline__ int cdf_bucket(float x, int K) {
+    const int k = (int)x_mul(x, (float)K);
+    return k < 0 ? 0 : (k > K - 1 ? K - 1 : k);
+}
+
 __host__ __device__ __forceinline__ float s_min(float a, float b) { return (b < a) ? b : a; }
 __host__ __device__ __forceinline__ float s_max(float a, float b) { return (a < b) ? b : a; }
 

@@ -715,10 +715,36 @@ __device__ __forceinline__ int cdf_search(const float* cdf, int size, float u) {
     r = (size - 2 < r) ? size - 2 : r;
     return r > 0 ? r : 0;
 }
-// Distribution1D::sampleContinuous (Sampling.h:151-163); n = function size.
+// cdf_search with a guide table (the cutpoint method, Chen and Asau 1974):
+// guide[k] is the first index i with cdf_bucket(cdf[i]) >= k, guide[K] =
+// size.  For a sorted CDF every entry before guide[k] is <= u and every
+// entry from guide[k + 1] on is > u when u falls in bucket k, so the count
+// of entries <= u -- what the binary search computes -- is found by the same
+// search over [guide[k], guide[k + 1]), usually zero to two steps instead of
+// log2(size).  The tables exist only for sorted CDFs.
+__device__ __forceinline__ int cdf_search_guided(const float* cdf, int size, float u, const int* guide, int K) {
+    const int k = cdf_bucket(u, K);
+    int first = guide[k];
+    int iter = guide[k + 1] - first;
+    while (iter > 0) {
+        int half = iter / 2;
+        int middle = first + half;
+        if (cdf[middle] <= u) {
+            first = middle + 1;
+            iter -= (half + 1);
+        } else {
+            iter = half;
+        }
+    }
+    int r = first - 1;
+    r = (size - 2 < r) ? size - 2 : r;
+    return r > 0 ? r : 0;
+}
+// Distribution1D::sampleContinuous (Sampling.h:151-163); n = function size;
+// guide: the CDF's guide table of n buckets, or nullptr.
 __device__ __forceinline__ float sample_continuous(const float* func, const float* cdf, float integral, int n, float u,
-                                                   float& pdf, int& off) {
-    off = cdf_search(cdf, n + 1, u);
+                                                   float& pdf, int& off, const int* guide = nullptr) {
+    off = guide ? cdf_search_guided(cdf, n + 1, u, guide, n) : cdf_search(cdf, n + 1, u);
     float du = u - cdf[off];
     if ((cdf[off + 1] - cdf[off]) > 0.f) du /= (cdf[off + 1] - cdf[off]);
     pdf = (integral > 0.f) ? (func[off] / integral) : 0.f;
@@ -760,9 +786,10 @@ __device__ __forceinline__ F3 env_sample_i(const DevEnv& e, uint64_t& rng, F3& c
     float rv = pgx_rng_next(rng);
     float pv, pu;
     int dv, du;
-    float v = sample_continuous(e.marg_func, e.marg_cdf, e.marg_int, e.height, rv, pv, dv);
+    float v = sample_continuous(e.marg_func, e.marg_cdf, e.marg_int, e.height, rv, pv, dv, e.marg_guide);
     float u = sample_continuous(e.cond_func + (size_t)dv * e.width, e.cond_cdf + (size_t)dv * (e.width + 1),
-                                e.cond_int[dv], e.width, ru, pu, du);
+                                e.cond_int[dv], e.width, ru, pu, du,
+                                e.cond_guide ? e.cond_guide + (size_t)dv * (e.width + 1) : nullptr);
     float sp = pu * pv;
     float theta = PGX_PI_F * v;
     float phi = PGX_2PI_F * u;

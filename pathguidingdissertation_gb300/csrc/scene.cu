@@ -201,6 +201,35 @@ __global__ void k_env_marginal(const float* __restrict__ integ, int H, float* __
     }
 }
 
+// Guide table of one CDF (`size` entries, K buckets of cdf_bucket):
+// g[k] = the first index whose bucket is >= k, g[K] = size.  *unsorted is
+// set when the CDF decreases or holds a NaN (negative texels): the sampler
+// then keeps the full binary search.
+__device__ void build_cdf_guide(const float* __restrict__ cdf, int size, int K, int* __restrict__ g, int* unsorted) {
+    int last = -1;
+    float prev = -FLT_MAX;
+    for (int i = 0; i < size; i++) {
+        const float c = cdf[i];
+        if (!(c >= prev)) *unsorted = 1;
+        prev = c;
+        const int b = cdf_bucket(c, K);
+        for (int k = last + 1; k <= b; k++) g[k] = i;
+        last = b > last ? b : last;
+    }
+    for (int k = last + 1; k <= K; k++) g[k] = size;
+}
+
+__global__ void k_env_row_guides(const float* __restrict__ cdf, int W, int H, int* __restrict__ guide, int* unsorted) {
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= H) return;
+    build_cdf_guide(cdf + (size_t)v * (W + 1), W + 1, W, guide + (size_t)v * (W + 1), unsorted);
+}
+
+__global__ void k_env_marginal_guide(const float* __restrict__ cdf, int H, int* __restrict__ guide, int* unsorted) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    build_cdf_guide(cdf, H + 1, H, guide, unsorted);
+}
+
 inline unsigned blocks_for(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
 }  // namespace
@@ -346,9 +375,21 @@ extern "C" int pgx_scene_upload(pgx_ctx* ctx, const pgx_triangle* tris, int64_t 
         float* total_dev = ctx->env_marg_cdf.as<float>() + (H + 1);
         k_env_marginal<<<1, 32, 0, s>>>(ctx->env_cond_int.as<float>(), H, ctx->env_marg_func.as<float>(),
                                         ctx->env_marg_cdf.as<float>(), total_dev);
+        // Guide tables of the row and marginal CDFs (sampling only; the
+        // indices they give are the binary search's).
+        PGX_CUDA_TRY(ctx, ctx->env_cond_guide.reserve(sizeof(int) * (size_t)H * (W + 1)));
+        PGX_CUDA_TRY(ctx, ctx->env_marg_guide.reserve(sizeof(int) * (H + 2)));
+        int* unsorted_dev = ctx->env_marg_guide.as<int>() + (H + 1);
+        PGX_CUDA_TRY(ctx, cudaMemsetAsync(unsorted_dev, 0, sizeof(int), s));
+        k_env_row_guides<<<blocks_for(H, 64), 64, 0, s>>>(ctx->env_cond_cdf.as<float>(), W, H,
+                                                          ctx->env_cond_guide.as<int>(), unsorted_dev);
+        k_env_marginal_guide<<<1, 32, 0, s>>>(ctx->env_marg_cdf.as<float>(), H, ctx->env_marg_guide.as<int>(),
+                                              unsorted_dev);
         PGX_CUDA_TRY(ctx, cudaGetLastError());
         float marg_int = 0.f;
+        int unsorted = 0;
         PGX_CUDA_TRY(ctx, cudaMemcpyAsync(&marg_int, total_dev, sizeof(float), cudaMemcpyDeviceToHost, s));
+        PGX_CUDA_TRY(ctx, cudaMemcpyAsync(&unsorted, unsorted_dev, sizeof(int), cudaMemcpyDeviceToHost, s));
         PGX_CUDA_TRY(ctx, cudaStreamSynchronize(s));
         // EnvironmentMap::totalIntegratedPower, Lights.h:200-210 (sequential sum).
         float total = 0.f;
@@ -373,6 +414,8 @@ extern "C" int pgx_scene_upload(pgx_ctx* ctx, const pgx_triangle* tris, int64_t 
         e.marg_cdf = ctx->env_marg_cdf.as<float>();
         e.marg_int = marg_int;
         e.power = total;
+        e.cond_guide = unsorted ? nullptr : ctx->env_cond_guide.as<int>();
+        e.marg_guide = unsorted ? nullptr : ctx->env_marg_guide.as<int>();
     }
 
     // Light list: the environment first when it has power (Scene::init,
