@@ -182,9 +182,10 @@ def cpu_baseline_reference(desc, frames_budget_s: float = 12.0) -> dict | None:
 # Training recipes of the guides on the 1280x720 interior (measured with
 # --study relmse): the QuadTree guide from an unguided pass of 8 frames and a
 # guided pass of 16 (each rebuilding the cache), 16,384-record regions,
-# guide fraction 0.7; the learned guide trained online on 64 frames.
+# guide fraction 0.7, GGX conductors (alpha <= 1.62 for roughness <= 1) left
+# to their BSDF; the learned guide trained online on 64 frames.
 QT_RECIPE = dict(train_first=8, train_iters=2, qt_region=16384, qt_refine=0.01, qt_clamp=10.0, qt_uniform=0.2,
-                 qt_compensate=0.0, guide_fraction=0.7)
+                 qt_compensate=0.0, qt_glossy_alpha=2.0, guide_fraction=0.7)
 MLP_RECIPE = dict(guide_fraction=0.75, train_frames=64)
 
 
@@ -198,7 +199,7 @@ def prepare_mode(ctx, mode: int, depth: int) -> float:
         r = QT_RECIPE
         ctx.guide_configure(region_records=r["qt_region"], refine_fraction=r["qt_refine"],
                             clamp_median=r["qt_clamp"], uniform_share=r["qt_uniform"],
-                            compensate=r["qt_compensate"])
+                            compensate=r["qt_compensate"], glossy_alpha=r["qt_glossy_alpha"])
         for it in range(r["train_iters"]):
             n = r["train_first"] << it
             ctx.render(n, mode=abi.MODE_PLAIN if it == 0 else mode, seed=99 + it, max_depth=depth,
@@ -633,7 +634,7 @@ def run_relmse_study(args) -> dict:
             # the image) guides the regions the network has not learned yet.
             ctx.guide_configure(region_records=args.qt_region, refine_fraction=args.qt_refine,
                                 clamp_median=args.qt_clamp, uniform_share=args.qt_uniform,
-                                compensate=args.qt_compensate)
+                                compensate=args.qt_compensate, glossy_alpha=args.qt_glossy_alpha)
             train_ms += render_ms(args.mlp_cache_frames, abi.MODE_PLAIN, 9 + args.study_seed,
                                   record_paths=args.mlp_cache_frames)
             train_ms += ctx.cache_stats().build_ms
@@ -658,7 +659,7 @@ def run_relmse_study(args) -> dict:
         mode = abi.MODE_GUIDED_PSS if args.guide == "pss" else abi.MODE_GUIDED_QUADTREE
         ctx.guide_configure(region_records=args.qt_region, refine_fraction=args.qt_refine,
                             clamp_median=args.qt_clamp, uniform_share=args.qt_uniform,
-                            compensate=args.qt_compensate)
+                            compensate=args.qt_compensate, glossy_alpha=args.qt_glossy_alpha)
         builds = []
         for it in range(args.train_iters):
             n = args.train_first << it
@@ -1143,6 +1144,8 @@ def main() -> None:
     ap.add_argument("--qt-clamp", type=float, default=10.0, help="QuadTree guide: flux clamp x median (0: none)")
     ap.add_argument("--qt-uniform", type=float, default=0.2, help="QuadTree guide: uniform share of its samples")
     ap.add_argument("--qt-compensate", type=float, default=0.0, help="QuadTree guide: MIS compensation (0: off)")
+    ap.add_argument("--qt-glossy-alpha", type=float, default=0.0,
+                    help="QuadTree guide: conductors with a smaller GGX alpha are not guided")
     ap.add_argument("--guide", choices=["mlp", "quadtree", "pss"], default="mlp")
     ap.add_argument("--metric", choices=["robust", "plain"], default="robust")
     ap.add_argument("--train-frames", type=int, default=64)

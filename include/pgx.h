@@ -433,14 +433,20 @@ int pgx_guide_sample(pgx_ctx* ctx, const float* positions, const float* u2, int6
  *                   area, floored at 0, so the guide concentrates on what
  *                   the BSDF samples poorly; regions left with under 5 % of
  *                   their flux keep the plain tree; 0: off [0, 4] [0]
+ *   glossy_alpha    conductor vertices whose GGX alpha is below this sample
+ *                   their BSDF alone in PGX_MODE_GUIDED_QUADTREE (the tree
+ *                   holds Li |cos|, not the product with a narrow lobe);
+ *                   0: every non-specular surface is guided [>= 0] [0]
  * region_records, refine_fraction, clamp_median and compensate shape the next
- * cache build; uniform_share applies to every later render and guide query. */
+ * cache build; uniform_share and glossy_alpha apply to every later render
+ * (uniform_share also to guide queries). */
 typedef struct pgx_guide_params {
     int32_t region_records;
     float refine_fraction;
     float clamp_median;
     float uniform_share;
     float compensate;
+    float glossy_alpha;
 } pgx_guide_params;
 /* params == NULL restores the defaults; out-of-range values are rejected
  * with PGX_ERR_INVALID_ARG and change nothing. */

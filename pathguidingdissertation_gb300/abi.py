@@ -109,7 +109,7 @@ class CacheStats(C.Structure):
 
 class GuideParams(C.Structure):
     _fields_ = [("region_records", C.c_int32), ("refine_fraction", C.c_float), ("clamp_median", C.c_float),
-                ("uniform_share", C.c_float), ("compensate", C.c_float)]
+                ("uniform_share", C.c_float), ("compensate", C.c_float), ("glossy_alpha", C.c_float)]
 
 
 class BatchTuning(C.Structure):

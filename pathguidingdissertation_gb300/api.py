@@ -252,12 +252,13 @@ class Context:
         return regions, qnodes, bool(pss.value)
 
     def guide_configure(self, region_records: int = 1024, refine_fraction: float = 0.01,
-                        clamp_median: float = 10.0, uniform_share: float = 0.2, compensate: float = 0.0) -> None:
+                        clamp_median: float = 10.0, uniform_share: float = 0.2, compensate: float = 0.0,
+                        glossy_alpha: float = 0.0) -> None:
         """QuadTree guide parameters (pgx_guide_configure): region size,
         refinement share, flux clamp and MIS compensation shape the next
-        cache build; the uniform share applies to later renders and
-        queries."""
-        gp = abi.GuideParams(region_records, refine_fraction, clamp_median, uniform_share, compensate)
+        cache build; the uniform share and the glossy threshold apply to
+        later renders (the share also to queries)."""
+        gp = abi.GuideParams(region_records, refine_fraction, clamp_median, uniform_share, compensate, glossy_alpha)
         self.check(self.lib.pgx_guide_configure(self.h, C.byref(gp)))
 
     def guide_params(self) -> dict:

@@ -793,6 +793,7 @@ GuideView guide_view(const pgx_ctx* ctx) {
     g.node_region = cs->node_region.as<int>();
     g.pss = cs->pss ? 1 : 0;
     g.uniform = ctx->guide.uniform_share;
+    g.min_alpha = ctx->guide.glossy_alpha;
     return g;
 }
 
@@ -1107,7 +1108,7 @@ extern "C" int pgx_guide_sample(pgx_ctx* ctx, const float* positions, const floa
 extern "C" int pgx_guide_configure(pgx_ctx* ctx, const pgx_guide_params* params) {
     if (!ctx) return PGX_ERR_INVALID_ARG;
     ctx->err.clear();
-    const pgx_guide_params defaults{1024, 0.01f, 10.f, 0.2f, 0.f};
+    const pgx_guide_params defaults{1024, 0.01f, 10.f, 0.2f, 0.f, 0.f};
     const pgx_guide_params p = params ? *params : defaults;
     if (p.region_records < 256 || p.region_records > (1 << 20))
         return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_guide_configure: region_records %d outside [256, 2^20]",
@@ -1120,6 +1121,8 @@ extern "C" int pgx_guide_configure(pgx_ctx* ctx, const pgx_guide_params* params)
         return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_guide_configure: uniform_share must be in [0, 1)");
     if (!(p.compensate >= 0.f && p.compensate <= 4.f))
         return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_guide_configure: compensate must be in [0, 4]");
+    if (!(p.glossy_alpha >= 0.f) || !std::isfinite(p.glossy_alpha))
+        return pgx_fail(ctx, PGX_ERR_INVALID_ARG, "pgx_guide_configure: glossy_alpha must be finite and >= 0");
     ctx->guide = p;
     return PGX_OK;
 }

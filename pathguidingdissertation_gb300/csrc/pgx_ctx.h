@@ -175,7 +175,7 @@ struct pgx_ctx {
     pgx_render_stats rstats{};
     void* render_state = nullptr;  // owned by render.cu
     void* cache_state = nullptr;   // owned by cache.cu
-    pgx_guide_params guide{1024, 0.01f, 10.f, 0.2f, 0.f};  // QuadTree guide parameters (pgx_guide_configure)
+    pgx_guide_params guide{1024, 0.01f, 10.f, 0.2f, 0.f, 0.f};  // QuadTree guide parameters (pgx_guide_configure)
     void* mlp_state = nullptr;     // owned by mlp.cu
 
     pgx_ctx() = default;

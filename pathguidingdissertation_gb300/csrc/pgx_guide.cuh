@@ -52,6 +52,7 @@ struct GuideView {
     const int* __restrict__ node_region;  // region index of region-root nodes, else -1
     int pss;  // 1: the quadtrees are over the diffuse BSDF's primary samples, 0: over directions
     float uniform;  // share of the guide's samples drawn uniformly (defensive)
+    float min_alpha;  // conductors with a smaller GGX alpha sample the BSDF alone
 };
 
 GuideView guide_view(const pgx_ctx* ctx);
@@ -229,6 +230,13 @@ __device__ __forceinline__ int guide_region_index(const GuideView& g, F3 x) {
 __device__ __forceinline__ int guide_region_root(const GuideView& g, F3 x) {
     const int r = guide_region_index(g, x);
     return r >= 0 ? g.region_qroot[r] : -1;
+}
+
+// Surfaces the direction-space QuadTree guides: every non-specular one
+// except conductors narrower than min_alpha.  K: the kind when known.
+template <int K = -1>
+__device__ __forceinline__ bool qt_guided_surface(const GuideView& g, const DevMaterial& m) {
+    return (K >= 0 ? K : m.kind) != PGX_BSDF_CONDUCTOR || m.alpha >= g.min_alpha;
 }
 
 // Solid-angle pdf of the guide (quadtree mixed with a uniform share).

@@ -790,7 +790,8 @@ __global__ void __launch_bounds__(kThreads, kShadeBlocksPerSM) k_shade(SceneView
                 } else {
                     int qroot = -1;
                     const bool spec = bsdf_pure_specular_k<KIND>(m);
-                    if (MODE == PGX_MODE_GUIDED_QUADTREE && depth < fp.guide_depth && !spec && !gv.pss)
+                    if (MODE == PGX_MODE_GUIDED_QUADTREE && depth < fp.guide_depth && !spec && !gv.pss &&
+                        qt_guided_surface<KIND>(gv, m))
                         qroot = guide_region_root(gv, sd.x);
                     if (MODE == PGX_MODE_GUIDED_PSS && depth < fp.guide_depth && gv.pss && pss_surface<KIND>(m))
                         qroot = guide_region_root(gv, sd.x);

@@ -198,14 +198,19 @@ def test_plain_recording_records(ctx):
     assert ctx.render_stats().path_vertices > 2 * n1
 
 
-@pytest.mark.parametrize("training", ["guided_li", "plain"])
+@pytest.mark.parametrize("training", ["guided_li", "plain", "plain_recipe"])
 @pytest.mark.parametrize("scene", ["cornell", "interior"])
 def test_guided_estimator_unbiased(ctx, scene, training):
+    """plain_recipe: the cache of the measured recipe (16,384-record
+    regions, conductors narrower than alpha 0.7 left to their BSDF)."""
     if scene == "cornell":
         desc = scenes.cornell_box(seed=1, width=48, height=48)
     else:
         desc = scenes.interior(seed=3, target_tris=20000, n_objects=40, width=48, height=27, env_width=256,
                                env_height=128)
+    if training == "plain_recipe":
+        ctx.guide_configure(region_records=16384, glossy_alpha=0.7)
+        training = "plain"
     _guided_scene(ctx, desc, training=training)
     spp = 1024
     ctx.render(spp, mode=abi.MODE_PLAIN, seed=5, max_depth=8)

@@ -186,7 +186,7 @@ def test_guide_params_match_oracle(ctx, params):
     for k, v in params.items():
         assert got[k] == pytest.approx(v)
     for bad in (dict(region_records=255), dict(refine_fraction=0.0), dict(clamp_median=-1.0),
-                dict(uniform_share=1.0), dict(compensate=-0.5)):
+                dict(uniform_share=1.0), dict(compensate=-0.5), dict(glossy_alpha=-1.0)):
         with pytest.raises(RuntimeError):
             ctx.guide_configure(**dict(params, **bad))
     assert ctx.guide_params() == got
