@@ -1135,16 +1135,18 @@ def main() -> None:
     ap.add_argument("--study-res", default="640x360")
     ap.add_argument("--ref-spp", type=int, default=16384)
     ap.add_argument("--plain-spp", type=int, default=1024)
-    ap.add_argument("--train-iters", type=int, default=6)
-    ap.add_argument("--train-first", type=int, default=1,
+    ap.add_argument("--train-iters", type=int, default=QT_RECIPE["train_iters"])
+    ap.add_argument("--train-first", type=int, default=QT_RECIPE["train_first"],
                     help="QuadTree/PSS study: frames of the first (unguided) cache pass; iteration k renders 2^k x as many")
-    ap.add_argument("--guide-fraction", type=float, default=0.5)
-    ap.add_argument("--qt-region", type=int, default=1024, help="QuadTree guide: records per region")
+    ap.add_argument("--guide-fraction", type=float, default=None,
+                    help="probability of sampling the guide (default: the guide's recipe, 0.7 QuadTree / PSS, "
+                         "0.75 learned)")
+    ap.add_argument("--qt-region", type=int, default=QT_RECIPE["qt_region"], help="QuadTree guide: records per region")
     ap.add_argument("--qt-refine", type=float, default=0.01, help="QuadTree guide: flux share that splits a cell")
     ap.add_argument("--qt-clamp", type=float, default=10.0, help="QuadTree guide: flux clamp x median (0: none)")
     ap.add_argument("--qt-uniform", type=float, default=0.2, help="QuadTree guide: uniform share of its samples")
     ap.add_argument("--qt-compensate", type=float, default=0.0, help="QuadTree guide: MIS compensation (0: off)")
-    ap.add_argument("--qt-glossy-alpha", type=float, default=0.0,
+    ap.add_argument("--qt-glossy-alpha", type=float, default=QT_RECIPE["qt_glossy_alpha"],
                     help="QuadTree guide: conductors with a smaller GGX alpha are not guided")
     ap.add_argument("--guide", choices=["mlp", "quadtree", "pss"], default="mlp")
     ap.add_argument("--metric", choices=["robust", "plain"], default="robust")
@@ -1171,6 +1173,8 @@ def main() -> None:
     ap.add_argument("--batch-res", type=int, default=0, help="0: resolutions drawn from {128,256,512,1024}")
     ap.add_argument("--batch-max-tris", type=float, default=2e6)
     args = ap.parse_args()
+    if args.guide_fraction is None:
+        args.guide_fraction = MLP_RECIPE["guide_fraction"] if args.guide == "mlp" else QT_RECIPE["guide_fraction"]
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.gpus != world:
