@@ -208,6 +208,40 @@ class RayTracer {
     }
     pgx_render_config& config() { return cfg_; }
 
+    // Guided rendering (extension): trains the radiance-cache guide that
+    // PGX_MODE_GUIDED_QUADTREE (or PGX_MODE_GUIDED_PSS) samples.  Pass k
+    // renders first x 2^k frames and records their path vertices, which
+    // rebuild the cache; the first pass is unguided (plain, or the PSS mode
+    // without a cache), the others use the previous pass's guide.  Records
+    // are weighted by Lum(Li) |cos| / pdf, so no pass inherits the guide that
+    // sampled it, and the frames stay in the film (they are unbiased
+    // samples).  params: as pgx_guide_configure (nullptr keeps the
+    // context's).  render() then continues in this tracer's mode.
+    void trainGuide(int first = 8, int passes = 2, const pgx_guide_params* params = nullptr) {
+        if (params) check(ctx(), pgx_guide_configure(ctx(), params));
+        const bool pss = cfg_.mode == PGX_MODE_GUIDED_PSS;
+        pgx_render_config c = cfg_;
+        for (int k = 0; k < passes; k++) {
+            const int n = first << k;
+            c.mode = pss ? PGX_MODE_GUIDED_PSS : (k == 0 ? PGX_MODE_PLAIN : PGX_MODE_GUIDED_QUADTREE);
+            c.record_paths = n;
+            check(ctx(), pgx_render(ctx(), &c, n));
+        }
+    }
+    // The guide parameters measured best on the 1280x720 procedural interior
+    // (with guide_fraction 0.7 and trainGuide(8, 2)): 16,384-record regions,
+    // GGX conductors left to their BSDF, the rest at their defaults.
+    static pgx_guide_params recommendedGuideParams() {
+        pgx_guide_params p{};
+        p.region_records = 16384;
+        p.refine_fraction = 0.01f;
+        p.clamp_median = 10.f;
+        p.uniform_share = 0.2f;
+        p.compensate = 0.f;
+        p.glossy_alpha = 2.f;
+        return p;
+    }
+
   private:
     pgx_ctx* ctx() const {
         if (!scene_) throw Error(PGX_ERR_STATE, "RayTracer used before init()");

@@ -3,6 +3,7 @@
 // scene is a closed-top box with a ceiling light, built in code.
 #include <cmath>
 #include <cstdio>
+#include <string>
 #include <vector>
 
 #include "pgx.hpp"
@@ -32,8 +33,15 @@ static void quad(std::vector<pgx_triangle>& out, const float o[3], const float u
     }
 }
 
+static double image_mean(const std::vector<float>& img) {
+    double m = 0;
+    for (float v : img) m += v;
+    return m / (double)img.size();
+}
+
 int main(int argc, char** argv) {
     const char* out = argc > 1 ? argv[1] : "box.hdr";
+    const bool guided = argc > 2 && std::string(argv[2]) == "guided";
     std::vector<pgx_material> mats(2);
     for (auto& m : mats) {
         m = pgx_material{};
@@ -69,6 +77,21 @@ int main(int argc, char** argv) {
         pgx::Scene scene(0);
         scene.init(tris, mats, nullptr, cam);
         scene.build();
+        if (guided) {
+            // Plain and QuadTree-guided images of the same box at 256 spp.
+            pgx::RayTracer plain(PGX_MODE_PLAIN, 8, 11);
+            plain.init(&scene);
+            plain.render(256);
+            const double mp = image_mean(plain.image());
+            pgx::RayTracer g(PGX_MODE_GUIDED_QUADTREE, 8, 12);
+            g.config().guide_fraction = 0.7f;
+            g.init(&scene);
+            const pgx_guide_params gp = pgx::RayTracer::recommendedGuideParams();
+            g.trainGuide(4, 2, &gp);  // 4 unguided + 8 guided frames, kept in the film
+            g.render(256 - g.getSPP());
+            std::printf("guided spp=%d mean_guided=%.6f mean_plain=%.6f\n", g.getSPP(), image_mean(g.image()), mp);
+            return 0;
+        }
         pgx::RayTracer tracer(PGX_MODE_PLAIN, 8, 1);
         tracer.init(&scene);
         while (tracer.getSPP() < 8) tracer.render();

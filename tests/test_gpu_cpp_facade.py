@@ -35,6 +35,20 @@ def test_cpp_facade_renders(tmp_path, pgx_lib):
 
 
 @pytest.mark.gpu
+def test_cpp_facade_trains_the_quadtree_guide(tmp_path, pgx_lib):
+    """RayTracer::trainGuide with the recommended parameters, then guided
+    frames: the guided image's mean agrees with plain path tracing's within
+    2 % at 256 spp (both unbiased; the means' standard errors are ~0.2 %)."""
+    exe = _build_example(tmp_path, pgx_lib)
+    r = subprocess.run([str(exe), str(tmp_path / "g.hdr"), "guided"], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    f = dict(kv.split("=") for kv in r.stdout.split() if "=" in kv)
+    assert int(f["spp"]) == 256
+    mg, mp = float(f["mean_guided"]), float(f["mean_plain"])
+    assert mp > 0.01 and abs(mg - mp) < 0.02 * mp, (mg, mp)
+
+
+@pytest.mark.gpu
 def test_cpp_load_scene_renders_reference_scene(tmp_path, pgx_lib):
     """pgx::loadScene on the reference's cornell-box directory (the C++
     host path of SceneLoader.h:222-269), rendered by pgx::RayTracer; the
