@@ -182,9 +182,10 @@ def cpu_baseline_reference(desc, frames_budget_s: float = 12.0) -> dict | None:
 # Training recipes of the guides on the 1280x720 interior (measured with
 # --study relmse): the QuadTree guide from an unguided pass of 8 frames and a
 # guided pass of 16 (each rebuilding the cache), 16,384-record regions,
-# guide fraction 0.7, GGX conductors (alpha <= 1.62 for roughness <= 1) left
-# to their BSDF; the learned guide trained online on 64 frames.
-QT_RECIPE = dict(train_first=8, train_iters=2, qt_region=16384, qt_refine=0.01, qt_clamp=10.0, qt_uniform=0.2,
+# guide fraction 0.7, flux clamped at 20x the region's median, GGX conductors
+# (alpha <= 1.62 for roughness <= 1) left to their BSDF; the learned guide
+# trained online on 64 frames.
+QT_RECIPE = dict(train_first=8, train_iters=2, qt_region=16384, qt_refine=0.01, qt_clamp=20.0, qt_uniform=0.2,
                  qt_compensate=0.0, qt_glossy_alpha=2.0, guide_fraction=0.7)
 MLP_RECIPE = dict(guide_fraction=0.75, train_frames=64)
 
@@ -1143,7 +1144,8 @@ def main() -> None:
                          "0.75 learned)")
     ap.add_argument("--qt-region", type=int, default=QT_RECIPE["qt_region"], help="QuadTree guide: records per region")
     ap.add_argument("--qt-refine", type=float, default=0.01, help="QuadTree guide: flux share that splits a cell")
-    ap.add_argument("--qt-clamp", type=float, default=10.0, help="QuadTree guide: flux clamp x median (0: none)")
+    ap.add_argument("--qt-clamp", type=float, default=QT_RECIPE["qt_clamp"],
+                    help="QuadTree guide: flux clamp x median (0: none)")
     ap.add_argument("--qt-uniform", type=float, default=0.2, help="QuadTree guide: uniform share of its samples")
     ap.add_argument("--qt-compensate", type=float, default=0.0, help="QuadTree guide: MIS compensation (0: off)")
     ap.add_argument("--qt-glossy-alpha", type=float, default=QT_RECIPE["qt_glossy_alpha"],

@@ -230,12 +230,13 @@ class RayTracer {
     }
     // The guide parameters measured best on the 1280x720 procedural interior
     // (with guide_fraction 0.7 and trainGuide(8, 2)): 16,384-record regions,
-    // GGX conductors left to their BSDF, the rest at their defaults.
+    // flux clamped at 20x the region's median, GGX conductors left to their
+    // BSDF, the rest at their defaults.
     static pgx_guide_params recommendedGuideParams() {
         pgx_guide_params p{};
         p.region_records = 16384;
         p.refine_fraction = 0.01f;
-        p.clamp_median = 10.f;
+        p.clamp_median = 20.f;
         p.uniform_share = 0.2f;
         p.compensate = 0.f;
         p.glossy_alpha = 2.f;
