@@ -3,21 +3,24 @@
 // point quadtree, QuadTree.h).
 //
 // Spatial side: the cache's point BVH is cut into regions — the subtrees
-// whose record count first drops to kRegionMax.  Directional side: each
-// region owns a quadtree over the cylindrical equal-area map of world
-// directions, (u, v) = ((cos(theta) + 1) / 2, (phi + pi) / 2pi) with theta
-// measured from +z (solid angle = 4*pi * area in (u, v)).  Cells are refined
-// while they hold more than 1 % of the region's flux, where a record's flux
-// is the luminance of its Li (Mueller et al. 2017, "Practical Path Guiding").
+// whose record count first drops to pgx_guide_params.region_records.
+// Directional side: each region owns a quadtree over the cylindrical
+// equal-area map of world directions, (u, v) = ((cos(theta) + 1) / 2,
+// (phi + pi) / 2pi) with theta measured from +z (solid angle = 4*pi * area
+// in (u, v)).  Cells are refined while they hold more than refine_fraction
+// (1 %) of the region's flux (Mueller et al. 2017, "Practical Path
+// Guiding").  A record's flux is its weight: Lum(Li) |cos| / pdf for the
+// records of plain and guided renders (an estimate of Li |cos| whichever
+// distribution sampled wi), Lum(Li) for host and guided-Li records; weights
+// are clamped at clamp_median x the region's median (10 by default).
 //
 // At a shading point the region is found by descending the point BVH; the
 // guide is the region's quadtree mixed with a uniform share (20 % by
-// default), records are weighted by their luminance, by default clamped at
-// 10x the region's median (pgx_guide_params in pgx.h), and the
-// continuation direction is drawn by one-sample MIS between the guide and
-// the BSDF (probability `guide_fraction` for the guide), and the combined
-// pdf is used both for the throughput and for the MIS weights of NEE and of
-// emitter hits, so the estimator stays unbiased.  Pure-specular BSDFs and
+// default), and the continuation direction is drawn by one-sample MIS
+// between the guide and the BSDF (probability `guide_fraction` for the
+// guide); the combined pdf is used both for the throughput and for the MIS
+// weights of NEE and of emitter hits, so the estimator stays unbiased.
+// Pure-specular BSDFs, glass, conductors narrower than glossy_alpha and
 // regions without flux sample the BSDF alone.
 #pragma once
 
