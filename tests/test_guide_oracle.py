@@ -152,3 +152,78 @@ def test_mis_compensation():
     u["wi"] = d / np.linalg.norm(d, axis=1, keepdims=True)
     u["Li"] = 1.0
     assert go.build_quadtree(u, compensate=1.0) == go.build_quadtree(u)
+
+
+def test_pdf_weighted_records_do_not_inherit_the_sampler():
+    """Records weighted by Lum(Li) |cos| / pdf (what the renderer attaches)
+    build the same tree whichever distribution sampled their directions:
+    from cosine-sampled directions and from directions drawn by a sharply
+    peaked guide, the trees' densities agree (both estimate Li |cos|), while
+    the unweighted deposits follow the sampler (the compounding that
+    iterated training suffered from)."""
+    rng = np.random.default_rng(11)
+    n = 200_000
+    light = np.array([0.3, 0.2, 0.93])
+    light /= np.linalg.norm(light)
+
+    def li_of(w):
+        # a bright lobe plus a dim sky, seen from a surface with normal +z
+        return 5.0 * np.exp(40.0 * (w @ light - 1.0)) + 0.2
+
+    def cosine(m):
+        r1, r2 = rng.random(m), rng.random(m)
+        s = np.sqrt(r1)
+        w = np.stack([s * np.cos(2 * np.pi * r2), s * np.sin(2 * np.pi * r2), np.sqrt(1 - r1)], 1)
+        return w, w[:, 2] / np.pi
+
+    def peaked(m):
+        # mixture: 70 % a narrow cone around (-0.6, 0, 0.8), 30 % cosine
+        axis = np.array([-0.6, 0.0, 0.8])
+        k = 30.0
+        pick = rng.random(m) < 0.7
+        wc, _ = cosine(m)
+        u = rng.random(m)
+        ct = 1.0 + np.log(u + (1 - u) * np.exp(-2 * k)) / k   # vMF about +z
+        st = np.sqrt(np.maximum(0, 1 - ct * ct))
+        ph = 2 * np.pi * rng.random(m)
+        loc = np.stack([st * np.cos(ph), st * np.sin(ph), ct], 1)
+        # rotate +z to axis
+        t = np.cross([0.0, 0.0, 1.0], axis)
+        ang = np.arccos(axis[2])
+        t /= np.linalg.norm(t)
+        K = np.array([[0, -t[2], t[1]], [t[2], 0, -t[0]], [-t[1], t[0], 0]])
+        R = np.eye(3) + np.sin(ang) * K + (1 - np.cos(ang)) * K @ K
+        wv = loc @ R.T
+        w = np.where(pick[:, None], wv, wc)
+        vmf = k / (2 * np.pi * (1 - np.exp(-2 * k))) * np.exp(k * (w @ axis - 1))
+        pdf = 0.7 * vmf + 0.3 * np.maximum(w[:, 2], 0) / np.pi
+        keep = w[:, 2] > 0
+        return w[keep], pdf[keep]
+
+    probe = rng.normal(size=(4000, 3))
+    probe[:, 2] = np.abs(probe[:, 2])
+    probe /= np.linalg.norm(probe, axis=1, keepdims=True)
+    pu, pv = go.dir_to_uv(probe.astype(np.float32))
+
+    def tree_density(w, weights):
+        r = np.zeros(len(w), PV)
+        r["wi"] = w
+        r["Li"] = 1.0
+        t = go.build_quadtree(r, clamp_median=0.0, weights=weights)
+        return np.array([go.quad_pdf(t, float(a), float(b)) for a, b in zip(pu, pv)])
+
+    w1, p1 = cosine(n)
+    w2, p2 = peaked(n)
+    d1 = tree_density(w1, (li_of(w1) * w1[:, 2] / p1).astype(np.float32))
+    d2 = tree_density(w2, (li_of(w2) * w2[:, 2] / p2).astype(np.float32))
+    # both approximate the same density, Li |cos| (up to the cells' averaging
+    # and the noise of 200k samples), where it is large
+    target = li_of(probe) * probe[:, 2]
+    mask = target > 0.5 * target.max()
+    assert mask.sum() > 20
+    assert np.median(np.abs(d1[mask] - d2[mask]) / d1[mask]) < 0.25
+    # unweighted deposits of the peaked sampler pile up around its axis
+    d3 = tree_density(w2, go.luminance(np.repeat(li_of(w2)[:, None], 3, 1)).astype(np.float32))
+    near = probe @ np.array([-0.6, 0.0, 0.8]) > 0.95
+    assert near.sum() > 20
+    assert d3[near].mean() > 3 * d1[near].mean()
