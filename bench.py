@@ -215,6 +215,22 @@ def prepare_mode(ctx, mode: int, depth: int) -> float:
     return 0.5
 
 
+def guarded(name: str, fn, *a) -> dict:
+    """Runs one of the default line's side measurements; a failure there is
+    recorded in the line ({"error": ...}) instead of ending the run, so the
+    headline measured before it is still printed."""
+    try:
+        return fn(*a)
+    except Exception as e:  # noqa: BLE001
+        print(f"[bench] {name} failed: {type(e).__name__}: {e}", file=sys.stderr, flush=True)
+        return {"error": f"{type(e).__name__}: {e}"}
+
+
+def pick(r: dict, keys) -> dict:
+    """The listed keys of a study's result (or its error)."""
+    return r if "error" in r else {k: r[k] for k in keys}
+
+
 def box_rate(flush, spp: int = 16, steps: int = 10, warmup: int = 3) -> dict:
     """Plain path tracing of the closed box (36 triangles, 256x256, depth 8,
     16 spp per step: the reference's CPU-runnable configuration), device
@@ -357,7 +373,10 @@ def run_pgx(args) -> dict:
                            ("guided_mlp", abi.MODE_GUIDED_MLP, depth), ("plain_depth8", abi.MODE_PLAIN, 8)):
             if m == mode and d == depth:
                 continue
-            side[name] = side_mode_rate(ctx, m, d, spp, max(1, min(args.steps, 4)), seed, flush, ranks)
+            side[name] = (side_mode_rate(ctx, m, d, spp, max(1, min(args.steps, 4)), seed, flush, ranks)
+                          if ranks.world > 1 else
+                          guarded(name, side_mode_rate, ctx, m, d, spp, max(1, min(args.steps, 4)), seed, flush,
+                                  ranks))
         ctx.clear()
 
     # End to end through the C ABI: camera from host, render, film to pinned host memory.
@@ -453,7 +472,10 @@ def run_pgx(args) -> dict:
                 for k, v in recipe.items():
                     setattr(sa, k, v)
                 print(f"[bench] equal-time relMSE study ({guide})", file=sys.stderr, flush=True)
-                r = run_relmse_study(sa)
+                r = guarded(f"equal-time study ({guide})", run_relmse_study, sa)
+                if "error" in r:
+                    equal_time["guides"][guide] = r
+                    continue
                 equal_time["workload"] = r["workload"]
                 equal_time["plain_ms"] = r["plain"]["ms"]
                 equal_time["plain_relmse"] = r["plain"]["relmse"]
@@ -492,26 +514,23 @@ def run_pgx(args) -> dict:
     if not args.no_workloads and ranks.world == 1 and args.workload == "interior" and not args.res:
         import copy
         print("[bench] other workloads", file=sys.stderr, flush=True)
-        workloads = {"plain_box": box_rate(flush)}
+        workloads = {"plain_box": guarded("box", box_rate, flush)}
         sa = copy.copy(args)
         sa.trav_rays, sa.steps, sa.warmup, sa.no_cpu_baseline = 10_000_000, 5, 2, True
-        t = run_traversal_study(sa)
-        workloads["traversal_2m"] = {k: t[k] for k in ("scene", "rays", "ms", "mrays_per_s", "interior_nodes_per_ray",
-                                                       "triangles_per_ray", "alg_gbs", "hbm_frac")}
+        workloads["traversal_2m"] = pick(guarded("traversal", run_traversal_study, sa), (
+            "scene", "rays", "ms", "mrays_per_s", "interior_nodes_per_ray", "triangles_per_ray", "alg_gbs",
+            "hbm_frac"))
         sa = copy.copy(args)
         sa.fd_params, sa.diff_grid, sa.diff_res, sa.diff_spp = 24, 1024, 512, 64
-        a = run_adjoint_study(sa)
-        workloads["adjoint_terrain"] = {k: a[k] for k in (
+        workloads["adjoint_terrain"] = pick(guarded("adjoint", run_adjoint_study, sa), (
             "workload", "spp", "primal_mpaths_per_s", "adjoint_mpaths_per_s", "gradient_entries", "fd_params",
-            "rel_err_median", "frac_significant_within_1e-3_rel", "n_significant")}
+            "rel_err_median", "frac_significant_within_1e-3_rel", "n_significant"))
         sa = copy.copy(args)
         sa.batch_scenes, sa.batch_res, sa.batch_max_tris, sa.batch_relmse = 64, 0, 2e6, False
         t0 = time.perf_counter()
-        bt = run_batch_study(sa)
-        workloads["batch_64_scenes"] = dict(
-            {k: bt[k] for k in ("scenes", "spp", "max_depth", "paths", "triangles_total", "tuning", "batch_mpaths_per_s",
-                                "graph_replay_mpaths_per_s", "sequential_mpaths_per_s")},
-            wall_s=time.perf_counter() - t0)
+        workloads["batch_64_scenes"] = dict(pick(guarded("batch", run_batch_study, sa), (
+            "scenes", "spp", "max_depth", "paths", "triangles_total", "tuning", "batch_mpaths_per_s",
+            "graph_replay_mpaths_per_s", "sequential_mpaths_per_s")), wall_s=time.perf_counter() - t0)
     print("[bench] device runs done; CPU baseline next", file=sys.stderr, flush=True)
     cpu = cpu_baseline_reference(desc) if not args.no_cpu_baseline and ranks.world == 1 else None
     print("[bench] CPU baseline done", file=sys.stderr, flush=True)

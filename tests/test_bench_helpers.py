@@ -49,3 +49,18 @@ def test_relmse_metrics():
 def test_measured_peaks_read():
     p = bench.measured_peaks()
     assert p["hbm_gbs"] > 1000 and p["source"] in ("measured", "fallback")
+
+
+def test_side_measurement_failures_are_recorded():
+    """A failing side measurement of the default line is recorded as an
+    error in the line instead of ending the run."""
+    import bench
+
+    def fails(x):
+        raise RuntimeError(f"cannot {x}")
+
+    r = bench.guarded("side", fails, "render")
+    assert r == {"error": "RuntimeError: cannot render"}
+    assert bench.pick(r, ("a",)) == r
+    assert bench.pick({"a": 1, "b": 2}, ("a",)) == {"a": 1}
+    assert bench.guarded("side", lambda v: {"v": v}, 3) == {"v": 3}
