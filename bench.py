@@ -363,9 +363,10 @@ def run_pgx(args) -> dict:
     value = rays_all / (ms_max * 1e-3) / 1e6
 
     # The other half of the metric: throughput of the guided estimators on the
-    # same workload (each after its own untimed set-up: the radiance cache from
-    # a 1-spp guided-Li pass, or 16 frames of online training), and plain path
-    # tracing at the reference arm's fixed depth 8 for an equal-depth anchor.
+    # same workload (each after its own untimed set-up, prepare_mode: the
+    # QuadTree recipe's 8 + 16 training frames, or 16 frames of online
+    # training), and plain path tracing at the reference arm's fixed depth 8
+    # for an equal-depth anchor.
     # Same L2 flush and device timing as the steps above, fewer steps.
     side = {}
     if not args.no_side_modes:
@@ -508,8 +509,8 @@ def run_pgx(args) -> dict:
     # The other configurations, each a bounded run outside the timed steps so
     # that the line records them too: the plain box (16 spp, 256x256, depth
     # 8), incoherent secondary rays on the 2M-triangle interior (10^7 rays),
-    # and the adjoint on the 2M-triangle terrain (with a few finite
-    # differences).  Rank 0 of a single-GPU run only.
+    # the adjoint on the 2M-triangle terrain (with a few finite differences)
+    # and the 64-scene batch.  Rank 0 of a single-GPU run only.
     workloads = None
     if not args.no_workloads and ranks.world == 1 and args.workload == "interior" and not args.res:
         import copy
