@@ -223,7 +223,7 @@ def test_trained_guide_lowers_the_error(ctx):
     against a 4,096-spp plain render than (a) plain path tracing, (b) the
     same estimator with the untrained network, by the stated margins, and
     stays within 40 % of (c) the QuadTree guide trained on as many samples
-    (the judge).  Measured: plain 0.196, untrained 0.546, QuadTree
+    (the yardstick).  Measured: plain 0.196, untrained 0.546, QuadTree
     0.118-0.120, learned 0.110-0.130 over runs (the gradient sums use float
     atomics, so the trained network differs in its last bits from run to
     run).  relMSE = mean((x - r)^2 / (r^2 + 0.01)) over pixels, without the
